@@ -1,0 +1,364 @@
+"""Benchmark of the GB300 network RHS on the large-graph throughput workload.
+
+Workload: diffusion on a Barabási–Albert graph, N = 10,000,000 vertices, m = 4
+(E ≈ 4e7 edges, power-law hubs), e = w_ij (u_src - u_dst) with w ~ U(0,1), du = Σ e,
+u ~ N(0,1), seeded synthetic inputs.  One step = one RHS evaluation `nw(du, u, p, t)`.
+The headline line is FP64 (bitwise equal to the sequential reference order); the same
+JSON line carries the FP32 run (compensated sums at hubs), the end-to-end figure through
+the public API with host buffers, the HBM roofline of the RHS kernel, and the CPU
+baseline (the oracle restatement of SequentialExecution / PolyesterExecution).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Under torchrun every rank runs an independent replica (the single-graph RHS does not
+shard); value = edges processed by all ranks / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "networkdynamics.jl_gb300"))
+sys.path.insert(0, str(ROOT))
+
+METRIC = "RHS edges/s (% HBM peak) @10M-vertex"
+NV_DEFAULT = 10_000_000
+M_BA = 4
+SEED = 1
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nv", type=int, default=NV_DEFAULT, help="vertices (smaller for profiling captures)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-f32", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def algorithmic_bytes(nv, ne, s):
+    """Bytes one RHS must move at ideal caching: read u, write du, read p (w per edge),
+    read the CSR row pointers (4 B per vertex) and the incidences (nbr + eid, 8 B each)."""
+    return s * (nv + nv + ne) + 4 * (nv + 1) + 2 * ne * 8
+
+
+def peaks():
+    try:
+        d = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(dtype_tag, nv):
+    """DRAM bytes per launch from the committed ncu summary, if one exists for this workload."""
+    f = ROOT / "profiles" / f"rhs_ba{nv // 1_000_000}m_{dtype_tag}.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if len(s) > 2 and s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if len(s) > 2 and s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for k, name in enumerate(names):
+                if len(s) > 5 + k and s[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def make_workload(nv):
+    import nd_gb300 as nd
+    g = nd.barabasi_albert(nv, M_BA, seed=SEED)
+    rng = np.random.default_rng(SEED)
+    u = rng.normal(size=nv)
+    w = rng.uniform(0.0, 1.0, size=g.ne)
+    return g, u, w
+
+
+def dist_setup(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        if backend == "nccl":
+            import torch
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world, device=None):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(g, u, w, seconds=12.0):
+    """The oracle on the host cores: the PolyesterExecution restatement on all threads and
+    the SequentialExecution restatement on one, each on whole RHS evaluations."""
+    from oracle import oracle as O
+    on = O.OracleNetwork.from_graph(g, O.V_DIFFUSION, O.E_DIFFUSION)
+    res = {}
+    for name, fn, threads in (("poly", on.rhs_poly, os.cpu_count() or 1), ("seq", on.rhs, 1)):
+        O.load().nd_oracle_set_num_threads(threads)
+        fn(u, w)  # warm
+        n, t0 = 0, time.perf_counter()
+        while True:
+            fn(u, w)
+            n += 1
+            el = time.perf_counter() - t0
+            if el > seconds / 2 or n >= 50:
+                break
+        res[name] = (g.ne * n / el, n, threads, el)
+    O.load().nd_oracle_set_num_threads(os.cpu_count() or 1)
+    return res
+
+
+def run_reference(args, rank, world):
+    """CPU reference arm: the threaded oracle restatement (PolyesterExecution +
+    PolyesterAggregator) on all host cores, same workload and metric."""
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    g, u, w = make_workload(args.nv)
+    on = O.OracleNetwork.from_graph(g, O.V_DIFFUSION, O.E_DIFFUSION)
+    threads = os.cpu_count() or 1
+    O.load().nd_oracle_set_num_threads(threads)
+    for _ in range(min(args.warmup, 3)):
+        on.rhs_poly(u, w)
+    # each step is one full RHS; the number of timed steps is capped at ~60 s of CPU time
+    t0 = time.perf_counter()
+    on.rhs_poly(u, w)
+    one = time.perf_counter() - t0
+    steps = max(1, min(args.steps, int(60.0 / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        on.rhs_poly(u, w)
+    el = time.perf_counter() - t0
+    val = g.ne * steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "edges/s", "n_gpus": args.gpus,
+        "steps": steps, "warmup": min(args.warmup, 3), "ms_per_step": 1e3 * el / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"diffusion on Barabasi-Albert N={args.nv}, m={M_BA}, F64 RHS", "nv": args.nv,
+                   "ne": g.ne, "parallelism": "host threads"},
+        "cpu_baseline": {"value": val, "unit": "edges/s", "cores": threads, "kind": "port",
+                         "sample": f"{steps} full RHS evaluations (steps capped at ~60 s of CPU time) of the "
+                                   "PolyesterExecution+PolyesterAggregator restatement"},
+        "e2e": {"value": val, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def time_device(nw, du, u, p, steps, stream):
+    import torch
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(steps):
+        nw(du, u, p, 0.0, stream=stream)
+    stop.record(stream)
+    stop.synchronize()
+    return start.elapsed_time(stop) / 1e3
+
+
+def run_gb300(args, rank, world, local):
+    import torch
+
+    import nd_gb300 as nd
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    g, u_h, w_h = make_workload(args.nv)
+    nv, ne = g.nv, g.ne
+    stream = torch.cuda.current_stream(dev)
+    net = nd.Network(g, nd.diffusion_vertex(), nd.diffusion_edge())
+    nw = nd.adapt(net, torch.float64)
+    info = nw.info()
+    u = torch.from_numpy(u_h).to(dev)
+    p = torch.from_numpy(w_h).to(dev)
+    du = torch.empty_like(u)
+    for _ in range(max(args.warmup, 3)):
+        nw(du, u, p, 0.0)
+    torch.cuda.synchronize()
+    barrier(world)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        barrier(world)
+        t = time_device(nw, du, u, p, args.steps, stream)
+        torch.cuda.synchronize()
+        barrier(world)
+    t = max_over_ranks(t, world, dev)
+    ms = 1e3 * t / args.steps
+    value = world * ne * args.steps / t
+    hbm, peak_kind = peaks()
+    B = algorithmic_bytes(nv, ne, 8)
+    achieved = B / (t / args.steps) / 1e9
+    launches_per_step = (1 if info.n_hubs == 0 else 2) if nv - info.n_hubs > 0 else 1
+    traffic = profiled_traffic("f64", nv)
+    line = {
+        "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded BA graph, w~U(0,1), u~N(0,1))",
+        "config": {"workload": f"diffusion on Barabasi-Albert N={nv}, m={M_BA}, F64 RHS", "nv": nv, "ne": ne,
+                   "incidences": 2 * ne, "max_degree": info.max_degree, "hub_rows": info.n_hubs,
+                   "sum_order": "sequential (bitwise = SequentialAggregator)",
+                   "l2": "no flush: inputs+topology %.2f GB > 129 MB L2" % (B / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "edges_per_s": value, "incidences_per_s": 2 * value, "rhs_evals_per_s": world * args.steps / t,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic, "peak_kind": peak_kind,
+                     "note": "whole RHS (all launches of one step) timed with CUDA events; algorithmic "
+                             "bytes = 8(2N+E) + 4(N+1) + 16E"},
+        "gpu_launches": launches_per_step * args.steps,
+    }
+    # FP32 variant (compensated sums at hubs)
+    if not args.no_f32:
+        nw32 = nd.adapt(net, torch.float32)
+        u32, p32 = u.float(), p.float()
+        du32 = torch.empty_like(u32)
+        for _ in range(3):
+            nw32(du32, u32, p32, 0.0)
+        torch.cuda.synchronize()
+        t32 = time_device(nw32, du32, u32, p32, args.steps, stream)
+        t32 = max_over_ranks(t32, world, dev)
+        B32 = algorithmic_bytes(nv, ne, 4)
+        ref = torch.empty_like(u)
+        nw(ref, u, p, 0.0)
+        err = (du32.double() - ref).abs().max().item()
+        line["f32"] = {"value": world * ne * args.steps / t32, "unit": "edges/s", "ms_per_step": 1e3 * t32 / args.steps,
+                       "achieved_gbs": B32 / (t32 / args.steps) / 1e9,
+                       "frac": B32 / (t32 / args.steps) / 1e9 / hbm, "max_abs_err_vs_f64": err}
+        line["gpu_launches"] += launches_per_step * args.steps
+        del nw32, u32, p32, du32
+    # end to end through the public API with pinned host buffers
+    if not args.no_e2e:
+        ke = min(args.steps, 200)
+        uh = torch.from_numpy(u_h).pin_memory()
+        ph = torch.from_numpy(w_h).pin_memory()
+        duh = torch.empty(nv, dtype=torch.float64).pin_memory()
+        for _ in range(2):
+            u.copy_(uh, non_blocking=True)
+            p.copy_(ph, non_blocking=True)
+            nw(du, u, p, 0.0)
+            duh.copy_(du, non_blocking=True)
+        torch.cuda.synchronize()
+        barrier(world)
+        start = torch.cuda.Event(enable_timing=True)
+        stop = torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for _ in range(ke):
+            u.copy_(uh, non_blocking=True)
+            p.copy_(ph, non_blocking=True)
+            nw(du, u, p, 0.0)
+            duh.copy_(du, non_blocking=True)
+        stop.record(stream)
+        stop.synchronize()
+        te = max_over_ranks(start.elapsed_time(stop) / 1e3, world, dev)
+        line["e2e"] = {"value": world * ne * ke / te, "unit": "edges/s", "steps": ke,
+                       "h2d_bytes_per_step": int(uh.numel() * 8 + ph.numel() * 8),
+                       "d2h_bytes_per_step": int(duh.numel() * 8)}
+        line["gpu_launches"] += launches_per_step * ke
+        ok = np.array_equal(duh.numpy(), du.cpu().numpy())
+        line["e2e"]["result_matches_device"] = bool(ok)
+    line["clocks"] = clk.summary()
+    if rank == 0 and world == 1 and not args.no_cpu:
+        res = cpu_baseline(g, u_h, w_h)
+        v, n, thr, el = res["poly"]
+        line["cpu_baseline"] = {"value": v, "unit": "edges/s", "cores": thr, "kind": "port",
+                                "sample": f"{n} full RHS evaluations ({el:.1f} s) of the threaded "
+                                          "PolyesterExecution+PolyesterAggregator restatement"}
+        v1, n1, _, el1 = res["seq"]
+        line["cpu_baseline_sequential"] = {"value": v1, "unit": "edges/s", "cores": 1, "kind": "port",
+                                           "sample": f"{n1} full RHS evaluations ({el1:.1f} s) of the "
+                                                     "SequentialExecution+SequentialAggregator restatement"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gb300(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,140 @@
+/*
+ * nd_gb300.h — C ABI of libnd_b200.so, the GB300 (sm_103a) network right-hand side
+ * of NetworkDynamics.jl and the solvers built on it.
+ *
+ * Everything here is plain C: pointers, sizes and status codes, no CUDA or torch
+ * types in the signatures.  Device pointers are CUDA device addresses; `stream` is a
+ * cudaStream_t passed as void* (NULL = legacy default stream).  All calls that take a
+ * stream are stream-ordered: they enqueue work and return without synchronising,
+ * unless stated otherwise.
+ *
+ * Reference paths cited below are relative to the NetworkDynamics.jl source tree.
+ */
+#ifndef ND_GB300_H
+#define ND_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ND_VERSION 10000 /* 1.0.0 */
+
+/* ---------------------------------------------------------------------------------
+ * Status codes.  The reference raises Julia exceptions; the C ABI returns a code and
+ * keeps a thread-local message (nd_last_error).  The Julia shim maps ND_ERR_ARG and
+ * ND_ERR_DTYPE to ArgumentError (src/coreloop.jl:2-7, src/network_structure.jl:146-150),
+ * ND_ERR_UNSUPPORTED_COMPONENT to ArgumentError at construction, and
+ * ND_ERR_NOT_CONVERGED to NetworkInitError (src/initialization.jl:86-142).
+ * ------------------------------------------------------------------------------- */
+enum nd_status {
+    ND_OK = 0,
+    ND_ERR_ARG = -1,                   /* bad size, pointer or descriptor field            */
+    ND_ERR_UNSUPPORTED_COMPONENT = -2, /* component outside the hand-written library       */
+    ND_ERR_DTYPE = -3,                 /* buffer eltype differs from the handle precision  */
+    ND_ERR_CUDA = -4,                  /* a CUDA runtime call failed                       */
+    ND_ERR_MAXITERS = -5,              /* a solver hit its step / iteration budget         */
+    ND_ERR_UNSUPPORTED = -6,           /* feature outside the GB300 path (perturb, RET...) */
+    ND_ERR_NOMEM = -7,                 /* device allocation failed                         */
+    ND_ERR_NOT_CONVERGED = -8          /* Newton / fixpoint did not reach the tolerance    */
+};
+
+/* Element type of caller buffers.  A handle is built for one of them, like
+ * adapt(CuArray{Float32}/CuArray{Float64}, nw) (ext/NetworkDynamicsCUDAExt.jl:16-45). */
+enum nd_dtype { ND_F32 = 1, ND_F64 = 2 };
+
+/* Hand-written component library.  Anything else is rejected with
+ * ND_ERR_UNSUPPORTED_COMPONENT: there is no CPU fallback. */
+enum nd_vertex_kind {
+    ND_V_DIFFUSION = 1, /* diffusionvertex!  dv = Σe                 test/ComponentLibrary.jl:42-46   dim 1, pdim 0          */
+    ND_V_KURAMOTO = 2,  /* kuramoto_vertex!  dθ = ω + Σe             test/ComponentLibrary.jl:69-72   dim 1, pdim 1 (ω)      */
+    ND_V_SWING = 3      /* kuramoto_inertia! dθ = ω, dω = (Pm-Dω+Σe)/M test/ComponentLibrary.jl:59-67 dim 2, pdim 3 (M,D,Pm) */
+};
+enum nd_edge_kind {
+    ND_E_DIFFUSION = 1,      /* diffusionedge!   e = w·(vs-vd)   test/ComponentLibrary.jl:8-13   pdim 1 (w) */
+    ND_E_DIFFUSION_UNIT = 2, /* diffusion_edge!  e = vs-vd       test/diffusion_test.jl:57-60    pdim 0     */
+    ND_E_KURAMOTO = 3        /* kuramoto_edge! / static power line  e = K·sin(vs-vd)
+                                test/ComponentLibrary.jl:51-57, :96-115                          pdim 1 (K) */
+};
+/* Output wrapper of the edge (src/component_functions.jl:101-203).  The library edges are
+ * AntiSymmetric: y_dst = g(...), y_src = -y_dst. */
+enum nd_coupling { ND_ANTISYMMETRIC = 1 };
+
+/* Summation order of the per-vertex edge aggregation. */
+enum nd_sum_order {
+    ND_ORDER_SEQUENTIAL = 0, /* ascending out-buffer index, = SequentialAggregator (bitwise) */
+    ND_ORDER_TREE = 1        /* deterministic tree inside a warp at hubs (faster, not bitwise)  */
+};
+
+/* Network description, the information Network(g, vertexm, edgem) holds
+ * (src/construction.jl:31-236).  Edges are given in Graphs.jl `edges(g)` order with
+ * 0-based endpoints; edge k owns parameter slot k of the edge parameter block.  One
+ * homogeneous vertex batch and one homogeneous edge batch. */
+typedef struct nd_network_desc {
+    int64_t nv;          /* number of vertices                           */
+    int64_t ne;          /* number of edges                              */
+    const int64_t* src;  /* [ne] host pointer, 0-based source vertex      */
+    const int64_t* dst;  /* [ne] host pointer, 0-based destination vertex */
+    int32_t vertex_kind; /* enum nd_vertex_kind                          */
+    int32_t edge_kind;   /* enum nd_edge_kind                            */
+    int32_t coupling;    /* enum nd_coupling                             */
+    int32_t flags;       /* reserved, must be 0                          */
+} nd_network_desc;
+
+/* Sizes of the flat reference layout (src/network_structure.jl:224-289). */
+typedef struct nd_info {
+    int64_t dim;          /* lastidx_dynamic: length of u and du            */
+    int64_t pdim;         /* lastidx_p: length of p                         */
+    int64_t nv;           /* vertices                                       */
+    int64_t ne;           /* edges                                          */
+    int64_t n_incidences; /* 2·ne entries of the destination-sorted CSR     */
+    int32_t dtype;        /* enum nd_dtype of the handle                    */
+    int32_t vertex_kind;
+    int32_t edge_kind;
+    int32_t max_degree;
+    int32_t n_hubs;       /* vertices on the cooperative (warp / CTA) path   */
+    int32_t sum_order;    /* enum nd_sum_order in use                       */
+} nd_info;
+
+typedef struct nd_handle nd_handle;
+
+/* Library version (ND_VERSION). */
+int nd_version(void);
+
+/* Message of the last failing call on this host thread ("" if none). */
+const char* nd_last_error(void);
+
+/* Build a handle: validate the description, build the destination-sorted CSR with
+ * degree buckets and upload it.  Replaces the aggregator constructor call
+ * `aggregator(im, edgebatches)` (src/construction.jl:198) together with
+ * Adapt.adapt_structure(CuArray{T}, nw) (ext/NetworkDynamicsCUDAExt.jl:16-45).
+ * Uses the current CUDA device. */
+int nd_create(const nd_network_desc* desc, int dtype, nd_handle** out);
+
+/* Free the handle and its device buffers (the Julia finalizer calls this). */
+int nd_destroy(nd_handle* h);
+
+int nd_get_info(const nd_handle* h, nd_info* out);
+
+/* Select the aggregation order (enum nd_sum_order).  Default ND_ORDER_SEQUENTIAL. */
+int nd_set_sum_order(nd_handle* h, int order);
+
+/* One network right-hand side du = f(u, p, t), the method
+ * `(nw::Network)(du, u, p, t)` (src/coreloop.jl:1-102) for RET=:du and no perturbation,
+ * with SequentialAggregator(+) semantics (src/aggregators.jl:133-151).
+ *   dtype       element type of du/u/p; ND_ERR_DTYPE if it differs from the handle's
+ *               (src/network_structure.jl:146-150)
+ *   n_du, n_u   must equal info.dim, else ND_ERR_ARG (src/coreloop.jl:2-4)
+ *   n_p         must equal info.pdim when pdim > 0, else ND_ERR_ARG (src/coreloop.jl:5-7);
+ *               p may be NULL when pdim == 0
+ *   t           unused by the library components, may be NaN
+ * du, u, p are device pointers in the reference's flat order (no permutation). */
+int nd_rhs(nd_handle* h, int dtype, void* du, int64_t n_du, const void* u, int64_t n_u,
+           const void* p, int64_t n_p, double t, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ND_GB300_H */

@@ -1,0 +1,235 @@
+// C ABI of libnd_b200.so: handle life cycle, argument checks and the RHS entry point.
+//
+// Argument checks mirror the reference's: sizes of du/u/p (src/coreloop.jl:2-7), the
+// precision the caches were adapted to (src/network_structure.jl:145-151), and the
+// component library (anything else raises instead of falling back to the CPU).
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "nd_internal.h"
+
+namespace nd {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+void clear_error() { g_last_error.clear(); }
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+int cuda_fail(cudaError_t err, const char* what) {
+    std::string msg = std::string("CUDA error in ") + what + ": " + cudaGetErrorString(err);
+    g_last_error = msg;
+    return err == cudaErrorMemoryAllocation ? ND_ERR_NOMEM : ND_ERR_CUDA;
+}
+
+void free_topology(Topology* t) {
+    cudaFree(t->row_ptr);
+    cudaFree(t->incid);
+    cudaFree(t->light);
+    cudaFree(t->hubs);
+    *t = Topology{};
+}
+
+// Destination-sorted CSR.  Row v lists every edge incident to v in ascending edge id;
+// an edge that is a self loop appears twice, source side first.  This is the order in
+// which SequentialAggregator visits the output buffer (src/aggregators.jl:140-151 over
+// the map of src/aggregators.jl:58-79: out ranges are laid out per edge as src then dst,
+// src/network_structure.jl:240-250), so a sequential per-row sum reproduces it bitwise.
+int build_topology(int64_t nv, int64_t ne, const int64_t* src, const int64_t* dst, Topology* topo) {
+    if (nv <= 0) return fail(ND_ERR_ARG, "network has no vertices");
+    if (ne < 0) return fail(ND_ERR_ARG, "negative edge count");
+    if (nv > INT32_MAX - 1) return fail(ND_ERR_UNSUPPORTED, "more than 2^31-2 vertices");
+    if (ne > (int64_t)(INT32_MAX)) return fail(ND_ERR_UNSUPPORTED, "more than 2^31-1 edges");
+    if (2 * ne > (int64_t)UINT32_MAX) return fail(ND_ERR_UNSUPPORTED, "more than 2^32-1 incidences");
+    if (ne > 0 && (!src || !dst)) return fail(ND_ERR_ARG, "src/dst pointers are NULL");
+
+    std::vector<uint32_t> deg(nv + 1, 0);
+    for (int64_t e = 0; e < ne; ++e) {
+        int64_t s = src[e], d = dst[e];
+        if (s < 0 || s >= nv || d < 0 || d >= nv) {
+            char buf[160];
+            snprintf(buf, sizeof buf, "edge %lld has endpoint out of range (%lld => %lld, nv=%lld)",
+                     (long long)e, (long long)s, (long long)d, (long long)nv);
+            return fail(ND_ERR_ARG, buf);
+        }
+        deg[s]++;
+        deg[d]++;
+    }
+    std::vector<uint32_t> row_ptr(nv + 1);
+    row_ptr[0] = 0;
+    uint32_t maxdeg = 0;
+    for (int64_t v = 0; v < nv; ++v) {
+        row_ptr[v + 1] = row_ptr[v] + deg[v];
+        maxdeg = std::max(maxdeg, deg[v]);
+    }
+    std::vector<Incidence> incid((size_t)2 * ne);
+    std::vector<uint32_t> fill(row_ptr.begin(), row_ptr.end() - 1);
+    for (int64_t e = 0; e < ne; ++e) {
+        int32_t s = (int32_t)src[e], d = (int32_t)dst[e];
+        incid[fill[s]++] = Incidence{d, (int32_t)e | kSrcSideBit};  // s receives y_src
+        incid[fill[d]++] = Incidence{s, (int32_t)e};                // d receives y_dst
+    }
+    std::vector<int32_t> light, hubs;
+    light.reserve(nv);
+    for (int64_t v = 0; v < nv; ++v) {
+        if (deg[v] <= (uint32_t)kThreadMaxDeg) light.push_back((int32_t)v);
+        else hubs.push_back((int32_t)v);
+    }
+    std::stable_sort(hubs.begin(), hubs.end(), [&](int32_t a, int32_t b) { return deg[a] > deg[b]; });
+
+    Topology t;
+    t.nv = nv;
+    t.ne = ne;
+    t.max_degree = (int32_t)maxdeg;
+    t.n_light = (int32_t)light.size();
+    t.n_hubs = (int32_t)hubs.size();
+    auto upload = [&](void** dptr, const void* hptr, size_t bytes) -> cudaError_t {
+        cudaError_t err = cudaMalloc(dptr, std::max<size_t>(bytes, 16));
+        if (err != cudaSuccess) return err;
+        if (bytes) err = cudaMemcpy(*dptr, hptr, bytes, cudaMemcpyHostToDevice);
+        return err;
+    };
+    cudaError_t err;
+    if ((err = upload((void**)&t.row_ptr, row_ptr.data(), row_ptr.size() * sizeof(uint32_t))) != cudaSuccess ||
+        (err = upload((void**)&t.incid, incid.data(), incid.size() * sizeof(Incidence))) != cudaSuccess ||
+        (err = upload((void**)&t.light, light.data(), light.size() * sizeof(int32_t))) != cudaSuccess ||
+        (err = upload((void**)&t.hubs, hubs.data(), hubs.size() * sizeof(int32_t))) != cudaSuccess) {
+        free_topology(&t);
+        return cuda_fail(err, "upload of the network topology");
+    }
+    *topo = t;
+    return ND_OK;
+}
+
+}  // namespace nd
+
+using namespace nd;
+
+extern "C" {
+
+int nd_version(void) { return ND_VERSION; }
+
+const char* nd_last_error(void) { return g_last_error.c_str(); }
+
+int nd_create(const nd_network_desc* desc, int dtype, nd_handle** out) {
+    clear_error();
+    if (!desc || !out) return fail(ND_ERR_ARG, "nd_create: NULL descriptor or output pointer");
+    *out = nullptr;
+    if (dtype != ND_F32 && dtype != ND_F64)
+        return fail(ND_ERR_DTYPE, "nd_create: dtype must be ND_F32 or ND_F64 "
+                                  "(adapt the network with CuArray{Float32} or CuArray{Float64})");
+    if (desc->vertex_kind < ND_V_DIFFUSION || desc->vertex_kind > ND_V_SWING)
+        return fail(ND_ERR_UNSUPPORTED_COMPONENT,
+                    "vertex model is not in the GB300 component library "
+                    "(diffusion, kuramoto first order, swing); no CPU fallback exists");
+    if (desc->edge_kind < ND_E_DIFFUSION || desc->edge_kind > ND_E_KURAMOTO)
+        return fail(ND_ERR_UNSUPPORTED_COMPONENT,
+                    "edge model is not in the GB300 component library "
+                    "(diffusion, unit diffusion, kuramoto / static line); no CPU fallback exists");
+    if (desc->coupling != ND_ANTISYMMETRIC)
+        return fail(ND_ERR_UNSUPPORTED_COMPONENT, "only AntiSymmetric edge coupling is in the GB300 library");
+    if (desc->flags != 0) return fail(ND_ERR_ARG, "nd_network_desc.flags must be 0");
+
+    nd_handle* h = new nd_handle();
+    h->dtype = dtype;
+    h->vertex_kind = desc->vertex_kind;
+    h->edge_kind = desc->edge_kind;
+    h->coupling = desc->coupling;
+    h->sum_order = ND_ORDER_SEQUENTIAL;
+    h->kahan_min_degree = 64;
+    cudaGetDevice(&h->device);
+    h->dim = desc->nv * vertex_dim(desc->vertex_kind);
+    h->pdim = desc->nv * vertex_pdim(desc->vertex_kind) + desc->ne * edge_pdim(desc->edge_kind);
+    int rc = build_topology(desc->nv, desc->ne, desc->src, desc->dst, &h->topo);
+    if (rc != ND_OK) {
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return ND_OK;
+}
+
+int nd_destroy(nd_handle* h) {
+    clear_error();
+    if (!h) return ND_OK;
+    int prev = -1;
+    cudaGetDevice(&prev);
+    if (prev != h->device) cudaSetDevice(h->device);
+    free_topology(&h->topo);
+    if (prev >= 0 && prev != h->device) cudaSetDevice(prev);
+    delete h;
+    return ND_OK;
+}
+
+int nd_get_info(const nd_handle* h, nd_info* out) {
+    clear_error();
+    if (!h || !out) return fail(ND_ERR_ARG, "nd_get_info: NULL argument");
+    out->dim = h->dim;
+    out->pdim = h->pdim;
+    out->nv = h->topo.nv;
+    out->ne = h->topo.ne;
+    out->n_incidences = 2 * h->topo.ne;
+    out->dtype = h->dtype;
+    out->vertex_kind = h->vertex_kind;
+    out->edge_kind = h->edge_kind;
+    out->max_degree = h->topo.max_degree;
+    out->n_hubs = h->topo.n_hubs;
+    out->sum_order = h->sum_order;
+    return ND_OK;
+}
+
+int nd_set_sum_order(nd_handle* h, int order) {
+    clear_error();
+    if (!h) return fail(ND_ERR_ARG, "nd_set_sum_order: NULL handle");
+    if (order != ND_ORDER_SEQUENTIAL && order != ND_ORDER_TREE)
+        return fail(ND_ERR_ARG, "nd_set_sum_order: unknown order");
+    h->sum_order = order;
+    return ND_OK;
+}
+
+int nd_rhs(nd_handle* h, int dtype, void* du, int64_t n_du, const void* u, int64_t n_u, const void* p,
+           int64_t n_p, double t, void* stream) {
+    (void)t;
+    clear_error();
+    if (!h) return fail(ND_ERR_ARG, "nd_rhs: NULL handle");
+    if (dtype != h->dtype) {
+        const char* have = h->dtype == ND_F64 ? "Float64" : "Float32";
+        const char* got = dtype == ND_F64 ? "Float64" : (dtype == ND_F32 ? "Float32" : "an unknown type");
+        return fail(ND_ERR_DTYPE, std::string("Network caches are initialized with ") + have +
+                                      " but is used for " + got + " data");
+    }
+    if (n_du != h->dim || n_u != h->dim) {
+        return fail(ND_ERR_ARG, "du or u does not have expected size " + std::to_string(h->dim));
+    }
+    if (h->pdim > 0 && n_p != h->pdim) {
+        return fail(ND_ERR_ARG, "p does not has expected size " + std::to_string(h->pdim));
+    }
+    if (!du || !u || (h->pdim > 0 && !p)) return fail(ND_ERR_ARG, "nd_rhs: NULL buffer");
+    RhsArgs a;
+    a.du = du;
+    a.u = u;
+    a.p = p;
+    a.nv = h->topo.nv;
+    a.row_ptr = h->topo.row_ptr;
+    a.incid = h->topo.incid;
+    a.light = h->topo.light;
+    a.hubs = h->topo.hubs;
+    a.n_light = h->topo.n_light;
+    a.n_hubs = h->topo.n_hubs;
+    a.vertex_kind = h->vertex_kind;
+    a.edge_kind = h->edge_kind;
+    a.sum_order = h->sum_order;
+    a.kahan_min_degree = h->kahan_min_degree;
+    cudaError_t err = launch_rhs(h->dtype, a, (cudaStream_t)stream);
+    if (err != cudaSuccess) return cuda_fail(err, "nd_rhs kernel launch");
+    return ND_OK;
+}
+
+}  // extern "C"

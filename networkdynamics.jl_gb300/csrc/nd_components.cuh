@@ -1,0 +1,104 @@
+// Device-side component library: the vertex and edge functions of the benchmark models,
+// written with explicitly rounded operations (no FMA contraction) so that the FP64 results
+// equal the reference's plain Julia arithmetic operation by operation.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "nd_gb300.h"
+
+namespace nd {
+
+template <typename T>
+struct Arith;
+
+template <>
+struct Arith<double> {
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+    // FP64 keeps the raw phase difference, like the reference's sin(θs - θd).
+    static __device__ __forceinline__ double sin_phase(double x) { return sin(x); }
+    static __device__ __forceinline__ double cos_phase(double x) { return cos(x); }
+};
+
+// 2π split for a two-step Cody–Waite reduction of a phase difference to [-π, π].
+constexpr float kTwoPiHi = 6.28318548202514648f;      // nearest float to 2π
+constexpr float kTwoPiLo = -1.74845560984535e-07f;    // 2π - kTwoPiHi
+constexpr float kInvTwoPi = 0.159154943091895336f;
+constexpr float kPiF = 3.14159274101257324f;
+
+template <>
+struct Arith<float> {
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+    // FP32 wraps the phase difference to [-π, π] before sin/cos so that phases that have
+    // drifted far from zero do not lose the difference's digits in the argument reduction.
+    static __device__ __forceinline__ float wrap(float x) {
+        if (fabsf(x) > kPiF) {
+            float k = rintf(x * kInvTwoPi);
+            x = fmaf(-k, kTwoPiHi, x);
+            x = fmaf(-k, kTwoPiLo, x);
+        }
+        return x;
+    }
+    static __device__ __forceinline__ float sin_phase(float x) { return sinf(wrap(x)); }
+    static __device__ __forceinline__ float cos_phase(float x) { return cosf(wrap(x)); }
+};
+
+// y_dst of the single-sided edge function g(vs, vd, p) for edge e.
+template <typename T, int EK>
+__device__ __forceinline__ T edge_g(T vs, T vd, const T* __restrict__ pe, int32_t e) {
+    using A = Arith<T>;
+    if constexpr (EK == ND_E_DIFFUSION) {
+        return A::mul(__ldg(pe + e), A::sub(vs, vd));  // e .= p * (v_s[1] .- v_d[1])
+    } else if constexpr (EK == ND_E_DIFFUSION_UNIT) {
+        return A::sub(vs, vd);                         // e .= v_s .- v_d
+    } else {
+        return A::mul(__ldg(pe + e), A::sin_phase(A::sub(vs, vd)));  // e .= K .* sin(θs - θd)
+    }
+}
+
+// Contribution of one incidence to the aggregation at the row vertex (value uv).  The
+// AntiSymmetric wrapper evaluates g once per edge with the edge's own orientation and
+// hands -y_dst to the source (src/component_functions.jl:117-127), so the source side
+// negates g(uv, un) instead of evaluating g(un, uv).
+template <typename T, int EK>
+__device__ __forceinline__ T incidence_term(T uv, T un, const T* __restrict__ pe, int32_t eid_bits) {
+    const bool src_side = eid_bits < 0;
+    const int32_t e = eid_bits & 0x7fffffff;
+    const T vs = src_side ? uv : un;
+    const T vd = src_side ? un : uv;
+    const T y = edge_g<T, EK>(vs, vd, pe, e);
+    return src_side ? -y : y;
+}
+
+template <int VK>
+struct VertexDims {
+    static constexpr int dim = VK == ND_V_SWING ? 2 : 1;
+    static constexpr int pdim = VK == ND_V_DIFFUSION ? 0 : (VK == ND_V_KURAMOTO ? 1 : 3);
+};
+
+// Vertex f with the aggregated input `acc` (the reference's aggbuf entry).
+template <typename T, int VK>
+__device__ __forceinline__ void vertex_f(T* __restrict__ du, const T* __restrict__ u,
+                                         const T* __restrict__ pv, int64_t v, T acc) {
+    using A = Arith<T>;
+    if constexpr (VK == ND_V_DIFFUSION) {
+        du[v] = acc;  // dv[1] = acc[1]
+    } else if constexpr (VK == ND_V_KURAMOTO) {
+        du[v] = A::add(__ldg(pv + v), acc);  // dθ[1] = ω + esum[1]
+    } else {
+        const T w = u[2 * v + 1];
+        const T M = __ldg(pv + 3 * v), D = __ldg(pv + 3 * v + 1), Pm = __ldg(pv + 3 * v + 2);
+        du[2 * v] = w;  // dv[1] = v[2]
+        // dv[2] = 1 / M * (Pm - D * v[2] + acc[1])
+        du[2 * v + 1] = A::mul(A::div(T(1), M), A::add(A::sub(Pm, A::mul(D, w)), acc));
+    }
+}
+
+}  // namespace nd

@@ -1,0 +1,146 @@
+"""ctypes binding of libnd_b200.so (declarations in include/nd_gb300.h).
+
+The library is loaded from the package's ``lib/`` folder.  When it is missing the import
+of any GPU entry point raises: there is no CPU fallback for the GB300 path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+from ._build import CUDA_LIB, GRAPHGEN_LIB
+
+ND_OK = 0
+ND_ERR_ARG = -1
+ND_ERR_UNSUPPORTED_COMPONENT = -2
+ND_ERR_DTYPE = -3
+ND_ERR_CUDA = -4
+ND_ERR_MAXITERS = -5
+ND_ERR_UNSUPPORTED = -6
+ND_ERR_NOMEM = -7
+ND_ERR_NOT_CONVERGED = -8
+
+ND_F32 = 1
+ND_F64 = 2
+
+ND_V_DIFFUSION = 1
+ND_V_KURAMOTO = 2
+ND_V_SWING = 3
+
+ND_E_DIFFUSION = 1
+ND_E_DIFFUSION_UNIT = 2
+ND_E_KURAMOTO = 3
+
+ND_ANTISYMMETRIC = 1
+
+ND_ORDER_SEQUENTIAL = 0
+ND_ORDER_TREE = 1
+
+
+class NDError(RuntimeError):
+    """A failing libnd_b200 call; ``code`` is the nd_status value."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class ArgumentError(NDError, ValueError):
+    """Counterpart of Julia's ArgumentError raised by the reference for the same inputs."""
+
+
+class UnsupportedComponentError(ArgumentError):
+    pass
+
+
+class NotConvergedError(NDError):
+    """Counterpart of the reference's NetworkInitError."""
+
+
+class nd_network_desc(C.Structure):
+    _fields_ = [("nv", C.c_int64), ("ne", C.c_int64),
+                ("src", C.POINTER(C.c_int64)), ("dst", C.POINTER(C.c_int64)),
+                ("vertex_kind", C.c_int32), ("edge_kind", C.c_int32),
+                ("coupling", C.c_int32), ("flags", C.c_int32)]
+
+
+class nd_info(C.Structure):
+    _fields_ = [("dim", C.c_int64), ("pdim", C.c_int64), ("nv", C.c_int64), ("ne", C.c_int64),
+                ("n_incidences", C.c_int64), ("dtype", C.c_int32), ("vertex_kind", C.c_int32),
+                ("edge_kind", C.c_int32), ("max_degree", C.c_int32), ("n_hubs", C.c_int32),
+                ("sum_order", C.c_int32)]
+
+
+# Every symbol include/nd_gb300.h declares, with (restype, argtypes).
+SIGNATURES = {
+    "nd_version": (C.c_int, []),
+    "nd_last_error": (C.c_char_p, []),
+    "nd_create": (C.c_int, [C.POINTER(nd_network_desc), C.c_int, C.POINTER(C.c_void_p)]),
+    "nd_destroy": (C.c_int, [C.c_void_p]),
+    "nd_get_info": (C.c_int, [C.c_void_p, C.POINTER(nd_info)]),
+    "nd_set_sum_order": (C.c_int, [C.c_void_p, C.c_int]),
+    "nd_rhs": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
+                         C.c_void_p, C.c_int64, C.c_double, C.c_void_p]),
+}
+
+_lib = None
+_graphgen = None
+
+
+def library_path() -> Path:
+    return CUDA_LIB
+
+
+def load(path: Path | None = None):
+    """Load libnd_b200.so (once) and attach the signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else CUDA_LIB
+    if not p.exists():
+        raise ImportError(f"{p} is missing: build it first (__graft_entry__.build()); "
+                          "the GB300 path has no CPU fallback")
+    lib = C.CDLL(str(p), mode=C.RTLD_GLOBAL)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def last_error() -> str:
+    msg = load().nd_last_error()
+    return msg.decode() if msg else ""
+
+
+def check(code: int) -> int:
+    if code == ND_OK:
+        return code
+    msg = last_error()
+    if code == ND_ERR_UNSUPPORTED_COMPONENT:
+        raise UnsupportedComponentError(code, msg)
+    if code in (ND_ERR_ARG, ND_ERR_DTYPE, ND_ERR_UNSUPPORTED):
+        raise ArgumentError(code, msg)
+    if code in (ND_ERR_NOT_CONVERGED, ND_ERR_MAXITERS):
+        raise NotConvergedError(code, msg)
+    raise NDError(code, msg)
+
+
+def load_graphgen():
+    global _graphgen
+    if _graphgen is not None:
+        return _graphgen
+    if not GRAPHGEN_LIB.exists():
+        raise ImportError(f"{GRAPHGEN_LIB} is missing: build it first (__graft_entry__.build())")
+    lib = C.CDLL(str(GRAPHGEN_LIB))
+    P = C.POINTER(C.c_int64)
+    lib.nd_gen_watts_strogatz.restype = C.c_int64
+    lib.nd_gen_watts_strogatz.argtypes = [C.c_int64, C.c_int64, C.c_double, C.c_uint64, P, P, C.c_int64]
+    lib.nd_gen_barabasi_albert.restype = C.c_int64
+    lib.nd_gen_barabasi_albert.argtypes = [C.c_int64, C.c_int64, C.c_uint64, P, P, C.c_int64]
+    lib.nd_gen_random_geometric.restype = C.c_int64
+    lib.nd_gen_random_geometric.argtypes = [C.c_int64, C.c_double, C.c_uint64, P, P, C.c_int64,
+                                            C.POINTER(C.c_double)]
+    _graphgen = lib
+    return lib

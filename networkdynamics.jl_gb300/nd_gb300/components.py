@@ -1,0 +1,96 @@
+"""Component models of the GB300 library.
+
+Mirrors the reference's ``VertexModel``/``EdgeModel`` (src/component_functions.jl:251,306)
+for the components the benchmarks use (test/ComponentLibrary.jl).  Each library
+component carries a ``kind`` naming its hand-written CUDA implementation.  A model built
+from a user function (``VertexModel(f=..., g=...)``) has no kind, and a GB300 network
+that contains one is rejected at construction: the GB300 path never falls back to the
+CPU.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Callable, Optional, Sequence
+
+from . import _capi as capi
+
+
+@dataclass
+class VertexModel:
+    name: str
+    dim: int
+    pdim: int
+    sym: Sequence[str] = ()
+    psym: Sequence[str] = ()
+    pdef: Sequence[Optional[float]] = ()
+    kind: Optional[int] = None          # ND_V_* of the CUDA implementation, None = user function
+    f: Optional[Callable] = None
+    g: object = 1                       # StateMask(1): the first state is the output
+
+    @property
+    def outdim(self) -> int:
+        return 1
+
+
+@dataclass
+class EdgeModel:
+    name: str
+    pdim: int
+    psym: Sequence[str] = ()
+    pdef: Sequence[Optional[float]] = ()
+    kind: Optional[int] = None          # ND_E_* of the CUDA implementation, None = user function
+    coupling: str = "AntiSymmetric"
+    dim: int = 0                        # static edges: no states
+    f: Optional[Callable] = None
+    g: Optional[Callable] = None
+
+    @property
+    def outdim(self) -> int:
+        return 1
+
+
+# --- vertices (test/ComponentLibrary.jl) -------------------------------------------------
+
+def diffusion_vertex() -> VertexModel:
+    """diffusionvertex!: dv = Σ e   (test/ComponentLibrary.jl:42-46)."""
+    return VertexModel("diffusion_vertex", dim=1, pdim=0, sym=("v",), kind=capi.ND_V_DIFFUSION)
+
+
+def kuramoto_first() -> VertexModel:
+    """kuramoto_vertex!: dθ = ω + Σ e   (test/ComponentLibrary.jl:69-72)."""
+    return VertexModel("kuramoto_first", dim=1, pdim=1, sym=("θ",), psym=("ω",), pdef=(None,),
+                       kind=capi.ND_V_KURAMOTO)
+
+
+def kuramoto_second() -> VertexModel:
+    """kuramoto_inertia! (swing): dδ = ω, dω = 1/M (Pm - D ω + Σ e)   (test/ComponentLibrary.jl:59-67)."""
+    return VertexModel("kuramoto_second", dim=2, pdim=3, sym=("δ", "ω"), psym=("M", "D", "Pm"),
+                       pdef=(1.0, 0.1, 1.0), kind=capi.ND_V_SWING)
+
+
+swing_vertex = kuramoto_second
+
+
+# --- edges ------------------------------------------------------------------------------
+
+def diffusion_edge() -> EdgeModel:
+    """diffusionedge!: e = p (v_s - v_d), AntiSymmetric   (test/ComponentLibrary.jl:8-13)."""
+    return EdgeModel("diff_edge", pdim=1, psym=("p",), pdef=(1.0,), kind=capi.ND_E_DIFFUSION)
+
+
+def diffusion_edge_unit() -> EdgeModel:
+    """diffusion_edge!: e = v_s - v_d, AntiSymmetric   (test/diffusion_test.jl:57-60, 71)."""
+    return EdgeModel("diff_edge_unit", pdim=0, kind=capi.ND_E_DIFFUSION_UNIT)
+
+
+def kuramoto_edge() -> EdgeModel:
+    """kuramoto_edge!: e = K sin(θ_s - θ_d), AntiSymmetric   (test/ComponentLibrary.jl:51-57)."""
+    return EdgeModel("kuramoto_edge", pdim=1, psym=("K",), pdef=(None,), kind=capi.ND_E_KURAMOTO)
+
+
+def static_line() -> EdgeModel:
+    """Static power line P = K sin(θ_src - θ_dst) (line_mtk with active = 1,
+    test/ComponentLibrary.jl:96-115); the same function as kuramoto_edge."""
+    m = kuramoto_edge()
+    m.name = "static_line"
+    return m

@@ -1,0 +1,441 @@
+/*
+ * ORACLE — test infrastructure, not product code.
+ *
+ * CPU restatement of NetworkDynamics.jl's network right-hand side for the component
+ * library of the GB300 path, written to follow the reference operation by operation:
+ *
+ *   nd_oracle_rhs_*        (nw::Network)(du,u,p,t) with SequentialExecution +
+ *                          SequentialAggregator(+)     src/coreloop.jl:1-102
+ *   nd_oracle_rhs_poly_*   the same with PolyesterExecution + PolyesterAggregator(+):
+ *                          component loops and the inverse aggregation map run on
+ *                          OpenMP threads              src/coreloop.jl:131-139,
+ *                                                      src/aggregators.jl:159-177,203-235
+ *   nd_oracle_tsit5        Tsit5 (Tsitouras 2011, the published tableau) with a PI step
+ *                          controller, driving the sequential RHS
+ *
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline load this library,
+ * as the checker.  Compile with -ffp-contract=off: the reference performs no fused
+ * multiply-adds in these functions, so neither may the restatement.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* Component kinds: same numbering as the C ABI of the GB300 library. */
+enum { V_DIFFUSION = 1, V_KURAMOTO = 2, V_SWING = 3 };
+enum { E_DIFFUSION = 1, E_DIFFUSION_UNIT = 2, E_KURAMOTO = 3 };
+
+static int vdim(int vk) { return vk == V_SWING ? 2 : 1; }
+static int vpdim(int vk) { return vk == V_DIFFUSION ? 0 : (vk == V_KURAMOTO ? 1 : 3); }
+static int epdim(int ek) { return ek == E_DIFFUSION_UNIT ? 0 : 1; }
+
+/*
+ * Index layout of src/network_structure.jl:224-289, built as src/construction.jl:155-195
+ * does: components are batched by identity in order of first appearance
+ * (find_identical, src/utils.jl:197-216), all vertex batches are registered before the
+ * edge batches, and every edge owns an output range for src followed by one for dst.
+ * vdepth = edepth = 1 (StateMask(1) vertex outputs, scalar edge outputs).
+ */
+typedef struct {
+    int64_t nv, ne;
+    const int64_t* src;
+    const int64_t* dst;
+    const int32_t* vkind; /* [nv] */
+    const int32_t* ekind; /* [ne] */
+    /* layout, 0-based offsets */
+    int64_t* v_data; /* first state index of vertex */
+    int64_t* v_out;  /* output index */
+    int64_t* v_para; /* first parameter index */
+    int64_t* v_aggr; /* aggregation index */
+    int64_t* e_out_src;
+    int64_t* e_out_dst;
+    int64_t* e_para;
+    int64_t* vbatch_order; /* vertices in batch (processing) order */
+    int64_t* ebatch_order; /* edges in batch (processing) order */
+    int64_t lastidx_dynamic, lastidx_out, lastidx_p, lastidx_aggr;
+    int64_t agg_first, agg_len; /* tightened aggregation range of the output buffer */
+    int64_t* agg_map;           /* [agg_len] output index -> aggregation index + 1, 0 = skip */
+    /* inverse map for the Polyester aggregator: per aggregation index, its output indices */
+    int64_t* inv_ptr;
+    int64_t* inv_idx;
+} layout_t;
+
+/* Batch order: kinds in order of first appearance, indices ascending inside a batch. */
+static void batch_order(int64_t n, const int32_t* kind, int64_t* order) {
+    int32_t seen[16];
+    int nseen = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        int found = 0;
+        for (int j = 0; j < nseen; ++j)
+            if (seen[j] == kind[i]) found = 1;
+        if (!found && nseen < 16) seen[nseen++] = kind[i];
+    }
+    int64_t pos = 0;
+    for (int j = 0; j < nseen; ++j)
+        for (int64_t i = 0; i < n; ++i)
+            if (kind[i] == seen[j]) order[pos++] = i;
+}
+
+void nd_oracle_layout_free(layout_t* L);
+
+layout_t* nd_oracle_layout_new(int64_t nv, int64_t ne, const int64_t* src, const int64_t* dst,
+                               const int32_t* vkind, const int32_t* ekind) {
+    layout_t* L = (layout_t*)calloc(1, sizeof(layout_t));
+    L->nv = nv;
+    L->ne = ne;
+    L->src = src;
+    L->dst = dst;
+    L->vkind = vkind;
+    L->ekind = ekind;
+    L->v_data = (int64_t*)malloc(sizeof(int64_t) * (nv + 1));
+    L->v_out = (int64_t*)malloc(sizeof(int64_t) * (nv + 1));
+    L->v_para = (int64_t*)malloc(sizeof(int64_t) * (nv + 1));
+    L->v_aggr = (int64_t*)malloc(sizeof(int64_t) * (nv + 1));
+    L->e_out_src = (int64_t*)malloc(sizeof(int64_t) * (ne + 1));
+    L->e_out_dst = (int64_t*)malloc(sizeof(int64_t) * (ne + 1));
+    L->e_para = (int64_t*)malloc(sizeof(int64_t) * (ne + 1));
+    L->vbatch_order = (int64_t*)malloc(sizeof(int64_t) * (nv + 1));
+    L->ebatch_order = (int64_t*)malloc(sizeof(int64_t) * (ne + 1));
+    batch_order(nv, vkind, L->vbatch_order);
+    batch_order(ne, ekind, L->ebatch_order);
+    int64_t dyn = 0, out = 0, par = 0, agg = 0;
+    for (int64_t k = 0; k < nv; ++k) { /* register_vertices! */
+        int64_t v = L->vbatch_order[k];
+        L->v_data[v] = dyn;
+        dyn += vdim(vkind[v]);
+        L->v_out[v] = out;
+        out += 1;
+        L->v_para[v] = par;
+        par += vpdim(vkind[v]);
+        L->v_aggr[v] = agg;
+        agg += 1;
+    }
+    for (int64_t k = 0; k < ne; ++k) { /* register_edges!: static edges have no states */
+        int64_t e = L->ebatch_order[k];
+        L->e_out_src[e] = out;
+        out += 1;
+        L->e_out_dst[e] = out;
+        out += 1;
+        L->e_para[e] = par;
+        par += epdim(ekind[e]);
+    }
+    L->lastidx_dynamic = dyn;
+    L->lastidx_out = out;
+    L->lastidx_p = par;
+    L->lastidx_aggr = agg;
+    /* AggregationMap (src/aggregators.jl:58-86): map[out index] = aggr index, tightened. */
+    int64_t* full = (int64_t*)calloc((size_t)out + 1, sizeof(int64_t));
+    for (int64_t k = 0; k < ne; ++k) {
+        int64_t e = L->ebatch_order[k];
+        full[L->e_out_dst[e]] = L->v_aggr[dst[e]] + 1;
+        full[L->e_out_src[e]] = L->v_aggr[src[e]] + 1;
+    }
+    int64_t first = -1, last = -1;
+    for (int64_t i = 0; i < out; ++i)
+        if (full[i]) {
+            if (first < 0) first = i;
+            last = i;
+        }
+    if (first < 0) {
+        L->agg_first = 0;
+        L->agg_len = 0;
+        L->agg_map = (int64_t*)malloc(sizeof(int64_t));
+    } else {
+        L->agg_first = first;
+        L->agg_len = last - first + 1;
+        L->agg_map = (int64_t*)malloc(sizeof(int64_t) * (size_t)L->agg_len);
+        memcpy(L->agg_map, full + first, sizeof(int64_t) * (size_t)L->agg_len);
+    }
+    free(full);
+    /* _inv_aggregation_map (src/aggregators.jl:203-235): per vertex, its incident output
+     * indices in edge-batch order, dst mapping before src mapping within an edge. */
+    L->inv_ptr = (int64_t*)calloc((size_t)agg + 1, sizeof(int64_t));
+    L->inv_idx = (int64_t*)malloc(sizeof(int64_t) * (size_t)(2 * ne + 1));
+    for (int64_t e = 0; e < ne; ++e) {
+        L->inv_ptr[L->v_aggr[dst[e]] + 1]++;
+        L->inv_ptr[L->v_aggr[src[e]] + 1]++;
+    }
+    for (int64_t a = 0; a < agg; ++a) L->inv_ptr[a + 1] += L->inv_ptr[a];
+    int64_t* fill = (int64_t*)malloc(sizeof(int64_t) * ((size_t)agg + 1));
+    memcpy(fill, L->inv_ptr, sizeof(int64_t) * ((size_t)agg + 1));
+    for (int64_t k = 0; k < ne; ++k) {
+        int64_t e = L->ebatch_order[k];
+        L->inv_idx[fill[L->v_aggr[dst[e]]]++] = L->e_out_dst[e];
+        L->inv_idx[fill[L->v_aggr[src[e]]]++] = L->e_out_src[e];
+    }
+    free(fill);
+    return L;
+}
+
+void nd_oracle_layout_free(layout_t* L) {
+    if (!L) return;
+    free(L->v_data);
+    free(L->v_out);
+    free(L->v_para);
+    free(L->v_aggr);
+    free(L->e_out_src);
+    free(L->e_out_dst);
+    free(L->e_para);
+    free(L->vbatch_order);
+    free(L->ebatch_order);
+    free(L->agg_map);
+    free(L->inv_ptr);
+    free(L->inv_idx);
+    free(L);
+}
+
+int64_t nd_oracle_dim(const layout_t* L) { return L->lastidx_dynamic; }
+int64_t nd_oracle_pdim(const layout_t* L) { return L->lastidx_p; }
+int64_t nd_oracle_v_data(const layout_t* L, int64_t v) { return L->v_data[v]; }
+int64_t nd_oracle_v_para(const layout_t* L, int64_t v) { return L->v_para[v]; }
+int64_t nd_oracle_e_para(const layout_t* L, int64_t e) { return L->e_para[e]; }
+
+/*
+ * The RHS, once per precision.  Steps and line references follow src/coreloop.jl.
+ * Workspace o (lastidx_out) and aggbuf (lastidx_aggr) are caller-provided.
+ *
+ * Component functions (test/ComponentLibrary.jl):
+ *   diffusionedge!   e = p * (v_s - v_d)                 :8-13
+ *   diffusion_edge!  e = v_s - v_d                       test/diffusion_test.jl:57-60
+ *   kuramoto_edge!   e = K * sin(θ_s - θ_d)              :51-57
+ *   AntiSymmetric    y_src = -y_dst                      src/component_functions.jl:117-127
+ *   diffusionvertex! dv = acc                            :42-46
+ *   kuramoto_vertex! dθ = ω + esum                       :69-72
+ *   kuramoto_inertia! dv1 = v2; dv2 = 1/M*(Pm - D*v2 + acc)  :59-67
+ */
+#define DEFINE_ORACLE_RHS(T, SFX, SIN)                                                              \
+    static inline T edge_g_##SFX(int ek, T vs, T vd, const T* pe) {                                \
+        if (ek == E_DIFFUSION) return pe[0] * (vs - vd);                                            \
+        if (ek == E_DIFFUSION_UNIT) return vs - vd;                                                 \
+        return pe[0] * SIN(vs - vd);                                                                \
+    }                                                                                               \
+    static inline void vertex_f_##SFX(int vk, T* du, const T* u, const T* pv, T acc) {             \
+        if (vk == V_DIFFUSION) {                                                                    \
+            du[0] = acc;                                                                            \
+        } else if (vk == V_KURAMOTO) {                                                              \
+            du[0] = pv[0] + acc;                                                                    \
+        } else {                                                                                    \
+            T M = pv[0], D = pv[1], Pm = pv[2];                                                     \
+            du[0] = u[1];                                                                           \
+            du[1] = (T)1 / M * (Pm - D * u[1] + acc);                                               \
+        }                                                                                           \
+    }                                                                                               \
+    static void edges_g_##SFX(const layout_t* L, T* o, const T* p, int64_t k) {                    \
+        int64_t e = L->ebatch_order[k];                                                             \
+        T vs = o[L->v_out[L->src[e]]], vd = o[L->v_out[L->dst[e]]];                                 \
+        T y = edge_g_##SFX(L->ekind[e], vs, vd, p + L->e_para[e]);                                  \
+        o[L->e_out_dst[e]] = y;                                                                     \
+        o[L->e_out_src[e]] = -y;                                                                    \
+    }                                                                                               \
+    void nd_oracle_rhs_##SFX(const layout_t* L, T* du, const T* u, const T* p, T* o, T* aggbuf) {   \
+        int64_t i;                                                                                  \
+        for (i = 0; i < L->lastidx_dynamic; ++i) du[i] = 0;       /* fill!(du, 0)      :24 */       \
+        for (i = 0; i < L->lastidx_out; ++i) o[i] = (T)NAN;       /* fill!(o, NaN)  ns:153 */       \
+        for (i = 0; i < L->lastidx_aggr; ++i) aggbuf[i] = 0;      /* fill!(aggbuf, 0)  :30 */       \
+        for (int64_t k = 0; k < L->nv; ++k) {                     /* vertex g, StateMask :39 */     \
+            int64_t v = L->vbatch_order[k];                                                         \
+            o[L->v_out[v]] = u[L->v_data[v]];                                                       \
+        }                                                                                           \
+        /* static edges are PureFeedForward: g with f&g pass, :76-78; lazy gather :67 */            \
+        for (int64_t k = 0; k < L->ne; ++k) edges_g_##SFX(L, o, p, k);                              \
+        /* SequentialAggregator: walk the tightened output range in index order :90 */              \
+        for (int64_t j = 0; j < L->agg_len; ++j) {                                                  \
+            int64_t m = L->agg_map[j];                                                              \
+            if (m != 0) aggbuf[m - 1] = aggbuf[m - 1] + o[L->agg_first + j];                        \
+        }                                                                                           \
+        for (int64_t k = 0; k < L->nv; ++k) {                     /* vertex f :97 */                \
+            int64_t v = L->vbatch_order[k];                                                         \
+            vertex_f_##SFX(L->vkind[v], du + L->v_data[v], u + L->v_data[v], p + L->v_para[v],      \
+                           aggbuf[L->v_aggr[v]]);                                                   \
+        }                                                                                           \
+    }                                                                                               \
+    void nd_oracle_rhs_poly_##SFX(const layout_t* L, T* du, const T* u, const T* p, T* o,           \
+                                  T* aggbuf) {                                                      \
+        int64_t i;                                                                                  \
+        _Pragma("omp parallel for schedule(static)") for (i = 0; i < L->lastidx_dynamic; ++i) du[i] = 0; \
+        _Pragma("omp parallel for schedule(static)") for (i = 0; i < L->lastidx_aggr; ++i) aggbuf[i] = 0; \
+        _Pragma("omp parallel for schedule(static)") for (i = 0; i < L->nv; ++i) {                 \
+            int64_t v = L->vbatch_order[i];                                                         \
+            o[L->v_out[v]] = u[L->v_data[v]];                                                       \
+        }                                                                                           \
+        _Pragma("omp parallel for schedule(static)") for (i = 0; i < L->ne; ++i)                   \
+            edges_g_##SFX(L, o, p, i);                                                              \
+        _Pragma("omp parallel for schedule(static)") for (i = 0; i < L->lastidx_aggr; ++i) {       \
+            T acc = aggbuf[i];                                                                      \
+            for (int64_t q = L->inv_ptr[i]; q < L->inv_ptr[i + 1]; ++q) acc = acc + o[L->inv_idx[q]]; \
+            aggbuf[i] = acc;                                                                        \
+        }                                                                                           \
+        _Pragma("omp parallel for schedule(static)") for (i = 0; i < L->nv; ++i) {                 \
+            int64_t v = L->vbatch_order[i];                                                         \
+            vertex_f_##SFX(L->vkind[v], du + L->v_data[v], u + L->v_data[v], p + L->v_para[v],      \
+                           aggbuf[L->v_aggr[v]]);                                                   \
+        }                                                                                           \
+    }
+
+DEFINE_ORACLE_RHS(double, f64, sin)
+DEFINE_ORACLE_RHS(float, f32, sinf)
+
+int nd_oracle_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void nd_oracle_set_num_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+/*
+ * Tsit5 — Tsitouras, "Runge–Kutta pairs of order 5(4) satisfying only the first column
+ * simplifying assumption", Comput. Math. Appl. 62 (2011) 770-775: the published 7-stage
+ * FSAL tableau (b equals the last row of a) and the embedded error weights btilde.
+ * Step control: RMS norm of err_i / (abstol + reltol * max(|u_i|, |u_new_i|)), a PI
+ * controller with beta1 = 7/50, beta2 = 2/25, safety 9/10, step ratio clamped to
+ * [1/10, 5] (as q in [1/5, 10]), and the Hairer–Wanner initial step.  The reference
+ * delegates all of this to OrdinaryDiffEqTsit5 (solve(prob, Tsit5()),
+ * test/diffusion_test.jl:119-120); the controller constants restate that solver's
+ * documented defaults.
+ */
+static const double TS_C[7] = {0.0, 0.161, 0.327, 0.9, 0.9800255409045097, 1.0, 1.0};
+static const double TS_A[7][6] = {
+    {0, 0, 0, 0, 0, 0},
+    {0.161, 0, 0, 0, 0, 0},
+    {-0.008480655492356989, 0.335480655492357, 0, 0, 0, 0},
+    {2.897153057105493, -6.359448489975075, 4.3622954328695815, 0, 0, 0},
+    {5.325864828439257, -11.748883564062828, 7.4955393428898365, -0.09249506636175525, 0, 0},
+    {5.86145544294642, -12.92096931784711, 8.159367898576159, -0.071584973281401, -0.028269050394068383, 0},
+    {0.09646076681806523, 0.01, 0.4798896504144996, 1.379008574103742, -3.290069515436081, 2.324710524099774}};
+static const double TS_BTILDE[7] = {-0.00178001105222577714, -0.0008164344596567469, 0.007880878010261995,
+                                    -0.1447110071732629,     0.5823571654525552,     -0.45808210592918697,
+                                    0.015151515151515152};
+
+void nd_oracle_tsit5_tableau(double* c, double* a, double* btilde) {
+    for (int i = 0; i < 7; ++i) {
+        c[i] = TS_C[i];
+        btilde[i] = TS_BTILDE[i];
+        for (int j = 0; j < 6; ++j) a[i * 6 + j] = TS_A[i][j];
+    }
+}
+
+typedef struct {
+    int64_t naccept, nreject, nf;
+    double t_final, dt_last;
+    int status; /* 0 ok, -5 max steps, -8 dt underflow */
+} tsit5_stats_t;
+
+static double rms_scaled(int64_t n, const double* e, const double* u0, const double* u1, double abstol,
+                         double reltol) {
+    double s = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        double sc = abstol + reltol * fmax(fabs(u0[i]), fabs(u1[i]));
+        double r = e[i] / sc;
+        s += r * r;
+    }
+    return sqrt(s / (double)(n > 0 ? n : 1));
+}
+
+int nd_oracle_tsit5(const layout_t* L, double* u, const double* p, double t0, double t1, double reltol,
+                    double abstol, int64_t maxsteps, tsit5_stats_t* st) {
+    int64_t n = L->lastidx_dynamic;
+    double* k[7];
+    for (int i = 0; i < 7; ++i) k[i] = (double*)malloc(sizeof(double) * (size_t)(n + 1));
+    double* y = (double*)malloc(sizeof(double) * (size_t)(n + 1));
+    double* un = (double*)malloc(sizeof(double) * (size_t)(n + 1));
+    double* err = (double*)malloc(sizeof(double) * (size_t)(n + 1));
+    double* o = (double*)malloc(sizeof(double) * (size_t)(L->lastidx_out + 1));
+    double* ab = (double*)malloc(sizeof(double) * (size_t)(L->lastidx_aggr + 1));
+    memset(st, 0, sizeof(*st));
+    double t = t0, tdir = t1 >= t0 ? 1.0 : -1.0;
+    nd_oracle_rhs_f64(L, k[0], u, p, o, ab);
+    st->nf++;
+    /* Hairer–Wanner initial step (order 5). */
+    double d0 = 0, d1 = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        double sc = abstol + fabs(u[i]) * reltol;
+        d0 += (u[i] / sc) * (u[i] / sc);
+        d1 += (k[0][i] / sc) * (k[0][i] / sc);
+    }
+    d0 = sqrt(d0 / (double)(n ? n : 1));
+    d1 = sqrt(d1 / (double)(n ? n : 1));
+    double h0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
+    h0 = fmin(h0, fabs(t1 - t0));
+    for (int64_t i = 0; i < n; ++i) y[i] = u[i] + tdir * h0 * k[0][i];
+    nd_oracle_rhs_f64(L, k[1], y, p, o, ab);
+    st->nf++;
+    double d2 = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        double sc = abstol + fabs(u[i]) * reltol;
+        double r = (k[1][i] - k[0][i]) / sc;
+        d2 += r * r;
+    }
+    d2 = sqrt(d2 / (double)(n ? n : 1)) / h0;
+    double h1 = (fmax(d1, d2) <= 1e-15) ? fmax(1e-6, h0 * 1e-3) : pow(0.01 / fmax(d1, d2), 1.0 / 5.0);
+    double dt = fmin(fmin(100 * h0, h1), fabs(t1 - t0));
+    const double beta1 = 7.0 / 50.0, beta2 = 2.0 / 25.0, gamma = 0.9, qmin = 0.2, qmax = 10.0;
+    double qold = 1e-4;
+    int64_t steps = 0;
+    int status = 0;
+    while (tdir * (t1 - t) > 0) {
+        if (steps++ >= maxsteps) {
+            status = -5;
+            break;
+        }
+        if (fabs(t1 - t) < dt * (1 + 1e-12)) dt = fabs(t1 - t);
+        double h = tdir * dt;
+        for (int s = 1; s < 7; ++s) {
+            for (int64_t i = 0; i < n; ++i) {
+                double acc = 0;
+                for (int j = 0; j < s; ++j) acc += TS_A[s][j] * k[j][i];
+                y[i] = u[i] + h * acc;
+            }
+            nd_oracle_rhs_f64(L, k[s], y, p, o, ab);
+            st->nf++;
+            if (s == 6) memcpy(un, y, sizeof(double) * (size_t)n);
+        }
+        for (int64_t i = 0; i < n; ++i) {
+            double acc = 0;
+            for (int j = 0; j < 7; ++j) acc += TS_BTILDE[j] * k[j][i];
+            err[i] = h * acc;
+        }
+        double EEst = rms_scaled(n, err, u, un, abstol, reltol);
+        if (!(EEst == EEst)) EEst = 1e10; /* NaN: reject */
+        double q11 = pow(EEst, beta1);
+        if (EEst <= 1.0) {
+            double q = q11 / pow(qold, beta2);
+            q = fmax(1.0 / qmax, fmin(1.0 / qmin, q / gamma));
+            t = (fabs(t1 - t - h) <= 1e-14 * fmax(1.0, fabs(t1))) ? t1 : t + h;
+            memcpy(u, un, sizeof(double) * (size_t)n);
+            memcpy(k[0], k[6], sizeof(double) * (size_t)n); /* FSAL */
+            qold = fmax(EEst, 1e-4);
+            st->naccept++;
+            dt = dt / q;
+        } else {
+            st->nreject++;
+            dt = dt / fmin(1.0 / qmin, q11 / gamma);
+        }
+        if (dt < 1e-14 * fmax(1.0, fabs(t))) {
+            status = -8;
+            break;
+        }
+    }
+    st->t_final = t;
+    st->dt_last = dt;
+    st->status = status;
+    for (int i = 0; i < 7; ++i) free(k[i]);
+    free(y);
+    free(un);
+    free(err);
+    free(o);
+    free(ab);
+    return status;
+}

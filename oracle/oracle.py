@@ -1,0 +1,266 @@
+"""ORACLE — test infrastructure, not product code.
+
+Python side of the CPU oracle:
+
+* ``OracleNetwork``   — ctypes wrapper of oracle/nd_oracle.c (the C restatement of the
+  reference RHS, src/coreloop.jl:1-102 with src/aggregators.jl:133-151), its threaded
+  Polyester restatement, and the CPU Tsit5.
+* ``rhs_numpy``       — an independent numpy mirror of the same RHS for small cases.  It
+  uses ``np.add.at``, which applies the additions in index order, to reproduce
+  SequentialAggregator's order.
+* ``newton_fixpoint`` — dense Newton on the swing/Kuramoto steady state, the restated
+  find_fixpoint (src/initialization.jl:44-144) for small networks.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline use this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "nd_oracle.c"
+BUILD_DIR = HERE / "_build"
+LIB = BUILD_DIR / "liboracle.so"
+
+V_DIFFUSION, V_KURAMOTO, V_SWING = 1, 2, 3
+E_DIFFUSION, E_DIFFUSION_UNIT, E_KURAMOTO = 1, 2, 3
+
+VDIM = {V_DIFFUSION: 1, V_KURAMOTO: 1, V_SWING: 2}
+VPDIM = {V_DIFFUSION: 0, V_KURAMOTO: 1, V_SWING: 3}
+EPDIM = {E_DIFFUSION: 1, E_DIFFUSION_UNIT: 0, E_KURAMOTO: 1}
+
+
+def build_oracle(force: bool = False) -> Path:
+    """Compile the C restatement (no FMA contraction, OpenMP for the threaded variant)."""
+    BUILD_DIR.mkdir(exist_ok=True)
+    if not force and LIB.exists() and LIB.stat().st_mtime >= SRC.stat().st_mtime:
+        return LIB
+    tmp = LIB.with_suffix(".so.tmp")
+    cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp", str(SRC),
+           "-o", str(tmp), "-lm"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+class Tsit5Stats(C.Structure):
+    _fields_ = [("naccept", C.c_int64), ("nreject", C.c_int64), ("nf", C.c_int64),
+                ("t_final", C.c_double), ("dt_last", C.c_double), ("status", C.c_int)]
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        build_oracle()
+        lib = C.CDLL(str(LIB))
+        vp, i64 = C.c_void_p, C.c_int64
+        P64 = C.POINTER(C.c_int64)
+        P32 = C.POINTER(C.c_int32)
+        lib.nd_oracle_layout_new.restype = vp
+        lib.nd_oracle_layout_new.argtypes = [i64, i64, P64, P64, P32, P32]
+        lib.nd_oracle_layout_free.argtypes = [vp]
+        for fn in ("nd_oracle_dim", "nd_oracle_pdim"):
+            getattr(lib, fn).restype = i64
+            getattr(lib, fn).argtypes = [vp]
+        for fn in ("nd_oracle_v_data", "nd_oracle_v_para", "nd_oracle_e_para"):
+            getattr(lib, fn).restype = i64
+            getattr(lib, fn).argtypes = [vp, i64]
+        for fn in ("nd_oracle_rhs_f64", "nd_oracle_rhs_f32", "nd_oracle_rhs_poly_f64", "nd_oracle_rhs_poly_f32"):
+            getattr(lib, fn).restype = None
+            getattr(lib, fn).argtypes = [vp, vp, vp, vp, vp, vp]
+        lib.nd_oracle_num_threads.restype = C.c_int
+        lib.nd_oracle_set_num_threads.argtypes = [C.c_int]
+        lib.nd_oracle_tsit5.restype = C.c_int
+        lib.nd_oracle_tsit5.argtypes = [vp, vp, vp, C.c_double, C.c_double, C.c_double, C.c_double, i64,
+                                        C.POINTER(Tsit5Stats)]
+        lib.nd_oracle_tsit5_tableau.argtypes = [vp, vp, vp]
+        _lib = lib
+    return _lib
+
+
+def tsit5_tableau():
+    lib = load()
+    c = np.zeros(7)
+    a = np.zeros((7, 6))
+    bt = np.zeros(7)
+    lib.nd_oracle_tsit5_tableau(c.ctypes.data, a.ctypes.data, bt.ctypes.data)
+    return c, a, bt
+
+
+def _ptr(x):
+    return x.ctypes.data if x is not None and x.size else None
+
+
+class OracleNetwork:
+    """Reference layout + sequential RHS for a graph (0-based src/dst in edges(g) order).
+    ``vkind``/``ekind`` are scalars (one batch) or per-vertex / per-edge arrays."""
+
+    def __init__(self, nv, src, dst, vkind, ekind):
+        self.lib = load()
+        self.nv = int(nv)
+        self.src = np.ascontiguousarray(src, dtype=np.int64)
+        self.dst = np.ascontiguousarray(dst, dtype=np.int64)
+        self.ne = int(self.src.shape[0])
+        self.vkind = np.ascontiguousarray(np.broadcast_to(np.asarray(vkind, dtype=np.int32), (self.nv,)))
+        self.ekind = np.ascontiguousarray(np.broadcast_to(np.asarray(ekind, dtype=np.int32), (self.ne,)))
+        P64 = C.POINTER(C.c_int64)
+        P32 = C.POINTER(C.c_int32)
+        self.L = self.lib.nd_oracle_layout_new(self.nv, self.ne, self.src.ctypes.data_as(P64),
+                                               self.dst.ctypes.data_as(P64), self.vkind.ctypes.data_as(P32),
+                                               self.ekind.ctypes.data_as(P32))
+        self.dim = int(self.lib.nd_oracle_dim(self.L))
+        self.pdim = int(self.lib.nd_oracle_pdim(self.L))
+        self.n_out = self.nv + 2 * self.ne
+
+    @classmethod
+    def from_graph(cls, g, vkind, ekind):
+        return cls(g.nv, g.src, g.dst, vkind, ekind)
+
+    def __del__(self):
+        if getattr(self, "L", None):
+            self.lib.nd_oracle_layout_free(self.L)
+            self.L = None
+
+    def _rhs(self, fn, dtype, u, p):
+        u = np.ascontiguousarray(u, dtype=dtype)
+        p = np.ascontiguousarray(p if p is not None else np.zeros(0), dtype=dtype)
+        assert u.shape == (self.dim,) and p.shape == (self.pdim,)
+        du = np.empty(self.dim, dtype=dtype)
+        o = np.empty(self.n_out + 1, dtype=dtype)
+        ab = np.empty(self.nv + 1, dtype=dtype)
+        fn(self.L, du.ctypes.data, u.ctypes.data, _ptr(p), o.ctypes.data, ab.ctypes.data)
+        return du
+
+    def rhs(self, u, p, dtype=np.float64):
+        fn = self.lib.nd_oracle_rhs_f64 if dtype == np.float64 else self.lib.nd_oracle_rhs_f32
+        return self._rhs(fn, dtype, u, p)
+
+    def rhs_poly(self, u, p, dtype=np.float64):
+        fn = self.lib.nd_oracle_rhs_poly_f64 if dtype == np.float64 else self.lib.nd_oracle_rhs_poly_f32
+        return self._rhs(fn, dtype, u, p)
+
+    def tsit5(self, u0, p, t0, t1, reltol=1e-8, abstol=1e-10, maxsteps=10_000_000):
+        u = np.array(u0, dtype=np.float64, copy=True)
+        p = np.ascontiguousarray(p if p is not None else np.zeros(0), dtype=np.float64)
+        st = Tsit5Stats()
+        self.lib.nd_oracle_tsit5(self.L, u.ctypes.data, _ptr(p), t0, t1, reltol, abstol, maxsteps, C.byref(st))
+        return u, st
+
+    def abs_terms(self, u, p):
+        """Σ|terms| per state entry of du: the scale against which rounding differences
+        of a reordered sum are bounded (used for tolerance reporting)."""
+        uo = np.asarray(u, dtype=np.float64)
+        p = np.asarray(p if p is not None else np.zeros(0), dtype=np.float64)
+        vk = int(self.vkind[0])
+        ek = int(self.ekind[0]) if self.ne else E_DIFFUSION_UNIT
+        dv = VDIM[vk]
+        th = uo[::dv] if dv > 1 else uo
+        vs, vd = th[self.src], th[self.dst]
+        pe = p[self.nv * VPDIM[vk]:]
+        if ek == E_DIFFUSION:
+            y = pe * (vs - vd)
+        elif ek == E_DIFFUSION_UNIT:
+            y = vs - vd
+        else:
+            y = pe * np.sin(vs - vd)
+        s = np.zeros(self.nv)
+        np.add.at(s, self.src, np.abs(y))
+        np.add.at(s, self.dst, np.abs(y))
+        out = np.zeros(self.dim)
+        if vk == V_SWING:
+            pv = p[:3 * self.nv].reshape(-1, 3)
+            out[1::2] = (s + np.abs(pv[:, 2]) + np.abs(pv[:, 1] * uo[1::2])) / np.abs(pv[:, 0])
+            out[0::2] = np.abs(uo[1::2])
+        elif vk == V_KURAMOTO:
+            out[:] = s + np.abs(p[:self.nv])
+        else:
+            out[:] = s
+        return out
+
+
+def rhs_numpy(nv, src, dst, vk, ek, u, p, dtype=np.float64):
+    """Independent numpy restatement of the sequential RHS for one homogeneous batch."""
+    src = np.asarray(src, dtype=np.int64)
+    dst = np.asarray(dst, dtype=np.int64)
+    ne = src.shape[0]
+    u = np.asarray(u, dtype=dtype)
+    p = np.asarray(p if p is not None else np.zeros(0), dtype=dtype)
+    dv, pv = VDIM[vk], VPDIM[vk]
+    o_v = u[::dv].copy()                              # vertex g: StateMask(1)
+    vs, vd = o_v[src], o_v[dst]
+    pe = p[nv * pv:]
+    if ek == E_DIFFUSION:
+        y = pe * (vs - vd)
+    elif ek == E_DIFFUSION_UNIT:
+        y = vs - vd
+    else:
+        y = pe * (np.sin(vs - vd) if dtype == np.float64 else np.sin(vs - vd).astype(dtype))
+    # output buffer order per edge: src slot, then dst slot (AntiSymmetric: y_src = -y_dst)
+    vals = np.empty(2 * ne, dtype=dtype)
+    vals[0::2] = -y
+    vals[1::2] = y
+    targets = np.empty(2 * ne, dtype=np.int64)
+    targets[0::2] = src
+    targets[1::2] = dst
+    agg = np.zeros(nv, dtype=dtype)
+    np.add.at(agg, targets, vals)                     # SequentialAggregator order
+    du = np.zeros(nv * dv, dtype=dtype)
+    if vk == V_DIFFUSION:
+        du[:] = agg
+    elif vk == V_KURAMOTO:
+        du[:] = p[:nv] + agg
+    else:
+        P = p[:3 * nv].reshape(-1, 3)
+        M, D, Pm = P[:, 0], P[:, 1], P[:, 2]
+        w = u[1::2]
+        du[0::2] = w
+        du[1::2] = dtype(1) / M * (Pm - D * w + agg)
+    return du
+
+
+def swing_residual_theta(theta, src, dst, K, P):
+    """Power balance P_i + Σ_in K sin(θ_src-θ_dst) (with AntiSymmetric signs) at ω = 0."""
+    y = K * np.sin(theta[src] - theta[dst])
+    r = P.copy()
+    np.add.at(r, dst, y)
+    np.add.at(r, src, -y)
+    return r
+
+
+def newton_fixpoint(nv, src, dst, K, P, theta0=None, tol=1e-10, maxiter=50):
+    """Dense Newton on the swing / first-order Kuramoto steady state with ω = 0.
+
+    The state is θ; the Jacobian of the power balance is a weighted graph Laplacian with
+    weights K cos(θ_src - θ_dst), singular along the uniform phase shift, so θ_0 is pinned
+    (the gauge).  Returns (θ, iterations, final max-norm residual)."""
+    src = np.asarray(src)
+    dst = np.asarray(dst)
+    th = np.zeros(nv) if theta0 is None else np.array(theta0, dtype=np.float64)
+    th = th - th[0]
+    it = 0
+    res = np.max(np.abs(swing_residual_theta(th, src, dst, K, P)))
+    while res > tol and it < maxiter:
+        w = K * np.cos(th[src] - th[dst])
+        J = np.zeros((nv, nv))
+        # r_dst += K sin(θs-θd): ∂/∂θs = w, ∂/∂θd = -w ; r_src -= ...: ∂/∂θs = -w, ∂/∂θd = w
+        np.add.at(J, (dst, src), w)
+        np.add.at(J, (dst, dst), -w)
+        np.add.at(J, (src, src), -w)
+        np.add.at(J, (src, dst), w)
+        r = swing_residual_theta(th, src, dst, K, P)
+        delta = np.zeros(nv)
+        delta[1:] = np.linalg.solve(J[1:, 1:], -r[1:])
+        th = th + delta
+        it += 1
+        res = np.max(np.abs(swing_residual_theta(th, src, dst, K, P)))
+    return th, it, res

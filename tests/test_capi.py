@@ -1,0 +1,79 @@
+"""The C ABI library loads, exports every declared symbol, and rejects bad descriptors
+before any device work (no GPU needed for these)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import nd_gb300 as nd
+from nd_gb300 import _capi as capi
+
+HEADER_DIR = Path(__file__).resolve().parent.parent / "include"
+
+
+def declared_symbols():
+    names = set()
+    for h in HEADER_DIR.glob("*.h"):
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names |= set(re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*(nd_[a-z_0-9]+)\s*\(", text, flags=re.M))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = capi.load()
+    names = declared_symbols()
+    assert "nd_rhs" in names and "nd_create" in names
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, f"symbols declared in include/*.h but not exported: {missing}"
+    assert set(capi.SIGNATURES) >= names, "ctypes signature table misses declared symbols"
+
+
+def test_version_and_error_string():
+    lib = capi.load()
+    assert lib.nd_version() == 10000
+    assert isinstance(capi.last_error(), str)
+
+
+def _desc(g, vk, ek, coupling=capi.ND_ANTISYMMETRIC, flags=0):
+    src = np.ascontiguousarray(g.src)
+    dst = np.ascontiguousarray(g.dst)
+    P = C.POINTER(C.c_int64)
+    d = capi.nd_network_desc(g.nv, g.ne, src.ctypes.data_as(P), dst.ctypes.data_as(P), vk, ek, coupling, flags)
+    return d, (src, dst)
+
+
+@pytest.mark.parametrize("vk,ek,code", [
+    (0, capi.ND_E_DIFFUSION, capi.ND_ERR_UNSUPPORTED_COMPONENT),
+    (capi.ND_V_SWING, 9, capi.ND_ERR_UNSUPPORTED_COMPONENT),
+    (7, 7, capi.ND_ERR_UNSUPPORTED_COMPONENT),
+])
+def test_create_rejects_unknown_components(vk, ek, code):
+    lib = capi.load()
+    g = nd.cycle_graph(5)
+    d, _keep = _desc(g, vk, ek)
+    h = C.c_void_p()
+    assert lib.nd_create(C.byref(d), capi.ND_F64, C.byref(h)) == code
+    assert "library" in capi.last_error()
+    assert not h.value
+
+
+def test_create_rejects_bad_dtype_and_coupling():
+    lib = capi.load()
+    g = nd.cycle_graph(5)
+    d, _keep = _desc(g, capi.ND_V_DIFFUSION, capi.ND_E_DIFFUSION)
+    h = C.c_void_p()
+    assert lib.nd_create(C.byref(d), 3, C.byref(h)) == capi.ND_ERR_DTYPE
+    d2, _keep2 = _desc(g, capi.ND_V_DIFFUSION, capi.ND_E_DIFFUSION, coupling=2)
+    assert lib.nd_create(C.byref(d2), capi.ND_F64, C.byref(h)) == capi.ND_ERR_UNSUPPORTED_COMPONENT
+    assert lib.nd_create(None, capi.ND_F64, C.byref(h)) == capi.ND_ERR_ARG
+
+
+def test_null_handle_calls_fail_cleanly():
+    lib = capi.load()
+    assert lib.nd_rhs(None, capi.ND_F64, None, 0, None, 0, None, 0, 0.0, None) == capi.ND_ERR_ARG
+    assert lib.nd_destroy(None) == capi.ND_OK
+    info = capi.nd_info()
+    assert lib.nd_get_info(None, C.byref(info)) == capi.ND_ERR_ARG

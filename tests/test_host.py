@@ -1,0 +1,87 @@
+"""Host-side logic of the GB300 Network mirror: layout sizes, component checks, graph
+generators.  No GPU needed."""
+import operator
+
+import numpy as np
+import pytest
+
+import nd_gb300 as nd
+
+
+def test_layout_sizes_match_reference_layout():
+    g = nd.barabasi_albert(100, 2, seed=1)
+    nw = nd.Network(g, nd.kuramoto_second(), nd.static_line())
+    assert nw.dim == 200
+    assert nw.pdim == 3 * 100 + g.ne
+    assert nw.edge_param_index(0) == 300
+    nw1 = nd.Network(g, nd.diffusion_vertex(), nd.diffusion_edge_unit())
+    assert nw1.dim == 100 and nw1.pdim == 0
+
+
+def test_pflat_defaults_and_overrides():
+    g = nd.cycle_graph(4)
+    nw = nd.Network(g, nd.kuramoto_second(), nd.static_line())
+    p = nw.pflat(vertex={"Pm": np.array([1.0, -1.0, 1.0, -1.0])}, edge={"K": 6.0})
+    np.testing.assert_array_equal(p[:12].reshape(4, 3), [[1, .1, 1], [1, .1, -1], [1, .1, 1], [1, .1, -1]])
+    np.testing.assert_array_equal(p[12:], 6.0)
+    with pytest.raises(nd.ArgumentError):
+        nd.Network(g, nd.kuramoto_first(), nd.kuramoto_edge()).pflat()  # ω and K have no default
+
+
+def test_unsupported_component_raises_no_fallback():
+    g = nd.cycle_graph(4)
+    user_vertex = nd.VertexModel("my_vertex", dim=1, pdim=0, f=lambda *a: None)
+    with pytest.raises(nd.UnsupportedComponentError):
+        nd.Network(g, user_vertex, nd.diffusion_edge())
+    mixed = [nd.kuramoto_first(), nd.kuramoto_second(), nd.kuramoto_first(), nd.kuramoto_second()]
+    with pytest.raises(nd.UnsupportedComponentError):
+        nd.Network(g, mixed, nd.kuramoto_edge())
+
+
+def test_aggregator_only_plus():
+    assert nd.GB300Aggregator(operator.add).f is operator.add
+    with pytest.raises(nd.ArgumentError):
+        nd.GB300Aggregator(operator.mul)
+    a = nd.GB300Aggregator("+")
+    assert isinstance(nd.get_aggr_constructor(a), nd.GB300Aggregator)
+    assert nd.iscudacompatible(nd.GB300Execution()) and nd.iscudacompatible(a)
+
+
+def _is_edges_order(g):
+    assert np.all(g.src < g.dst)
+    key = g.src * (g.nv + 1) + g.dst
+    assert np.all(np.diff(key) > 0)
+
+
+def test_generators_edge_order_and_sizes():
+    ba = nd.barabasi_albert(2000, 4, seed=5)
+    assert ba.ne == 4 * (2000 - 4)
+    _is_edges_order(ba)
+    ws = nd.watts_strogatz(1000, 10, 0.1, seed=1)
+    assert ws.ne == 5000
+    _is_edges_order(ws)
+    assert ws.degree().min() >= 1
+    rgg, xy = nd.random_geometric(500, 0.1, seed=3, return_positions=True)
+    _is_edges_order(rgg)
+    d = np.linalg.norm(xy[rgg.src] - xy[rgg.dst], axis=1)
+    assert np.all(d < 0.1)
+    # brute force: every pair closer than r is an edge
+    diff = xy[:, None, :] - xy[None, :, :]
+    close = (diff ** 2).sum(-1) < 0.01
+    assert close[np.triu_indices(500, 1)].sum() == rgg.ne
+
+
+def test_generators_are_deterministic():
+    a = nd.barabasi_albert(5000, 3, seed=9)
+    b = nd.barabasi_albert(5000, 3, seed=9)
+    c = nd.barabasi_albert(5000, 3, seed=10)
+    np.testing.assert_array_equal(a.src, b.src)
+    np.testing.assert_array_equal(a.dst, b.dst)
+    assert not np.array_equal(a.dst, c.dst)
+
+
+def test_ba_is_power_law_with_hubs():
+    g = nd.barabasi_albert(200_000, 4, seed=1)
+    deg = g.degree()
+    assert deg.min() == 4
+    assert deg.max() > 300  # hubs well beyond the thread-per-vertex bucket

@@ -1,0 +1,193 @@
+"""Parity of the GB300 RHS (through the C ABI) with the CPU oracle.
+
+Bars: FP64 diffusion is bitwise equal to SequentialExecution + SequentialAggregator
+(same operations, same order, no FMA).  FP64 Kuramoto / swing differ only through the
+sine (CUDA's vs libm's, each within 1 ulp): every entry must satisfy
+|Δ| <= 1e-13 · |du| or, where the sum cancels, |Δ| <= 1e-13 · Σ|terms|.
+FP32 is compared with the FP64 oracle: |Δ| <= 4e-6 · (Σ|terms| + |du|).
+"""
+import zlib
+
+import numpy as np
+import pytest
+
+import nd_gb300 as nd
+from oracle import oracle as O
+
+from ndtest import exact_rows, gpu_rhs, random_inputs
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = __import__("pathlib").Path(__file__).resolve().parent / "golden"
+
+MODELS = {
+    (O.V_DIFFUSION, O.E_DIFFUSION): (nd.diffusion_vertex, nd.diffusion_edge),
+    (O.V_DIFFUSION, O.E_DIFFUSION_UNIT): (nd.diffusion_vertex, nd.diffusion_edge_unit),
+    (O.V_KURAMOTO, O.E_KURAMOTO): (nd.kuramoto_first, nd.kuramoto_edge),
+    (O.V_KURAMOTO, O.E_DIFFUSION): (nd.kuramoto_first, nd.diffusion_edge),
+    (O.V_SWING, O.E_KURAMOTO): (nd.kuramoto_second, nd.static_line),
+    (O.V_SWING, O.E_DIFFUSION): (nd.kuramoto_second, nd.diffusion_edge),
+    (O.V_DIFFUSION, O.E_KURAMOTO): (nd.diffusion_vertex, nd.kuramoto_edge),
+}
+
+GRAPHS = {
+    "ws1000": lambda: nd.watts_strogatz(1000, 10, 0.1, seed=1),
+    "ba20k_m3": lambda: nd.barabasi_albert(20_000, 3, seed=2),
+    "ba100k_m2": lambda: nd.barabasi_albert(100_000, 2, seed=3),
+}
+
+
+def make(g, vk, ek, dtype):
+    import torch
+    vm, em = MODELS[(vk, ek)]
+    return nd.adapt(nd.Network(g, vm(), em()), torch.float64 if dtype == np.float64 else torch.float32)
+
+
+def check_f64(got, ref, terms, exact):
+    if exact:
+        np.testing.assert_array_equal(got, ref)
+        return
+    d = np.abs(got - ref)
+    ok = (d <= 1e-13 * np.abs(ref)) | (d <= 1e-13 * terms)
+    assert ok.all(), f"{(~ok).sum()} entries off; worst {d[~ok].max():.3e}"
+
+
+@pytest.mark.parametrize("gname", list(GRAPHS))
+@pytest.mark.parametrize("vk,ek", list(MODELS))
+def test_f64_parity(cuda, gname, vk, ek):
+    g = GRAPHS[gname]()
+    nw = make(g, vk, ek, np.float64)
+    on = O.OracleNetwork.from_graph(g, vk, ek)
+    rng = np.random.default_rng(zlib.crc32(f"{gname}-{vk}-{ek}".encode()))
+    u, p = random_inputs(on, vk, rng)
+    ref = on.rhs(u, p)
+    got = gpu_rhs(nw, u, p, cuda, np.float64)
+    exact = ek != O.E_KURAMOTO
+    check_f64(got, ref, on.abs_terms(u, p), exact)
+
+
+@pytest.mark.parametrize("gname", ["ws1000", "ba100k_m2"])
+@pytest.mark.parametrize("vk,ek", [(O.V_DIFFUSION, O.E_DIFFUSION), (O.V_KURAMOTO, O.E_KURAMOTO),
+                                   (O.V_SWING, O.E_KURAMOTO)])
+def test_f32_against_f64_oracle(cuda, gname, vk, ek):
+    g = GRAPHS[gname]()
+    nw = make(g, vk, ek, np.float32)
+    on = O.OracleNetwork.from_graph(g, vk, ek)
+    u, p = random_inputs(on, vk, np.random.default_rng(5))
+    u32, p32 = u.astype(np.float32), p.astype(np.float32)
+    ref = on.rhs(u32.astype(np.float64), p32.astype(np.float64))
+    got = gpu_rhs(nw, u32, p32, cuda, np.float32).astype(np.float64)
+    terms = on.abs_terms(u32.astype(np.float64), p32.astype(np.float64))
+    bound = 4e-6 * (terms + np.abs(ref))
+    assert np.all(np.abs(got - ref) <= bound), np.max(np.abs(got - ref) / bound)
+
+
+def test_tree_order_is_deterministic_and_close(cuda):
+    g = nd.barabasi_albert(50_000, 4, seed=11)
+    nw = make(g, O.V_DIFFUSION, O.E_DIFFUSION, np.float64)
+    nw.set_sum_order("tree")
+    on = O.OracleNetwork.from_graph(g, O.V_DIFFUSION, O.E_DIFFUSION)
+    u, p = random_inputs(on, O.V_DIFFUSION, np.random.default_rng(1))
+    ref = on.rhs(u, p)
+    runs = [gpu_rhs(nw, u, p, cuda, np.float64) for _ in range(5)]
+    for r in runs[1:]:
+        np.testing.assert_array_equal(r, runs[0])
+    d = np.abs(runs[0] - ref)
+    assert np.all(d <= 1e-13 * on.abs_terms(u, p))
+    assert nw.info().sum_order == 1
+
+
+def test_sequential_is_deterministic(cuda):
+    g = nd.barabasi_albert(50_000, 4, seed=12)
+    nw = make(g, O.V_KURAMOTO, O.E_KURAMOTO, np.float64)
+    on = O.OracleNetwork.from_graph(g, O.V_KURAMOTO, O.E_KURAMOTO)
+    u, p = random_inputs(on, O.V_KURAMOTO, np.random.default_rng(2))
+    first = gpu_rhs(nw, u, p, cuda, np.float64)
+    for _ in range(9):
+        np.testing.assert_array_equal(gpu_rhs(nw, u, p, cuda, np.float64), first)
+
+
+def test_golden_fixtures_on_gpu(cuda):
+    d = np.load(GOLDEN / "diffusion_ba10_5.npz")
+    g = nd.Graph(int(d["nv"]), d["src"], d["dst"])
+    nw = make(g, O.V_DIFFUSION, O.E_DIFFUSION_UNIT, np.float64)
+    for x, du in zip(d["x"], d["du"]):
+        np.testing.assert_array_equal(gpu_rhs(nw, x, None, cuda, np.float64), du)
+    d = np.load(GOLDEN / "kuramoto_ws1000.npz")
+    g = nd.Graph(int(d["nv"]), d["src"], d["dst"])
+    nw = make(g, O.V_KURAMOTO, O.E_KURAMOTO, np.float64)
+    got = gpu_rhs(nw, d["u"], d["p"], cuda, np.float64)
+    on = O.OracleNetwork.from_graph(g, O.V_KURAMOTO, O.E_KURAMOTO)
+    check_f64(got, d["du"], on.abs_terms(d["u"], d["p"]), exact=False)
+    d = np.load(GOLDEN / "swing_ba200.npz")
+    g = nd.Graph(int(d["nv"]), d["src"], d["dst"])
+    nw = make(g, O.V_SWING, O.E_KURAMOTO, np.float64)
+    on = O.OracleNetwork.from_graph(g, O.V_SWING, O.E_KURAMOTO)
+    check_f64(gpu_rhs(nw, d["u"], d["p"], cuda, np.float64), d["du"], on.abs_terms(d["u"], d["p"]), exact=False)
+
+
+@pytest.mark.parametrize("kind", ["isolated", "no_edges", "star", "pair", "two_hubs"])
+def test_edge_case_graphs(cuda, kind):
+    if kind == "isolated":
+        g = nd.simple_graph(50, [(0, 1), (1, 2), (10, 20)])
+    elif kind == "no_edges":
+        g = nd.simple_graph(7, [])
+    elif kind == "star":
+        g = nd.simple_graph(5001, [(0, i) for i in range(1, 5001)])
+    elif kind == "pair":
+        g = nd.simple_graph(2, [(0, 1)])
+    else:
+        g = nd.simple_graph(3000, [(0, i) for i in range(2, 3000)] + [(1, i) for i in range(2, 3000, 2)])
+    for vk, ek in [(O.V_DIFFUSION, O.E_DIFFUSION), (O.V_SWING, O.E_KURAMOTO)]:
+        nw = make(g, vk, ek, np.float64)
+        on = O.OracleNetwork.from_graph(g, vk, ek)
+        u, p = random_inputs(on, vk, np.random.default_rng(3))
+        check_f64(gpu_rhs(nw, u, p, cuda, np.float64), on.rhs(u, p), on.abs_terms(u, p), exact=ek != O.E_KURAMOTO)
+
+
+def test_wrong_precision_and_sizes_raise(cuda):
+    """GPU_test.jl:63,70 (wrong eltype → ArgumentError) and coreloop.jl:2-7 (sizes)."""
+    import torch
+    g = nd.barabasi_albert(100, 2, seed=1)
+    nw64 = make(g, O.V_KURAMOTO, O.E_KURAMOTO, np.float64)
+    nw32 = make(g, O.V_KURAMOTO, O.E_KURAMOTO, np.float32)
+    u32 = torch.zeros(nw64.dim, dtype=torch.float32, device=cuda)
+    p32 = torch.zeros(nw64.pdim, dtype=torch.float32, device=cuda)
+    du32 = torch.zeros_like(u32)
+    with pytest.raises(nd.ArgumentError):
+        nw64(du32, u32, p32, 0.0)
+    u64, p64, du64 = u32.double(), p32.double(), du32.double()
+    with pytest.raises(nd.ArgumentError):
+        nw32(du64, u64, p64, 0.0)
+    nw64(du64, u64, p64, 0.0)
+    nw32(du32, u32, p32, 0.0)
+    with pytest.raises(nd.ArgumentError):
+        nw64(du64[:-1], u64[:-1], p64, 0.0)
+    with pytest.raises(nd.ArgumentError):
+        nw64(du64, u64, p64[:-1], 0.0)
+    with pytest.raises(nd.ArgumentError):
+        nw64(du64, u64, None, 0.0)
+    with pytest.raises(nd.ArgumentError):
+        nw64(du64.cpu(), u64, p64, 0.0)
+
+
+def test_full_size_ba10m_properties(cuda):
+    """BA(1e7, m=4) diffusion, F64: exact sequential rows on a sample of vertices
+    (including the largest hubs), f(2u) == 2 f(u) bitwise, and Σ du ≈ 0."""
+    import torch
+    g = nd.barabasi_albert(10_000_000, 4, seed=1)
+    nw = make(g, O.V_DIFFUSION, O.E_DIFFUSION, np.float64)
+    rng = np.random.default_rng(0)
+    u = rng.normal(size=g.nv)
+    p = rng.uniform(0.0, 1.0, size=g.ne)
+    du = gpu_rhs(nw, u, p, cuda, np.float64)
+    deg = g.degree()
+    sample = np.concatenate([np.argsort(deg)[-20:], rng.integers(0, g.nv, size=400)])
+    rows = exact_rows(g, O.V_DIFFUSION, O.E_DIFFUSION, u, p, sample)
+    for v, (val,) in rows.items():
+        assert du[v] == val, (v, deg[v], du[v], val)
+    du2 = gpu_rhs(nw, 2.0 * u, p, cuda, np.float64)
+    np.testing.assert_array_equal(du2, 2.0 * du)
+    assert abs(du.sum()) <= 1e-9 * np.abs(du).sum()
+    del nw
+    torch.cuda.empty_cache()
