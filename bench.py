@@ -266,7 +266,7 @@ def run_gb300(args, rank, world, local):
     hbm, peak_kind = peaks()
     B = algorithmic_bytes(nv, ne, 8)
     achieved = B / (t / args.steps) / 1e9
-    launches_per_step = (1 if info.n_hubs == 0 else 2) if nv - info.n_hubs > 0 else 1
+    launches_per_step = 1  # one fused RHS kernel per evaluation
     traffic = profiled_traffic("f64", nv)
     line = {
         "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
@@ -284,6 +284,17 @@ def run_gb300(args, rank, world, local):
                              "bytes = 8(2N+E) + 4(N+1) + 16E"},
         "gpu_launches": launches_per_step * args.steps,
     }
+    # the other FP64 summation modes, for comparison (same workload, fewer steps)
+    ks = min(args.steps, 200)
+    modes = {}
+    for mode in ("sequential_hw", "tree"):
+        nw.set_sum_order(mode)
+        nw(du, u, p, 0.0)
+        tm = time_device(nw, du, u, p, ks, stream)
+        modes[mode] = {"ms_per_step": 1e3 * tm / ks, "edges_per_s": ne * ks / tm}
+        line["gpu_launches"] += launches_per_step * (ks + 1)
+    nw.set_sum_order("sequential")
+    line["f64_modes"] = modes
     # FP32 variant (compensated sums at hubs)
     if not args.no_f32:
         nw32 = nd.adapt(net, torch.float32)

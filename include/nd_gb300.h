@@ -64,8 +64,11 @@ enum nd_coupling { ND_ANTISYMMETRIC = 1 };
 
 /* Summation order of the per-vertex edge aggregation. */
 enum nd_sum_order {
-    ND_ORDER_SEQUENTIAL = 0, /* ascending out-buffer index, = SequentialAggregator (bitwise) */
-    ND_ORDER_TREE = 1        /* deterministic tree inside a warp at hubs (faster, not bitwise)  */
+    ND_ORDER_SEQUENTIAL = 0,   /* ascending out-buffer index, = SequentialAggregator (bitwise);
+                                  FP64 adds run as exact integer arithmetic, hubs as an exact scan */
+    ND_ORDER_TREE = 1,         /* deterministic tree inside a warp at hubs (not bitwise)          */
+    ND_ORDER_SEQUENTIAL_HW = 2 /* the sequential order with hardware FP64 adds (bitwise, slower on
+                                  GB300, whose FP64 pipe is 1/64 of FP32)                         */
 };
 
 /* Network description, the information Network(g, vertexm, edgem) holds

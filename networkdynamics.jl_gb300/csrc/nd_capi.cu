@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "nd_internal.h"
+#include "nd_gb300_selftest.h"
 
 namespace nd {
 
@@ -30,10 +31,10 @@ int cuda_fail(cudaError_t err, const char* what) {
 }
 
 void free_topology(Topology* t) {
-    cudaFree(t->row_ptr);
+    cudaFree(t->slot_ptr);
+    cudaFree(t->slot_vertex);
     cudaFree(t->incid);
-    cudaFree(t->light);
-    cudaFree(t->hubs);
+    cudaFree(t->win_ptr);
     *t = Topology{};
 }
 
@@ -76,20 +77,67 @@ int build_topology(int64_t nv, int64_t ne, const int64_t* src, const int64_t* ds
         incid[fill[s]++] = Incidence{d, (int32_t)e | kSrcSideBit};  // s receives y_src
         incid[fill[d]++] = Incidence{s, (int32_t)e};                // d receives y_dst
     }
-    std::vector<int32_t> light, hubs;
+    // Degree buckets (see nd_internal.h).  The windowed rows, medium rows by degree then
+    // light rows in ascending vertex order, are cut into windows of at most kWindow rows
+    // and kWindowIncidences incidences and sorted by degree (descending, stable) inside
+    // each window.
+    std::vector<int32_t> light, medium, heavy;
     light.reserve(nv);
     for (int64_t v = 0; v < nv; ++v) {
-        if (deg[v] <= (uint32_t)kThreadMaxDeg) light.push_back((int32_t)v);
-        else hubs.push_back((int32_t)v);
+        if (deg[v] <= (uint32_t)kLightMaxDeg) light.push_back((int32_t)v);
+        else if (deg[v] <= (uint32_t)kMediumMaxDeg) medium.push_back((int32_t)v);
+        else heavy.push_back((int32_t)v);
     }
-    std::stable_sort(hubs.begin(), hubs.end(), [&](int32_t a, int32_t b) { return deg[a] > deg[b]; });
+    auto by_degree = [&](int32_t a, int32_t b) { return deg[a] > deg[b]; };
+    std::stable_sort(medium.begin(), medium.end(), by_degree);
+    std::stable_sort(heavy.begin(), heavy.end(), by_degree);
+    std::vector<int32_t> windowed;
+    windowed.reserve(medium.size() + light.size());
+    windowed.insert(windowed.end(), medium.begin(), medium.end());
+    windowed.insert(windowed.end(), light.begin(), light.end());
+    std::vector<int32_t> win_ptr;  // slot offsets within the windowed part
+    win_ptr.push_back(0);
+    {
+        size_t w0 = 0;
+        uint32_t inc = 0;
+        for (size_t i = 0; i < windowed.size(); ++i) {
+            const uint32_t d = deg[windowed[i]];
+            if (i - w0 == (size_t)kWindow || inc + d > (uint32_t)kWindowIncidences) {
+                std::stable_sort(windowed.begin() + w0, windowed.begin() + i, by_degree);
+                win_ptr.push_back((int32_t)i);
+                w0 = i;
+                inc = 0;
+            }
+            inc += d;
+        }
+        if (w0 < windowed.size()) {
+            std::stable_sort(windowed.begin() + w0, windowed.end(), by_degree);
+            win_ptr.push_back((int32_t)windowed.size());
+        }
+    }
+    // Slot order: heavy rows, then the windows.
+    std::vector<int32_t> slot_vertex;
+    slot_vertex.reserve(nv);
+    slot_vertex.insert(slot_vertex.end(), heavy.begin(), heavy.end());
+    slot_vertex.insert(slot_vertex.end(), windowed.begin(), windowed.end());
+    std::vector<uint32_t> slot_ptr(nv + 1);
+    std::vector<Incidence> sincid((size_t)2 * ne);
+    slot_ptr[0] = 0;
+    for (int64_t s = 0; s < nv; ++s) {
+        const int32_t v = slot_vertex[s];
+        const uint32_t b = row_ptr[v], n = deg[v];
+        std::copy(incid.begin() + b, incid.begin() + b + n, sincid.begin() + slot_ptr[s]);
+        slot_ptr[s + 1] = slot_ptr[s] + n;
+    }
 
     Topology t;
     t.nv = nv;
     t.ne = ne;
     t.max_degree = (int32_t)maxdeg;
     t.n_light = (int32_t)light.size();
-    t.n_hubs = (int32_t)hubs.size();
+    t.n_medium = (int32_t)medium.size();
+    t.n_heavy = (int32_t)heavy.size();
+    t.n_windows = (int32_t)win_ptr.size() - 1;
     auto upload = [&](void** dptr, const void* hptr, size_t bytes) -> cudaError_t {
         cudaError_t err = cudaMalloc(dptr, std::max<size_t>(bytes, 16));
         if (err != cudaSuccess) return err;
@@ -97,10 +145,11 @@ int build_topology(int64_t nv, int64_t ne, const int64_t* src, const int64_t* ds
         return err;
     };
     cudaError_t err;
-    if ((err = upload((void**)&t.row_ptr, row_ptr.data(), row_ptr.size() * sizeof(uint32_t))) != cudaSuccess ||
-        (err = upload((void**)&t.incid, incid.data(), incid.size() * sizeof(Incidence))) != cudaSuccess ||
-        (err = upload((void**)&t.light, light.data(), light.size() * sizeof(int32_t))) != cudaSuccess ||
-        (err = upload((void**)&t.hubs, hubs.data(), hubs.size() * sizeof(int32_t))) != cudaSuccess) {
+    if ((err = upload((void**)&t.slot_ptr, slot_ptr.data(), slot_ptr.size() * sizeof(uint32_t))) != cudaSuccess ||
+        (err = upload((void**)&t.slot_vertex, slot_vertex.data(), slot_vertex.size() * sizeof(int32_t))) !=
+            cudaSuccess ||
+        (err = upload((void**)&t.incid, sincid.data(), sincid.size() * sizeof(Incidence))) != cudaSuccess ||
+        (err = upload((void**)&t.win_ptr, win_ptr.data(), win_ptr.size() * sizeof(int32_t))) != cudaSuccess) {
         free_topology(&t);
         return cuda_fail(err, "upload of the network topology");
     }
@@ -143,7 +192,7 @@ int nd_create(const nd_network_desc* desc, int dtype, nd_handle** out) {
     h->edge_kind = desc->edge_kind;
     h->coupling = desc->coupling;
     h->sum_order = ND_ORDER_SEQUENTIAL;
-    h->kahan_min_degree = 64;
+    h->rhs_mode = kModeExact;
     cudaGetDevice(&h->device);
     h->dim = desc->nv * vertex_dim(desc->vertex_kind);
     h->pdim = desc->nv * vertex_pdim(desc->vertex_kind) + desc->ne * edge_pdim(desc->edge_kind);
@@ -180,7 +229,7 @@ int nd_get_info(const nd_handle* h, nd_info* out) {
     out->vertex_kind = h->vertex_kind;
     out->edge_kind = h->edge_kind;
     out->max_degree = h->topo.max_degree;
-    out->n_hubs = h->topo.n_hubs;
+    out->n_hubs = h->topo.n_medium + h->topo.n_heavy;
     out->sum_order = h->sum_order;
     return ND_OK;
 }
@@ -188,9 +237,10 @@ int nd_get_info(const nd_handle* h, nd_info* out) {
 int nd_set_sum_order(nd_handle* h, int order) {
     clear_error();
     if (!h) return fail(ND_ERR_ARG, "nd_set_sum_order: NULL handle");
-    if (order != ND_ORDER_SEQUENTIAL && order != ND_ORDER_TREE)
+    if (order != ND_ORDER_SEQUENTIAL && order != ND_ORDER_TREE && order != ND_ORDER_SEQUENTIAL_HW)
         return fail(ND_ERR_ARG, "nd_set_sum_order: unknown order");
     h->sum_order = order;
+    h->rhs_mode = order == ND_ORDER_TREE ? kModeTree : (order == ND_ORDER_SEQUENTIAL_HW ? kModeNative : kModeExact);
     return ND_OK;
 }
 
@@ -217,19 +267,42 @@ int nd_rhs(nd_handle* h, int dtype, void* du, int64_t n_du, const void* u, int64
     a.u = u;
     a.p = p;
     a.nv = h->topo.nv;
-    a.row_ptr = h->topo.row_ptr;
+    a.slot_ptr = h->topo.slot_ptr;
+    a.slot_vertex = h->topo.slot_vertex;
     a.incid = h->topo.incid;
-    a.light = h->topo.light;
-    a.hubs = h->topo.hubs;
+    a.win_ptr = h->topo.win_ptr;
     a.n_light = h->topo.n_light;
-    a.n_hubs = h->topo.n_hubs;
+    a.n_medium = h->topo.n_medium;
+    a.n_heavy = h->topo.n_heavy;
+    a.n_windows = h->topo.n_windows;
     a.vertex_kind = h->vertex_kind;
     a.edge_kind = h->edge_kind;
-    a.sum_order = h->sum_order;
-    a.kahan_min_degree = h->kahan_min_degree;
+    a.mode = h->rhs_mode;
     cudaError_t err = launch_rhs(h->dtype, a, (cudaStream_t)stream);
     if (err != cudaSuccess) return cuda_fail(err, "nd_rhs kernel launch");
     return ND_OK;
+}
+
+}  // extern "C"
+
+// ----------------------------------------------------------------------------------------
+// Diagnostic entry points (include/nd_gb300_selftest.h).
+extern "C" {
+
+int nd_selftest_exact_add(const double* a, const double* b, double* out, int64_t n, void* stream) {
+    clear_error();
+    if (n < 0 || (n > 0 && (!a || !b || !out))) return fail(ND_ERR_ARG, "nd_selftest_exact_add: bad arguments");
+    cudaError_t err = launch_exact_selftest(a, b, out, n, (cudaStream_t)stream);
+    return err == cudaSuccess ? ND_OK : cuda_fail(err, "nd_selftest_exact_add");
+}
+
+int nd_selftest_exact_scan(const double* terms, const int64_t* seg, const double* s0, double* out, int64_t nseg,
+                           void* stream) {
+    clear_error();
+    if (nseg < 0 || (nseg > 0 && (!terms || !seg || !s0 || !out)))
+        return fail(ND_ERR_ARG, "nd_selftest_exact_scan: bad arguments");
+    cudaError_t err = launch_scan_selftest(terms, seg, s0, out, nseg, (cudaStream_t)stream);
+    return err == cudaSuccess ? ND_OK : cuda_fail(err, "nd_selftest_exact_scan");
 }
 
 }  // extern "C"

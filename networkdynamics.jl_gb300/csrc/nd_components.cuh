@@ -63,6 +63,33 @@ __device__ __forceinline__ T edge_g(T vs, T vd, const T* __restrict__ pe, int32_
     }
 }
 
+// y_dst of g(vs, vd) with the edge parameter already loaded (w is ignored by the
+// parameter-free unit diffusion edge).
+template <typename T, int EK>
+__device__ __forceinline__ T edge_g_w(T vs, T vd, T w) {
+    using A = Arith<T>;
+    if constexpr (EK == ND_E_DIFFUSION) {
+        return A::mul(w, A::sub(vs, vd));
+    } else if constexpr (EK == ND_E_DIFFUSION_UNIT) {
+        return A::sub(vs, vd);
+    } else {
+        return A::mul(w, A::sin_phase(A::sub(vs, vd)));
+    }
+}
+
+// The incidence contribution from preloaded operands (see incidence_term).
+template <typename T, int EK>
+__device__ __forceinline__ T incidence_term_w(T uv, T un, T w, bool src_side) {
+    const T vs = src_side ? uv : un;
+    const T vd = src_side ? un : uv;
+    const T y = edge_g_w<T, EK>(vs, vd, w);
+    if constexpr (sizeof(T) == 8) {
+        return __longlong_as_double(__double_as_longlong(y) ^ ((long long)src_side << 63));
+    } else {
+        return __int_as_float(__float_as_int(y) ^ ((int)src_side << 31));
+    }
+}
+
 // Contribution of one incidence to the aggregation at the row vertex (value uv).  The
 // AntiSymmetric wrapper evaluates g once per edge with the edge's own orientation and
 // hands -y_dst to the source (src/component_functions.jl:117-127), so the source side
@@ -74,7 +101,12 @@ __device__ __forceinline__ T incidence_term(T uv, T un, const T* __restrict__ pe
     const T vs = src_side ? uv : un;
     const T vd = src_side ? un : uv;
     const T y = edge_g<T, EK>(vs, vd, pe, e);
-    return src_side ? -y : y;
+    // negate by flipping the sign bit (an integer op, not an FP64 subtraction)
+    if constexpr (sizeof(T) == 8) {
+        return __longlong_as_double(__double_as_longlong(y) ^ ((long long)src_side << 63));
+    } else {
+        return __int_as_float(__float_as_int(y) ^ ((int)src_side << 31));
+    }
 }
 
 template <int VK>

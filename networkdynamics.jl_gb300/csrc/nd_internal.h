@@ -35,42 +35,64 @@ inline int vertex_dim(int vk) { return vk == ND_V_SWING ? 2 : 1; }
 inline int vertex_pdim(int vk) { return vk == ND_V_DIFFUSION ? 0 : (vk == ND_V_KURAMOTO ? 1 : 3); }
 inline int edge_pdim(int ek) { return ek == ND_E_DIFFUSION_UNIT ? 0 : 1; }
 
-// Degree-bucket thresholds.  Rows with degree <= kThreadMaxDeg run thread-per-vertex,
-// rows above it run on the cooperative hub path (a warp per row).
-constexpr int kThreadMaxDeg = 32;
+// Degree buckets.  Rows with degree <= kMediumMaxDeg are processed in windows: a block
+// evaluates all edge terms of up to kWindow rows / kWindowIncidences incidences in
+// parallel, then sums one row per thread; rows are sorted by degree inside a window so
+// the lanes of a warp walk rows of nearly equal length.  Medium rows (degree above
+// kLightMaxDeg) come first, globally sorted by degree; light rows follow in vertex order.
+// Longer rows (power-law hubs) get a block each and are summed by an exact parallel scan:
+// a per-thread chain that long would wait on the shared FP64 pipe at every step.
+constexpr int kLightMaxDeg = 32;
+constexpr int kMediumMaxDeg = 512;
+constexpr int kWindow = 256;
 
 // Device-resident topology of one network.
+// Rows are stored in processing order ("slots"): heavy rows (by degree, descending), then
+// medium rows (by degree, descending), then the light windows, each window's rows sorted
+// by degree.  slot_ptr indexes the incidences of a slot, slot_vertex names its vertex.
+constexpr int kWindowIncidences = 2048;  // light window: at most this many incidences
+
 struct Topology {
     int64_t nv = 0, ne = 0;
     int32_t max_degree = 0;
-    uint32_t* row_ptr = nullptr;     // [nv+1] offsets into incid
-    Incidence* incid = nullptr;      // [2ne]
-    int32_t* light = nullptr;        // [n_light] vertices on the thread-per-vertex path, ascending
-    int32_t* hubs = nullptr;         // [n_hubs] vertices on the cooperative path, by degree desc
-    int32_t n_light = 0, n_hubs = 0;
+    uint32_t* slot_ptr = nullptr;    // [nv+1] offsets into incid, by slot
+    int32_t* slot_vertex = nullptr;  // [nv] vertex of each slot
+    Incidence* incid = nullptr;      // [2ne] incidences in slot order, each row by edge id
+    int32_t* win_ptr = nullptr;      // [n_windows+1] first slot of each light window
+    int32_t n_light = 0, n_medium = 0, n_heavy = 0, n_windows = 0;
 };
 
 // Build the CSR on the host and upload it.  src/dst are 0-based host arrays.
 int build_topology(int64_t nv, int64_t ne, const int64_t* src, const int64_t* dst, Topology* topo);
 void free_topology(Topology* topo);
 
+// Accumulation modes of the FP64 RHS.
+enum RhsMode : int32_t {
+    kModeExact = 0,   // sequential order; integer-exact adds; hubs by exact scan (default)
+    kModeNative = 1,  // sequential order; hardware DADD chains (reference timing mode)
+    kModeTree = 2     // sequential order for short rows, warp tree at hubs (not bitwise)
+};
+
 struct RhsArgs {
     void* du;
     const void* u;
     const void* p;
     int64_t nv;
-    const uint32_t* row_ptr;
+    const uint32_t* slot_ptr;
+    const int32_t* slot_vertex;
     const Incidence* incid;
-    const int32_t* light;
-    const int32_t* hubs;
-    int32_t n_light, n_hubs;
+    const int32_t* win_ptr;
+    int32_t n_light, n_medium, n_heavy, n_windows;
     int32_t vertex_kind, edge_kind;
-    int32_t sum_order;
-    int32_t kahan_min_degree;  // F32: compensated sums on rows at least this long
+    int32_t mode;
 };
 
 // Launch the fused RHS for the given element type.
 cudaError_t launch_rhs(int dtype, const RhsArgs& a, cudaStream_t stream);
+
+cudaError_t launch_exact_selftest(const double* a, const double* b, double* out, int64_t n, cudaStream_t s);
+cudaError_t launch_scan_selftest(const double* terms, const int64_t* seg, const double* s0, double* out,
+                                 int64_t nseg, cudaStream_t s);
 
 }  // namespace nd
 
@@ -78,7 +100,7 @@ struct nd_handle {
     int dtype;
     int vertex_kind, edge_kind, coupling;
     int sum_order;
-    int kahan_min_degree;
+    int rhs_mode;
     int device;
     int64_t dim, pdim;
     nd::Topology topo;

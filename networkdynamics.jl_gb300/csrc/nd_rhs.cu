@@ -3,136 +3,433 @@
 // One RHS replaces the reference's phased core loop (src/coreloop.jl:22-101): vertex g,
 // edge g/f, the gather of vertex outputs into edge inputs (src/gbufs.jl:7-25), the
 // aggregation (src/aggregators.jl:133-151) and vertex f.  Vertex outputs are the first
-// state (StateMask(1)), so edges read u directly; edge values live in registers; the
-// per-vertex sum walks the row in ascending edge id, which is the SequentialAggregator
-// order, and du is written once.  No output, gather or aggregation buffers exist.
+// state (StateMask(1)), so edges read u directly; edge values live in registers or shared
+// memory; each row is summed in ascending edge id, the SequentialAggregator order; du is
+// written once.  There are no output, gather or aggregation buffers.
 //
-// Degree buckets: rows with degree <= kThreadMaxDeg are summed by one thread each; longer
-// rows (power-law hubs) by a warp that loads and evaluates 32 incidences at a time and
-// then adds them in order (sequential mode) or as a fixed shuffle tree (tree mode).
+// One launch, two roles chosen per block (degree buckets and slot order: nd_internal.h):
+//   heavy   a block per row: the terms of kTile incidences at a time go to shared memory
+//           and warp 0 adds them in order with the exact scan (FP64), or the block sums
+//           thread-strided slices in a fixed tree (FP32 with Kahan, FP64 tree mode);
+//   window  a block per window of rows: phase A evaluates the window's edge terms, one
+//           incidence per thread (coalesced incidence loads, independent gathers and FP64
+//           operations in flight) into shared memory; phase B sums one row per thread.
+// Heavy blocks come first so the long rows start early.
+//
+// Cache policy: u is gathered at random and is re-read by every incidence, so its loads
+// ask L2 to keep the lines (evict_last); the incidence stream and the edge parameters are
+// read once per side and ask to be evicted first.
+//
+// FP64 on GB300 retires ~2 lanes/clock/SM and a DADD holds its sub-partition's FP64 pipe
+// for a full warp even with one lane active.  Window rows (at most kMediumMaxDeg long)
+// add with hardware DADDs, all lanes busy on rows of similar length.  A hub's sum would
+// be a chain of thousands of DADDs on one sub-partition, so it runs on the integer pipes:
+//   * the heavy rows' warp sums use an exact scan: while the running sum S stays inside one binade,
+//     RN(S + t) = S + RN(t / ulp(S)) ulp(S), so a run of additions becomes an integer
+//     prefix sum of the terms scaled to S's ulp.  A lane whose prefix leaves the binade
+//     (or whose scaled term is a tie) ends the run; that one step is done with the exact
+//     adder and the scan resumes.  The result equals the sequential sum bit for bit.
 
 #include "nd_components.cuh"
+#include "nd_exact.cuh"
 #include "nd_internal.h"
 
 namespace nd {
 
 namespace {
 
-constexpr int kLightBlock = 256;
-constexpr int kHubBlock = 256;
-constexpr int kWarpsPerHubBlock = kHubBlock / 32;
+constexpr int kBlock = 256;
+constexpr int kWarpsPerBlock = kBlock / 32;
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kTile = 2048;  // heavy rows: terms per shared-memory tile
 
-template <typename T, int VK, int EK>
-__global__ void __launch_bounds__(kLightBlock) rhs_light_kernel(RhsArgs a) {
+// ---- loads with an L2 eviction policy -------------------------------------------------
+__device__ __forceinline__ uint64_t policy_evict_first() {
+    uint64_t p;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ uint64_t policy_evict_last() {
+    uint64_t p;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ int2 ld_hint(const int2* ptr, uint64_t pol) {
+    int2 r;
+    asm("ld.global.nc.L2::cache_hint.v2.s32 {%0, %1}, [%2], %3;" : "=r"(r.x), "=r"(r.y) : "l"(ptr), "l"(pol));
+    return r;
+}
+__device__ __forceinline__ double ld_hint(const double* ptr, uint64_t pol) {
+    double r;
+    asm("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(r) : "l"(ptr), "l"(pol));
+    return r;
+}
+__device__ __forceinline__ float ld_hint(const float* ptr, uint64_t pol) {
+    float r;
+    asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(r) : "l"(ptr), "l"(pol));
+    return r;
+}
+
+// Edge parameter of edge e (0 for the parameter-free unit diffusion edge).
+template <typename T, int EK>
+__device__ __forceinline__ T edge_param(const T* __restrict__ pe, int32_t e, uint64_t pol) {
+    if constexpr (EK == ND_E_DIFFUSION_UNIT) {
+        return T(0);
+    } else {
+        return ld_hint(pe + e, pol);
+    }
+}
+
+// ---- exact sequential sums on the integer pipes ----------------------------------------
+
+// Scaled term R = RN(t / 2^(eS-1075)) for a running sum whose exponent field is eS.
+// ok = false when the step cannot be taken by the scan (too large, inf/nan).  For a
+// tie (t / ulp exactly halfway between two integers) the truncated magnitude is returned
+// with tie = true; the scan then rounds it to even against the running sum's parity.
+__device__ __forceinline__ int64_t scaled_term(double t, int eS, bool& ok, bool& tie) {
+    const uint64_t tb = exact::to_bits(t);
+    uint64_t ft = tb & exact::kFrac;
+    int et = (int)((tb >> 52) & 0x7ff);
+    if ((tb & ~exact::kSign) == 0) return 0;
+    if (et == 0x7ff) {
+        ok = false;
+        return 0;
+    }
+    if (et) ft |= exact::kHidden;
+    else et = 1;
+    const int sh = eS - et;  // t / ulp(S) = ft · 2^-sh
+    uint64_t mag;
+    if (sh <= 0) {
+        if (sh < -9) {
+            ok = false;
+            return 0;
+        }
+        mag = ft << (-sh);
+    } else if (sh >= 64) {
+        mag = 0;  // |t| < 2^-11 ulp: rounds to zero, never a tie
+    } else {
+        mag = ft >> sh;
+        const uint64_t rem = ft & ((1ull << sh) - 1);
+        const uint64_t half = 1ull << (sh - 1);
+        if (rem > half) mag += 1;
+        else if (rem == half) tie = true;
+    }
+    if (mag >= (1ull << 52)) ok = false;
+    return (tb & exact::kSign) ? -(int64_t)mag : (int64_t)mag;
+}
+
+// Add the terms held by lanes [0, n) of the warp to S, in lane order, exactly as the
+// sequential loop S = S + t_0; S = S + t_1; ... would.  S is warp-uniform.
+__device__ __forceinline__ double exact_scan_add(double S, double t, int n, int lane) {
+    int j0 = 0;
+    while (j0 < n) {
+        const uint64_t sb = exact::to_bits(S);
+        const int eS = (int)((sb >> 52) & 0x7ff);
+        if (eS == 0 || eS == 0x7ff) {  // zero / subnormal / non-finite sum: one exact step
+            S = exact::add_rn(S, __shfl_sync(kFull, t, j0));
+            ++j0;
+            continue;
+        }
+        const bool active = lane >= j0 && lane < n;
+        bool ok = true, tie = false;
+        int64_t x = active ? scaled_term(t, eS, ok, tie) : 0;
+        // Ties round to even against the running sum.  Its parity evolves as p -> p ^ (R & 1)
+        // for ordinary steps and p -> 0 after a tie step; the composition of such maps
+        // (p -> (p & ka) ^ kb) is scanned to give each lane the parity before its step.
+        unsigned ka = tie ? 0u : 1u, kb = tie ? 0u : (unsigned)(x & 1);
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const unsigned pa = __shfl_up_sync(kFull, ka, off), pb = __shfl_up_sync(kFull, kb, off);
+            if (lane >= off) {
+                kb = (pb & ka) ^ kb;
+                ka = pa & ka;
+            }
+        }
+        if (__any_sync(kFull, tie)) {
+            unsigned xa = __shfl_up_sync(kFull, ka, 1), xb = __shfl_up_sync(kFull, kb, 1);
+            if (lane == 0) {
+                xa = 1u;
+                xb = 0u;
+            }
+            const unsigned p_prev = ((unsigned)(sb & 1) & xa) ^ xb;
+            if (tie) {
+                const uint64_t mag = (uint64_t)(x < 0 ? -x : x);
+                const uint64_t c = (p_prev ^ (unsigned)(mag & 1)) & 1u;  // 1: round away from zero
+                x = (exact::to_bits(t) & exact::kSign) ? -(int64_t)(mag + c) : (int64_t)(mag + c);
+            }
+        }
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int64_t y = __shfl_up_sync(kFull, x, off);
+            if (lane >= off) x += y;
+        }
+        const int64_t mS = (int64_t)((sb & exact::kFrac) | exact::kHidden);
+        const int64_t m = (sb & exact::kSign) ? x - mS : x + mS;
+        const uint64_t am = (uint64_t)(m < 0 ? -m : m);
+        const bool valid = ok && am >= (1ull << 52) + 1 && am <= (1ull << 53) - 2;
+        const unsigned bad = __ballot_sync(kFull, active && !valid);
+        const int L = bad ? __ffs(bad) - 1 : n;
+        if (L > j0) {
+            const int64_t mL = __shfl_sync(kFull, m, L - 1);
+            const uint64_t aL = (uint64_t)(mL < 0 ? -mL : mL);
+            S = exact::from_bits((mL < 0 ? exact::kSign : 0) | ((uint64_t)eS << 52) | (aL & exact::kFrac));
+        }
+        if (L < n) S = exact::add_rn(S, __shfl_sync(kFull, t, L));
+        j0 = L + 1;
+    }
+    return S;
+}
+
+// Sequential exact sum of n terms in shared memory by one warp, 32 at a time.
+__device__ __forceinline__ double exact_scan_smem(double S, const double* __restrict__ tile, int n, int lane) {
+    for (int c = 0; c < n; c += 32) {
+        const int k = c + lane;
+        const double t = k < n ? tile[k] : 0.0;
+        S = exact_scan_add(S, t, min(32, n - c), lane);
+    }
+    return S;
+}
+
+// The same sum with a sliding window of 8 terms per lane (256 per step): each lane scales
+// and prefix-sums its 8 terms locally, one warp scan adds the lanes before it, and every
+// position checks that its running sum stays strictly inside S's binade.  The window then
+// slides to just past the first position that failed (a binade change or a tie), which is
+// added with the hardware adder.  Long hub rows change binade every ~50-100 terms, so a
+// step advances far at the cost of a single warp scan.
+constexpr int kScanPer = 8;
+__device__ __noinline__ double exact_scan_wide(double S, const double* __restrict__ tile, int n, int lane) {
+    int pos = 0;
+    while (pos < n) {
+        const uint64_t sb = exact::to_bits(S);
+        const int eS = (int)((sb >> 52) & 0x7ff);
+        if (eS == 0 || eS == 0x7ff) {  // zero / subnormal / non-finite sum: one exact step
+            S = exact::add_rn(S, tile[pos]);
+            ++pos;
+            continue;
+        }
+        const int end = min(n, pos + 32 * kScanPer);
+        const int base = pos + lane * kScanPer;
+        int64_t pre[kScanPer];
+        unsigned okmask = 0;
+        int64_t run = 0;
+#pragma unroll
+        for (int i = 0; i < kScanPer; ++i) {
+            bool ok = true, tie = false;
+            const int q = base + i;
+            const int64_t R = q < end ? scaled_term(tile[q], eS, ok, tie) : 0;
+            run += R;
+            pre[i] = run;
+            okmask |= (unsigned)(ok && !tie) << i;
+        }
+        int64_t x = run;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int64_t y = __shfl_up_sync(kFull, x, off);
+            if (lane >= off) x += y;
+        }
+        const int64_t mS0 = (int64_t)((sb & exact::kFrac) | exact::kHidden);
+        const int64_t mS = (sb & exact::kSign) ? -mS0 : mS0;
+        const int64_t before = mS + x - run;  // running sum before this lane's first term
+        int firstbad = 0x7fffffff;
+#pragma unroll
+        for (int i = kScanPer - 1; i >= 0; --i) {
+            const int64_t m = before + pre[i];
+            const uint64_t am = (uint64_t)(m < 0 ? -m : m);
+            const bool valid = ((okmask >> i) & 1u) && am >= (1ull << 52) + 1 && am <= (1ull << 53) - 2;
+            if (base + i < end && !valid) firstbad = base + i;
+        }
+        const int P = (int)__reduce_min_sync(kFull, (unsigned)firstbad);
+        const int acc_end = P < end ? P : end;  // positions [pos, acc_end) are exact
+        if (acc_end > pos) {
+            const int q = acc_end - 1 - pos, owner = q / kScanPer, idx = q % kScanPer;
+            int64_t mine = 0;
+#pragma unroll
+            for (int i = 0; i < kScanPer; ++i)
+                if (i == idx) mine = before + pre[i];
+            const int64_t mL = __shfl_sync(kFull, mine, owner);
+            const uint64_t aL = (uint64_t)(mL < 0 ? -mL : mL);
+            S = exact::from_bits((mL < 0 ? exact::kSign : 0) | ((uint64_t)eS << 52) | (aL & exact::kFrac));
+        }
+        if (P < end) {
+            S = __dadd_rn(S, tile[P]);
+            pos = P + 1;
+        } else {
+            pos = end;
+        }
+    }
+    return S;
+}
+
+// Shared memory of one block, sized for the largest role (light windows in FP64).
+template <typename T>
+struct Smem {
+    static constexpr int kWin = (kWindowIncidences + kWindow) * (int)sizeof(T) + kWindowIncidences;
+    static constexpr int kHeavy = kTile * (int)sizeof(double);
+    static constexpr int kBytes = kWin > kHeavy ? kWin : kHeavy;
+};
+
+// ---- heavy: a block per row ---------------------------------------------------------------
+template <typename T, int VK, int EK, int MODE>
+__device__ __forceinline__ void block_row(const RhsArgs& a, int slot, unsigned char* smem) {
     using A = Arith<T>;
     constexpr int DV = VertexDims<VK>::dim;
-    const int i = blockIdx.x * kLightBlock + threadIdx.x;
-    if (i >= a.n_light) return;
-    const int64_t v = a.light[i];
     const T* __restrict__ u = static_cast<const T*>(a.u);
     const T* __restrict__ p = static_cast<const T*>(a.p);
     const T* __restrict__ pe = p + a.nv * VertexDims<VK>::pdim;
-    const uint32_t beg = a.row_ptr[v], end = a.row_ptr[v + 1];
-    const T uv = u[v * DV];
+    const int2* __restrict__ incid = reinterpret_cast<const int2*>(a.incid);
+    const uint64_t keep = policy_evict_last(), stream = policy_evict_first();
+    const int64_t v = __ldg(a.slot_vertex + slot);
+    const uint32_t beg = __ldg(a.slot_ptr + slot), end = __ldg(a.slot_ptr + slot + 1);
+    const T uv = __ldg(u + v * DV);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if constexpr (sizeof(T) == 8 && MODE != kModeTree) {
+        double* tile = reinterpret_cast<double*>(smem);
+        double S = 0.0;
+        for (uint32_t base = beg; base < end; base += kTile) {
+            const int n = (int)min((uint32_t)kTile, end - base);
+#pragma unroll 4
+            for (int i = tid; i < n; i += kBlock) {
+                const int2 inc = ld_hint(incid + base + i, stream);
+                const T un = ld_hint(u + (int64_t)inc.x * DV, keep);
+                const T w = edge_param<T, EK>(pe, inc.y & 0x7fffffff, stream);
+                tile[i] = incidence_term_w<T, EK>(uv, un, w, inc.y < 0);
+            }
+            __syncthreads();
+            if (warp == 0) {
+                if constexpr (MODE == kModeNative) {
+                    if (lane == 0)
+                        for (int i = 0; i < n; ++i) S = __dadd_rn(S, tile[i]);
+                } else {
+                    S = exact_scan_wide(S, tile, n, lane);
+                }
+            }
+            __syncthreads();
+        }
+        if (tid == 0) vertex_f<T, VK>(static_cast<T*>(a.du), u, p, v, (T)S);
+    } else {
+        T* red = reinterpret_cast<T*>(smem);
+        T acc = T(0), comp = T(0);
+#pragma unroll 4
+        for (uint32_t k = beg + tid; k < end; k += kBlock) {
+            const int2 inc = ld_hint(incid + k, stream);
+            const T un = ld_hint(u + (int64_t)inc.x * DV, keep);
+            const T w = edge_param<T, EK>(pe, inc.y & 0x7fffffff, stream);
+            const T term = incidence_term_w<T, EK>(uv, un, w, inc.y < 0);
+            if constexpr (sizeof(T) == 4) {
+                const T y = A::sub(term, comp);
+                const T s = A::add(acc, y);
+                comp = A::sub(A::sub(s, acc), y);
+                acc = s;
+            } else {
+                acc = A::add(acc, term);
+            }
+        }
+        if constexpr (sizeof(T) == 4) acc = A::sub(acc, comp);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) acc = A::add(acc, __shfl_xor_sync(kFull, acc, off));
+        if (lane == 0) red[warp] = acc;
+        __syncthreads();
+        if (tid == 0) {
+            T s = red[0];
+#pragma unroll
+            for (int w = 1; w < kWarpsPerBlock; ++w) s = A::add(s, red[w]);
+            vertex_f<T, VK>(static_cast<T*>(a.du), u, p, v, s);
+        }
+    }
+}
+
+// ---- windows: a block per window of rows ----------------------------------------------------
+template <typename T, int VK, int EK, int MODE>
+__device__ __forceinline__ void window_block(const RhsArgs& a, int win, unsigned char* smem) {
+    using A = Arith<T>;
+    constexpr int DV = VertexDims<VK>::dim;
+    const T* __restrict__ u = static_cast<const T*>(a.u);
+    const T* __restrict__ p = static_cast<const T*>(a.p);
+    const T* __restrict__ pe = p + a.nv * VertexDims<VK>::pdim;
+    const int2* __restrict__ incid = reinterpret_cast<const int2*>(a.incid);
+    T* s_term = reinterpret_cast<T*>(smem);                        // [kWindowIncidences]
+    T* s_uv = s_term + kWindowIncidences;                          // [kWindow]
+    uint8_t* s_owner = reinterpret_cast<uint8_t*>(s_uv + kWindow);  // [kWindowIncidences]
+    const uint64_t keep = policy_evict_last(), stream = policy_evict_first();
+    const int first = a.n_heavy;
+    const int slot0 = first + __ldg(a.win_ptr + win), slot1 = first + __ldg(a.win_ptr + win + 1);
+    const uint32_t i0 = __ldg(a.slot_ptr + slot0), i1 = __ldg(a.slot_ptr + slot1);
+    const int n = (int)(i1 - i0);  // <= kWindowIncidences
+    const int tid = threadIdx.x;
+    // phase 0: each row's vertex value and the owner (row) of each incidence
+    const int s = slot0 + tid;
+    const bool has_row = s < slot1;
+    int64_t v = 0;
+    int beg = 0, end = 0;
+    if (has_row) {
+        v = __ldg(a.slot_vertex + s);
+        beg = (int)(__ldg(a.slot_ptr + s) - i0);
+        end = (int)(__ldg(a.slot_ptr + s + 1) - i0);
+        s_uv[tid] = ld_hint(u + v * DV, keep);
+        for (int j = beg; j < end; ++j) s_owner[j] = (uint8_t)tid;
+    }
+    __syncthreads();
+    // phase A: the edge terms, one incidence per thread: coalesced incidence loads, many
+    // independent gathers and FP64 operations in flight
+#pragma unroll 4
+    for (int k = tid; k < n; k += kBlock) {
+        const int2 inc = ld_hint(incid + i0 + k, stream);
+        const T un = ld_hint(u + (int64_t)inc.x * DV, keep);
+        const T w = edge_param<T, EK>(pe, inc.y & 0x7fffffff, stream);
+        s_term[k] = incidence_term_w<T, EK>(s_uv[s_owner[k]], un, w, inc.y < 0);
+    }
+    __syncthreads();
+    // phase B: one row per thread, in edge order.  FP64: hardware adds (a row is at most
+    // kMediumMaxDeg long; one DADD per term is cheaper than the ~100 integer operations
+    // of an emulated add).  FP32: compensated sums on the rows above kLightMaxDeg.
+    if (!has_row) return;
     T acc = T(0);
-    for (uint32_t k = beg; k < end; ++k) {
-        const Incidence inc = a.incid[k];
-        const T un = u[(int64_t)inc.nbr * DV];
-        acc = A::add(acc, incidence_term<T, EK>(uv, un, pe, inc.eid));
+    if constexpr (sizeof(T) == 8) {
+        for (int j = beg; j < end; ++j) acc = __dadd_rn(acc, s_term[j]);
+    } else {
+        if (end - beg > kLightMaxDeg) {
+            T comp = T(0);
+            for (int j = beg; j < end; ++j) {
+                const T y = A::sub(s_term[j], comp);
+                const T t = A::add(acc, y);
+                comp = A::sub(A::sub(t, acc), y);
+                acc = t;
+            }
+            acc = A::sub(acc, comp);
+        } else {
+            for (int j = beg; j < end; ++j) acc = A::add(acc, s_term[j]);
+        }
     }
     vertex_f<T, VK>(static_cast<T*>(a.du), u, p, v, acc);
 }
 
-// Sequential (in-order) warp-per-hub: lanes evaluate 32 consecutive incidences, lane 0
-// adds them in row order.  With KAHAN (FP32 only) lane 0 keeps a compensation term.
-template <typename T, int VK, int EK, bool KAHAN>
-__global__ void __launch_bounds__(kHubBlock) rhs_hub_seq_kernel(RhsArgs a) {
-    using A = Arith<T>;
-    constexpr int DV = VertexDims<VK>::dim;
-    __shared__ T stage[kWarpsPerHubBlock][32];
-    const int warp_in_block = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int w = blockIdx.x * kWarpsPerHubBlock + warp_in_block;
-    if (w >= a.n_hubs) return;
-    const int64_t v = a.hubs[w];
-    const T* __restrict__ u = static_cast<const T*>(a.u);
-    const T* __restrict__ p = static_cast<const T*>(a.p);
-    const T* __restrict__ pe = p + a.nv * VertexDims<VK>::pdim;
-    const uint32_t beg = a.row_ptr[v], end = a.row_ptr[v + 1];
-    const T uv = u[v * DV];
-    T acc = T(0), comp = T(0);
-    for (uint32_t c = beg; c < end; c += 32) {
-        const uint32_t k = c + lane;
-        T term = T(0);
-        if (k < end) {
-            const Incidence inc = a.incid[k];
-            term = incidence_term<T, EK>(uv, u[(int64_t)inc.nbr * DV], pe, inc.eid);
-        }
-        stage[warp_in_block][lane] = term;
-        __syncwarp();
-        if (lane == 0) {
-            const uint32_t n = min(32u, end - c);
-            for (uint32_t j = 0; j < n; ++j) {
-                if constexpr (KAHAN) {
-                    const T y = A::sub(stage[warp_in_block][j], comp);
-                    const T s = A::add(acc, y);
-                    comp = A::sub(A::sub(s, acc), y);
-                    acc = s;
-                } else {
-                    acc = A::add(acc, stage[warp_in_block][j]);
-                }
-            }
-        }
-        __syncwarp();
+template <typename T, int VK, int EK, int MODE>
+__global__ void __launch_bounds__(kBlock, 8) rhs_kernel(RhsArgs a) {
+    __shared__ __align__(16) unsigned char smem[Smem<T>::kBytes];
+    const int b = blockIdx.x;
+    if (b < a.n_heavy) {
+        block_row<T, VK, EK, MODE>(a, b, smem);
+    } else {
+        window_block<T, VK, EK, MODE>(a, b - a.n_heavy, smem);
     }
-    if (lane == 0) vertex_f<T, VK>(static_cast<T*>(a.du), u, p, v, acc);
-}
-
-// Tree warp-per-hub: each lane sums a strided slice, then a fixed xor-shuffle tree.  The
-// result is deterministic but rounds differently from the sequential order.
-template <typename T, int VK, int EK, bool KAHAN>
-__global__ void __launch_bounds__(kHubBlock) rhs_hub_tree_kernel(RhsArgs a) {
-    using A = Arith<T>;
-    constexpr int DV = VertexDims<VK>::dim;
-    const int lane = threadIdx.x & 31;
-    const int w = blockIdx.x * kWarpsPerHubBlock + (threadIdx.x >> 5);
-    if (w >= a.n_hubs) return;
-    const int64_t v = a.hubs[w];
-    const T* __restrict__ u = static_cast<const T*>(a.u);
-    const T* __restrict__ p = static_cast<const T*>(a.p);
-    const T* __restrict__ pe = p + a.nv * VertexDims<VK>::pdim;
-    const uint32_t beg = a.row_ptr[v], end = a.row_ptr[v + 1];
-    const T uv = u[v * DV];
-    T acc = T(0), comp = T(0);
-    for (uint32_t k = beg + lane; k < end; k += 32) {
-        const Incidence inc = a.incid[k];
-        const T term = incidence_term<T, EK>(uv, u[(int64_t)inc.nbr * DV], pe, inc.eid);
-        if constexpr (KAHAN) {
-            const T y = A::sub(term, comp);
-            const T s = A::add(acc, y);
-            comp = A::sub(A::sub(s, acc), y);
-            acc = s;
-        } else {
-            acc = A::add(acc, term);
-        }
-    }
-    if constexpr (KAHAN) acc = A::sub(acc, comp);
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) acc = A::add(acc, __shfl_xor_sync(0xffffffffu, acc, off));
-    if (lane == 0) vertex_f<T, VK>(static_cast<T*>(a.du), u, p, v, acc);
 }
 
 template <typename T, int VK, int EK>
 cudaError_t launch_typed(const RhsArgs& a, cudaStream_t s) {
-    if (a.n_light > 0) {
-        rhs_light_kernel<T, VK, EK><<<(a.n_light + kLightBlock - 1) / kLightBlock, kLightBlock, 0, s>>>(a);
-    }
-    if (a.n_hubs > 0) {
-        const int grid = (a.n_hubs + kWarpsPerHubBlock - 1) / kWarpsPerHubBlock;
-        constexpr bool kF32 = sizeof(T) == 4;
-        if (a.sum_order == ND_ORDER_TREE) {
-            rhs_hub_tree_kernel<T, VK, EK, kF32><<<grid, kHubBlock, 0, s>>>(a);
-        } else {
-            rhs_hub_seq_kernel<T, VK, EK, kF32><<<grid, kHubBlock, 0, s>>>(a);
+    const int grid = a.n_heavy + a.n_windows;
+    if (grid == 0) return cudaSuccess;
+    if constexpr (sizeof(T) == 4) {
+        rhs_kernel<T, VK, EK, kModeTree><<<grid, kBlock, 0, s>>>(a);
+    } else {
+        switch (a.mode) {
+            case kModeNative:
+                rhs_kernel<T, VK, EK, kModeNative><<<grid, kBlock, 0, s>>>(a);
+                break;
+            case kModeTree:
+                rhs_kernel<T, VK, EK, kModeTree><<<grid, kBlock, 0, s>>>(a);
+                break;
+            default:
+                rhs_kernel<T, VK, EK, kModeExact><<<grid, kBlock, 0, s>>>(a);
         }
     }
     return cudaGetLastError();
@@ -155,10 +452,59 @@ cudaError_t launch_dtype(const RhsArgs& a, cudaStream_t s) {
     return cudaErrorInvalidValue;
 }
 
+// Self-test of the integer-exact adder.
+__global__ void exact_add_selftest_kernel(const double* a, const double* b, double* out, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = exact::add_rn(a[i], b[i]);
+}
+
+// Self-test of the exact scans: one block per segment; odd segments use the 32-term warp
+// scan on registers, even segments shared-memory tiles with the 32-term scan (w % 4 == 2)
+// or the sliding 256-term scan of the heavy rows' path (w % 4 == 0).
+__global__ void exact_scan_selftest_kernel(const double* terms, const int64_t* seg, const double* s0, double* out,
+                                           int64_t nseg) {
+    __shared__ double tile[kTile];
+    const int64_t w = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double S = s0[w];
+    if (w & 1) {
+        if (warp == 0) {
+            for (int64_t c = seg[w]; c < seg[w + 1]; c += 32) {
+                const int64_t k = c + lane;
+                const double t = k < seg[w + 1] ? terms[k] : 0.0;
+                const int n = (int)min((int64_t)32, seg[w + 1] - c);
+                S = exact_scan_add(S, t, n, lane);
+            }
+        }
+    } else {
+        for (int64_t base = seg[w]; base < seg[w + 1]; base += kTile) {
+            const int n = (int)min((int64_t)kTile, seg[w + 1] - base);
+            for (int i = threadIdx.x; i < n; i += blockDim.x) tile[i] = terms[base + i];
+            __syncthreads();
+            if (warp == 0) S = (w & 2) ? exact_scan_smem(S, tile, n, lane) : exact_scan_wide(S, tile, n, lane);
+            __syncthreads();
+        }
+    }
+    if (threadIdx.x == 0) out[w] = S;
+}
+
 }  // namespace
 
 cudaError_t launch_rhs(int dtype, const RhsArgs& a, cudaStream_t s) {
     return dtype == ND_F64 ? launch_dtype<double>(a, s) : launch_dtype<float>(a, s);
+}
+
+cudaError_t launch_exact_selftest(const double* a, const double* b, double* out, int64_t n, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    exact_add_selftest_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, b, out, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scan_selftest(const double* terms, const int64_t* seg, const double* s0, double* out, int64_t nseg,
+                                 cudaStream_t s) {
+    if (nseg <= 0) return cudaSuccess;
+    exact_scan_selftest_kernel<<<(unsigned)nseg, kBlock, 0, s>>>(terms, seg, s0, out, nseg);
+    return cudaGetLastError();
 }
 
 }  // namespace nd

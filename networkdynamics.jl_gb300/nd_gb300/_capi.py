@@ -35,6 +35,7 @@ ND_ANTISYMMETRIC = 1
 
 ND_ORDER_SEQUENTIAL = 0
 ND_ORDER_TREE = 1
+ND_ORDER_SEQUENTIAL_HW = 2
 
 
 class NDError(RuntimeError):
@@ -81,6 +82,9 @@ SIGNATURES = {
     "nd_set_sum_order": (C.c_int, [C.c_void_p, C.c_int]),
     "nd_rhs": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
                          C.c_void_p, C.c_int64, C.c_double, C.c_void_p]),
+    # include/nd_gb300_selftest.h
+    "nd_selftest_exact_add": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    "nd_selftest_exact_scan": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
 }
 
 _lib = None

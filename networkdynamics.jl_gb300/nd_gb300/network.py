@@ -188,7 +188,8 @@ class Network:
         return out
 
     def set_sum_order(self, order: str) -> None:
-        code = {"sequential": capi.ND_ORDER_SEQUENTIAL, "tree": capi.ND_ORDER_TREE}[order]
+        code = {"sequential": capi.ND_ORDER_SEQUENTIAL, "tree": capi.ND_ORDER_TREE,
+                "sequential_hw": capi.ND_ORDER_SEQUENTIAL_HW}[order]
         capi.check(capi.load().nd_set_sum_order(self.handle, code))
 
     def __del__(self):

@@ -191,3 +191,20 @@ def test_full_size_ba10m_properties(cuda):
     assert abs(du.sum()) <= 1e-9 * np.abs(du).sum()
     del nw
     torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("vk,ek", [(O.V_DIFFUSION, O.E_DIFFUSION), (O.V_SWING, O.E_KURAMOTO)])
+def test_exact_integer_sums_equal_hardware_sums(cuda, vk, ek):
+    """The integer-exact adds / hub scan and hardware DADD chains give identical bits
+    (both are the sequential order); heavy rows (degree > 512) included."""
+    g = nd.barabasi_albert(300_000, 4, seed=21)
+    assert g.degree().max() > 512
+    nw = make(g, vk, ek, np.float64)
+    on = O.OracleNetwork.from_graph(g, vk, ek)
+    u, p = random_inputs(on, vk, np.random.default_rng(4))
+    exact = gpu_rhs(nw, u, p, cuda, np.float64)
+    nw.set_sum_order("sequential_hw")
+    hw = gpu_rhs(nw, u, p, cuda, np.float64)
+    np.testing.assert_array_equal(exact, hw)
+    if ek != O.E_KURAMOTO:
+        np.testing.assert_array_equal(exact, on.rhs(u, p))
