@@ -124,6 +124,14 @@ int nd_get_info(const nd_handle* h, nd_info* out);
 /* Select the aggregation order (enum nd_sum_order).  Default ND_ORDER_SEQUENTIAL. */
 int nd_set_sum_order(nd_handle* h, int order);
 
+/* Kernel layout of the RHS.  ND_LAYOUT_AUTO (default) evaluates each edge once in edge
+ * order and then sums the rows (two phases; needs the canonical edge list of an
+ * undirected Graphs.jl graph: sorted by source, src < dst); other edge lists, or
+ * ND_LAYOUT_FUSED, use one fused kernel over the destination-sorted CSR.  Both give the
+ * same bits. */
+enum nd_layout { ND_LAYOUT_AUTO = 0, ND_LAYOUT_FUSED = 1 };
+int nd_set_layout(nd_handle* h, int layout);
+
 /* One network right-hand side du = f(u, p, t), the method
  * `(nw::Network)(du, u, p, t)` (src/coreloop.jl:1-102) for RET=:du and no perturbation,
  * with SequentialAggregator(+) semantics (src/aggregators.jl:133-151).

@@ -35,7 +35,74 @@ void free_topology(Topology* t) {
     cudaFree(t->slot_vertex);
     cudaFree(t->incid);
     cudaFree(t->win_ptr);
+    EdgeLayout& el = t->edge;
+    cudaFree(el.esrc);
+    cudaFree(el.edst);
+    cudaFree(el.q);
+    cudaFree(el.dptr);
+    cudaFree(el.loc);
+    cudaFree(el.sptr);
+    cudaFree(el.y);
+    cudaFree(el.ybkt);
     *t = Topology{};
+}
+
+// Canonical edge list: sorted by source, src < dst for every edge.
+static bool is_canonical(int64_t ne, const int64_t* src, const int64_t* dst) {
+    for (int64_t e = 0; e < ne; ++e) {
+        if (src[e] >= dst[e]) return false;
+        if (e > 0 && src[e] < src[e - 1]) return false;
+    }
+    return true;
+}
+
+// Host side of the edge-centric layout (see EdgeLayout in nd_internal.h).
+struct EdgeLayoutHost {
+    std::vector<int32_t> esrc, edst, q, loc;
+    std::vector<uint32_t> dptr, sptr;
+    int64_t n_chunks = 0;
+};
+
+static void build_edge_layout(int64_t nv, int64_t ne, const int64_t* src, const int64_t* dst, EdgeLayoutHost& h) {
+    h.esrc.resize(ne);
+    h.edst.resize(ne);
+    h.dptr.assign(nv + 1, 0);
+    h.sptr.assign(nv + 1, 0);
+    for (int64_t e = 0; e < ne; ++e) {
+        h.esrc[e] = (int32_t)src[e];
+        h.edst[e] = (int32_t)dst[e];
+        h.dptr[dst[e] + 1]++;
+        h.sptr[src[e] + 1]++;
+    }
+    for (int64_t v = 0; v < nv; ++v) {
+        h.dptr[v + 1] += h.dptr[v];
+        h.sptr[v + 1] += h.sptr[v];
+    }
+    // destination-CSR position of each edge (ascending edge id inside a destination)
+    std::vector<uint32_t> tpos(ne);
+    {
+        std::vector<uint32_t> fill(h.dptr.begin(), h.dptr.end() - 1);
+        for (int64_t e = 0; e < ne; ++e) tpos[e] = fill[dst[e]]++;
+    }
+    // buckets of destination-CSR positions; ybkt is bucket-major, chunk-major inside a
+    // bucket, edge order inside a (bucket, chunk) run
+    const int64_t bsize = std::max<int64_t>(1, (ne + kBuckets - 1) / kBuckets);
+    h.n_chunks = (ne + kEdgeChunk - 1) / kEdgeChunk;
+    std::vector<int64_t> cnt((size_t)kBuckets * std::max<int64_t>(h.n_chunks, 1), 0);
+    for (int64_t e = 0; e < ne; ++e) cnt[(tpos[e] / bsize) * h.n_chunks + e / kEdgeChunk]++;
+    int64_t run = 0;
+    for (size_t i = 0; i < cnt.size(); ++i) {
+        const int64_t c = cnt[i];
+        cnt[i] = run;
+        run += c;
+    }
+    h.q.resize(ne);
+    h.loc.resize(ne);
+    for (int64_t e = 0; e < ne; ++e) {
+        const int64_t qe = cnt[(tpos[e] / bsize) * h.n_chunks + e / kEdgeChunk]++;
+        h.q[e] = (int32_t)qe;
+        h.loc[tpos[e]] = (int32_t)qe;
+    }
 }
 
 // Destination-sorted CSR.  Row v lists every edge incident to v in ascending edge id;
@@ -43,7 +110,8 @@ void free_topology(Topology* t) {
 // which SequentialAggregator visits the output buffer (src/aggregators.jl:140-151 over
 // the map of src/aggregators.jl:58-79: out ranges are laid out per edge as src then dst,
 // src/network_structure.jl:240-250), so a sequential per-row sum reproduces it bitwise.
-int build_topology(int64_t nv, int64_t ne, const int64_t* src, const int64_t* dst, Topology* topo) {
+int build_topology(int64_t nv, int64_t ne, const int64_t* src, const int64_t* dst, int edge_elem,
+                   Topology* topo) {
     if (nv <= 0) return fail(ND_ERR_ARG, "network has no vertices");
     if (ne < 0) return fail(ND_ERR_ARG, "negative edge count");
     if (nv > INT32_MAX - 1) return fail(ND_ERR_UNSUPPORTED, "more than 2^31-2 vertices");
@@ -153,6 +221,24 @@ int build_topology(int64_t nv, int64_t ne, const int64_t* src, const int64_t* ds
         free_topology(&t);
         return cuda_fail(err, "upload of the network topology");
     }
+    if (edge_elem > 0 && ne > 0 && is_canonical(ne, src, dst)) {
+        EdgeLayoutHost h;
+        build_edge_layout(nv, ne, src, dst, h);
+        EdgeLayout& el = t.edge;
+        el.n_chunks = h.n_chunks;
+        if ((err = upload((void**)&el.esrc, h.esrc.data(), h.esrc.size() * sizeof(int32_t))) != cudaSuccess ||
+            (err = upload((void**)&el.edst, h.edst.data(), h.edst.size() * sizeof(int32_t))) != cudaSuccess ||
+            (err = upload((void**)&el.q, h.q.data(), h.q.size() * sizeof(int32_t))) != cudaSuccess ||
+            (err = upload((void**)&el.dptr, h.dptr.data(), h.dptr.size() * sizeof(uint32_t))) != cudaSuccess ||
+            (err = upload((void**)&el.loc, h.loc.data(), h.loc.size() * sizeof(int32_t))) != cudaSuccess ||
+            (err = upload((void**)&el.sptr, h.sptr.data(), h.sptr.size() * sizeof(uint32_t))) != cudaSuccess ||
+            (err = cudaMalloc(&el.y, (size_t)ne * edge_elem)) != cudaSuccess ||
+            (err = cudaMalloc(&el.ybkt, (size_t)ne * edge_elem)) != cudaSuccess) {
+            free_topology(&t);
+            return cuda_fail(err, "upload of the edge-centric layout");
+        }
+        el.enabled = true;
+    }
     *topo = t;
     return ND_OK;
 }
@@ -193,10 +279,20 @@ int nd_create(const nd_network_desc* desc, int dtype, nd_handle** out) {
     h->coupling = desc->coupling;
     h->sum_order = ND_ORDER_SEQUENTIAL;
     h->rhs_mode = kModeExact;
+    h->edge_path = 1;
+    if (cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaError_t err = cudaGetLastError();
+        if (h->side) cudaStreamDestroy(h->side);
+        if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+        delete h;
+        return cuda_fail(err, "nd_create: stream / event creation");
+    }
     cudaGetDevice(&h->device);
     h->dim = desc->nv * vertex_dim(desc->vertex_kind);
     h->pdim = desc->nv * vertex_pdim(desc->vertex_kind) + desc->ne * edge_pdim(desc->edge_kind);
-    int rc = build_topology(desc->nv, desc->ne, desc->src, desc->dst, &h->topo);
+    int rc = build_topology(desc->nv, desc->ne, desc->src, desc->dst, dtype == ND_F64 ? 8 : 4, &h->topo);
     if (rc != ND_OK) {
         delete h;
         return rc;
@@ -211,7 +307,11 @@ int nd_destroy(nd_handle* h) {
     int prev = -1;
     cudaGetDevice(&prev);
     if (prev != h->device) cudaSetDevice(h->device);
+    if (h->side) cudaStreamSynchronize(h->side);
     free_topology(&h->topo);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (h->side) cudaStreamDestroy(h->side);
     if (prev >= 0 && prev != h->device) cudaSetDevice(prev);
     delete h;
     return ND_OK;
@@ -241,6 +341,14 @@ int nd_set_sum_order(nd_handle* h, int order) {
         return fail(ND_ERR_ARG, "nd_set_sum_order: unknown order");
     h->sum_order = order;
     h->rhs_mode = order == ND_ORDER_TREE ? kModeTree : (order == ND_ORDER_SEQUENTIAL_HW ? kModeNative : kModeExact);
+    return ND_OK;
+}
+
+int nd_set_layout(nd_handle* h, int layout) {
+    clear_error();
+    if (!h) return fail(ND_ERR_ARG, "nd_set_layout: NULL handle");
+    if (layout != ND_LAYOUT_AUTO && layout != ND_LAYOUT_FUSED) return fail(ND_ERR_ARG, "nd_set_layout: unknown layout");
+    h->edge_path = layout == ND_LAYOUT_AUTO;
     return ND_OK;
 }
 
@@ -278,7 +386,39 @@ int nd_rhs(nd_handle* h, int dtype, void* du, int64_t n_du, const void* u, int64
     a.vertex_kind = h->vertex_kind;
     a.edge_kind = h->edge_kind;
     a.mode = h->rhs_mode;
-    cudaError_t err = launch_rhs(h->dtype, a, (cudaStream_t)stream);
+    const EdgeLayout& el = h->topo.edge;
+    a.ne = h->topo.ne;
+    a.n_chunks = el.n_chunks;
+    a.esrc = el.esrc;
+    a.edst = el.edst;
+    a.q = el.q;
+    a.dptr = el.dptr;
+    a.loc = el.loc;
+    a.sptr = el.sptr;
+    a.y = el.y;
+    a.ybkt = el.ybkt;
+    a.heavy_only = 0;
+    a.heavy_separate = 0;
+    cudaStream_t s = (cudaStream_t)stream;
+    const bool edge = el.enabled && h->edge_path;
+    cudaError_t err;
+    if (h->topo.n_heavy > 0 && h->side) {
+        // Heavy rows run concurrently on the handle's side stream, one per SM, computed
+        // from u and p directly (they need nothing from the other kernels); fork / join
+        // with events so the call stays ordered on the caller's stream (and capturable).
+        a.heavy_separate = 1;
+        RhsArgs hv = a;
+        hv.heavy_only = 1;
+        if ((err = cudaEventRecord(h->ev_fork, s)) != cudaSuccess ||
+            (err = cudaStreamWaitEvent(h->side, h->ev_fork, 0)) != cudaSuccess ||
+            (err = launch_rhs(h->dtype, hv, h->side)) != cudaSuccess ||
+            (err = (edge ? launch_rhs_edge(h->dtype, a, s) : launch_rhs(h->dtype, a, s))) != cudaSuccess ||
+            (err = cudaEventRecord(h->ev_join, h->side)) != cudaSuccess ||
+            (err = cudaStreamWaitEvent(s, h->ev_join, 0)) != cudaSuccess)
+            return cuda_fail(err, "nd_rhs kernel launch");
+        return ND_OK;
+    }
+    err = edge ? launch_rhs_edge(h->dtype, a, s) : launch_rhs(h->dtype, a, s);
     if (err != cudaSuccess) return cuda_fail(err, "nd_rhs kernel launch");
     return ND_OK;
 }

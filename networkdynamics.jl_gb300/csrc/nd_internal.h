@@ -52,18 +52,49 @@ constexpr int kWindow = 256;
 // by degree.  slot_ptr indexes the incidences of a slot, slot_vertex names its vertex.
 constexpr int kWindowIncidences = 2048;  // light window: at most this many incidences
 
+// Edge-centric layout, used when the edge list is canonical: sorted by source with
+// src < dst for every edge, the order Graphs.jl's edges(g) gives for a SimpleGraph.
+// Then every row is [its dst-side edges, ascending] followed by [its own source block,
+// a contiguous edge range], so the RHS can run in two phases:
+//   E: each edge's value y_e = g(u_src, u_dst, p_e) once, in edge order, written to y
+//      (edge order) and to ybkt, the same values grouped into kBuckets buckets of
+//      destination-CSR positions (each block writes contiguous runs per bucket);
+//   R: each row sums its dst-side values (gathered from one bucket, which stays in L2
+//      while the rows of that range run) and then -y over its source block.
+// Each edge's function is evaluated once instead of twice, and the edge parameters and
+// the incidence stream are read in order instead of gathered.
+constexpr int kEdgeChunk = 4096;  // edges per phase-E block
+constexpr int kBuckets = 64;
+
+struct EdgeLayout {
+    bool enabled = false;
+    int64_t n_chunks = 0;
+    int32_t* esrc = nullptr;   // [ne]
+    int32_t* edst = nullptr;   // [ne]
+    int32_t* q = nullptr;      // [ne] position of edge e's value in ybkt
+    uint32_t* dptr = nullptr;  // [nv+1] each vertex's range in destination-CSR order
+    int32_t* loc = nullptr;    // [ne] ybkt position of destination-CSR entry k
+    uint32_t* sptr = nullptr;  // [nv+1] each vertex's source block (edge ids)
+    void* y = nullptr;         // [ne] scratch, element type of the handle
+    void* ybkt = nullptr;      // [ne] scratch
+};
+
 struct Topology {
     int64_t nv = 0, ne = 0;
     int32_t max_degree = 0;
     uint32_t* slot_ptr = nullptr;    // [nv+1] offsets into incid, by slot
     int32_t* slot_vertex = nullptr;  // [nv] vertex of each slot
-    Incidence* incid = nullptr;      // [2ne] incidences in slot order, each row by edge id
+    Incidence* incid = nullptr;      // [2ne] incidences in slot order, each row by edge id (fused path)
     int32_t* win_ptr = nullptr;      // [n_windows+1] first slot of each light window
     int32_t n_light = 0, n_medium = 0, n_heavy = 0, n_windows = 0;
+    EdgeLayout edge;
 };
 
-// Build the CSR on the host and upload it.  src/dst are 0-based host arrays.
-int build_topology(int64_t nv, int64_t ne, const int64_t* src, const int64_t* dst, Topology* topo);
+// Build the CSR on the host and upload it.  src/dst are 0-based host arrays.  The
+// edge-centric layout is built too when the edge list is canonical and edge_elem > 0
+// (the scratch element size, 4 or 8 bytes).
+int build_topology(int64_t nv, int64_t ne, const int64_t* src, const int64_t* dst, int edge_elem,
+                   Topology* topo);
 void free_topology(Topology* topo);
 
 // Accumulation modes of the FP64 RHS.
@@ -85,10 +116,24 @@ struct RhsArgs {
     int32_t n_light, n_medium, n_heavy, n_windows;
     int32_t vertex_kind, edge_kind;
     int32_t mode;
+    int32_t heavy_only;      // launch_rhs: only the heavy rows, one per SM
+    int32_t heavy_separate;  // launch_rhs_edge: heavy rows are launched elsewhere
+    // edge-centric layout (see EdgeLayout)
+    int64_t ne, n_chunks;
+    const int32_t* esrc;
+    const int32_t* edst;
+    const int32_t* q;
+    const uint32_t* dptr;
+    const int32_t* loc;
+    const uint32_t* sptr;
+    void* y;
+    void* ybkt;
 };
 
 // Launch the fused RHS for the given element type.
 cudaError_t launch_rhs(int dtype, const RhsArgs& a, cudaStream_t stream);
+// Launch the two-phase (edge-centric) RHS.
+cudaError_t launch_rhs_edge(int dtype, const RhsArgs& a, cudaStream_t stream);
 
 cudaError_t launch_exact_selftest(const double* a, const double* b, double* out, int64_t n, cudaStream_t s);
 cudaError_t launch_scan_selftest(const double* terms, const int64_t* seg, const double* s0, double* out,
@@ -101,7 +146,10 @@ struct nd_handle {
     int vertex_kind, edge_kind, coupling;
     int sum_order;
     int rhs_mode;
+    int edge_path;  // use the two-phase layout when it exists (default on)
     int device;
+    cudaStream_t side = nullptr;  // heavy rows run here, forked from / joined to the caller's stream
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int64_t dim, pdim;
     nd::Topology topo;
 };

@@ -80,6 +80,7 @@ SIGNATURES = {
     "nd_destroy": (C.c_int, [C.c_void_p]),
     "nd_get_info": (C.c_int, [C.c_void_p, C.POINTER(nd_info)]),
     "nd_set_sum_order": (C.c_int, [C.c_void_p, C.c_int]),
+    "nd_set_layout": (C.c_int, [C.c_void_p, C.c_int]),
     "nd_rhs": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
                          C.c_void_p, C.c_int64, C.c_double, C.c_void_p]),
     # include/nd_gb300_selftest.h

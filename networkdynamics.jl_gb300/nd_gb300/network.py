@@ -192,6 +192,11 @@ class Network:
                 "sequential_hw": capi.ND_ORDER_SEQUENTIAL_HW}[order]
         capi.check(capi.load().nd_set_sum_order(self.handle, code))
 
+    def set_layout(self, layout: str) -> None:
+        """'auto' (two-phase edge-centric kernels for canonical edge lists) or 'fused'."""
+        code = {"auto": 0, "fused": 1}[layout]
+        capi.check(capi.load().nd_set_layout(self.handle, code))
+
     def __del__(self):
         h = getattr(self, "_handle", None)
         if h is not None and getattr(self, "_lib", None) is not None:
