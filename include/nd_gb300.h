@@ -145,6 +145,25 @@ int nd_set_layout(nd_handle* h, int layout);
 int nd_rhs(nd_handle* h, int dtype, void* du, int64_t n_du, const void* u, int64_t n_u,
            const void* p, int64_t n_p, double t, void* stream);
 
+/* Allocation-free RHS.  This entry point has no counterpart in the reference.  It is for
+ * callers that must not allocate device memory while they evaluate the RHS, for example
+ * code recording a solver step into a CUDA graph during a stream capture (where cudaMalloc
+ * is not allowed), or a process whose device memory belongs to a caching allocator.  It
+ * calls no cudaMalloc / cudaFree: the caller passes the topology as device arrays, and
+ * the edge values go to one file-scope device array of 64 MiB (8 Mi FP64 or 16 Mi FP32
+ * edges) that every GPU loading the library holds until the process exits.
+ *   edges  canonical list (sorted by source, src < dst): src[ne], dst[ne] (0-based int32)
+ *   src_ptr[nv+1]  first edge of each vertex's source block
+ *   dst_ptr[nv+1], dst_eid[ne]  each vertex's destination-side edge ids, ascending
+ *   du, u, p  as for nd_rhs, element type `dtype`
+ * Result: the same du as nd_rhs on the same network.  ne above the scratch size returns
+ * ND_ERR_ARG.  The first call on a device looks up the scratch array's device address
+ * (cudaGetSymbolAddress) and should come before any stream capture.  All calls share the
+ * scratch: calls that overlap on the GPU (other streams, other host threads) race. */
+int nd_rhs_static_scratch(int dtype, int vertex_kind, int edge_kind, int64_t nv, int64_t ne, const int32_t* src,
+                          const int32_t* dst, const uint32_t* src_ptr, const uint32_t* dst_ptr,
+                          const int32_t* dst_eid, void* du, const void* u, const void* p, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,153 @@
+// Allocation-free RHS entry point: nd_rhs_static_scratch (include/nd_gb300.h).
+//
+// Who needs it: a caller that must not allocate device memory while it runs the RHS --
+// for example code that records the solver's step into a CUDA graph while a stream
+// capture is open (cudaMalloc is not allowed inside the capture), or a process whose
+// device memory is entirely owned by a caching allocator (CUDA.jl's or PyTorch's pool),
+// where a stray cudaMalloc from a library can fail or fragment the pool.  nd_create
+// allocates the network's topology and its scratch; this entry point allocates nothing:
+// the caller passes the topology arrays and the input / output buffers, and the scratch
+// comes from one file-scope __device__ array of fixed size.
+//
+// The computation is the two-phase RHS of nd_rhs_edge.cu in its simplest form: phase E
+// writes each edge's value y_e = g(u_src, u_dst, p_e) to the scratch array, phase R sums
+// every vertex's destination-side values (ascending edge id) and then the negated values
+// of its source block with hardware adds, in the reference's order, and applies vertex f.
+// Phase E writes every scratch entry phase R reads, so nothing needs clearing between
+// calls.
+#include <algorithm>
+#include <mutex>
+#include <string>
+
+#include "nd_components.cuh"
+#include "nd_internal.h"
+
+namespace nd {
+
+namespace {
+
+// The scratch: every GPU that loads this library holds it until the process exits.
+constexpr size_t kStaticScratchBytes = 64ull << 20;  // 64 MiB: 8 Mi FP64 / 16 Mi FP32 edge values
+__device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+void* g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of the scratch on the current device; looked up once per device.
+cudaError_t scratch_address(void** out) {
+    int dev = 0;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err != cudaSuccess) return err;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_ptr[dev]) {
+        void* p = nullptr;
+        err = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (err != cudaSuccess) return err;
+        g_scratch_ptr[dev] = p;
+    }
+    *out = g_scratch_ptr[dev];
+    return cudaSuccess;
+}
+
+template <typename T, int VK, int EK>
+__global__ void static_edge_kernel(int64_t nv, int64_t ne, const int32_t* __restrict__ src,
+                                   const int32_t* __restrict__ dst, const T* __restrict__ u,
+                                   const T* __restrict__ p, T* __restrict__ y) {
+    constexpr int DV = VertexDims<VK>::dim;
+    const T* __restrict__ pe = p + nv * VertexDims<VK>::pdim;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
+        const T us = __ldg(u + (int64_t)src[e] * DV), ud = __ldg(u + (int64_t)dst[e] * DV);
+        const T w = EK == ND_E_DIFFUSION_UNIT ? T(0) : __ldg(pe + e);
+        y[e] = edge_g_w<T, EK>(us, ud, w);
+    }
+}
+
+template <typename T, int VK, int EK>
+__global__ void static_row_kernel(int64_t nv, const uint32_t* __restrict__ src_ptr,
+                                  const uint32_t* __restrict__ dst_ptr, const int32_t* __restrict__ dst_eid,
+                                  const T* __restrict__ y, const T* __restrict__ u, const T* __restrict__ p,
+                                  T* __restrict__ du) {
+    using A = Arith<T>;
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+        T acc = T(0);
+        for (uint32_t k = dst_ptr[v]; k < dst_ptr[v + 1]; ++k) acc = A::add(acc, y[dst_eid[k]]);
+        for (uint32_t e = src_ptr[v]; e < src_ptr[v + 1]; ++e) acc = A::add(acc, -y[e]);
+        vertex_f<T, VK>(du, u, p, v, acc);
+    }
+}
+
+template <typename T, int VK, int EK>
+cudaError_t launch_static(int64_t nv, int64_t ne, const int32_t* src, const int32_t* dst, const uint32_t* src_ptr,
+                          const uint32_t* dst_ptr, const int32_t* dst_eid, void* du, const void* u, const void* p,
+                          void* scratch, cudaStream_t s) {
+    const int block = 256;
+    const unsigned ge = (unsigned)std::min<int64_t>((ne + block - 1) / block, 152 * 16);
+    const unsigned gv = (unsigned)std::min<int64_t>((nv + block - 1) / block, 152 * 16);
+    T* y = static_cast<T*>(scratch);
+    if (ne > 0)
+        static_edge_kernel<T, VK, EK><<<ge, block, 0, s>>>(nv, ne, src, dst, static_cast<const T*>(u),
+                                                           static_cast<const T*>(p), y);
+    static_row_kernel<T, VK, EK><<<gv, block, 0, s>>>(nv, src_ptr, dst_ptr, dst_eid, y, static_cast<const T*>(u),
+                                                      static_cast<const T*>(p), static_cast<T*>(du));
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_static_dtype(int vk, int ek, int64_t nv, int64_t ne, const int32_t* src, const int32_t* dst,
+                                const uint32_t* src_ptr, const uint32_t* dst_ptr, const int32_t* dst_eid, void* du,
+                                const void* u, const void* p, void* scratch, cudaStream_t s) {
+#define ND_CASE(VK, EK)            \
+    if (vk == VK && ek == EK)      \
+        return launch_static<T, VK, EK>(nv, ne, src, dst, src_ptr, dst_ptr, dst_eid, du, u, p, scratch, s);
+    ND_CASE(ND_V_DIFFUSION, ND_E_DIFFUSION)
+    ND_CASE(ND_V_DIFFUSION, ND_E_DIFFUSION_UNIT)
+    ND_CASE(ND_V_DIFFUSION, ND_E_KURAMOTO)
+    ND_CASE(ND_V_KURAMOTO, ND_E_DIFFUSION)
+    ND_CASE(ND_V_KURAMOTO, ND_E_DIFFUSION_UNIT)
+    ND_CASE(ND_V_KURAMOTO, ND_E_KURAMOTO)
+    ND_CASE(ND_V_SWING, ND_E_DIFFUSION)
+    ND_CASE(ND_V_SWING, ND_E_DIFFUSION_UNIT)
+    ND_CASE(ND_V_SWING, ND_E_KURAMOTO)
+#undef ND_CASE
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+}  // namespace nd
+
+using namespace nd;
+
+extern "C" int nd_rhs_static_scratch(int dtype, int vertex_kind, int edge_kind, int64_t nv, int64_t ne,
+                                     const int32_t* src, const int32_t* dst, const uint32_t* src_ptr,
+                                     const uint32_t* dst_ptr, const int32_t* dst_eid, void* du, const void* u,
+                                     const void* p, void* stream) {
+    clear_error();
+    if (dtype != ND_F32 && dtype != ND_F64) return fail(ND_ERR_DTYPE, "nd_rhs_static_scratch: dtype must be ND_F32 or ND_F64");
+    if (vertex_kind < ND_V_DIFFUSION || vertex_kind > ND_V_SWING || edge_kind < ND_E_DIFFUSION ||
+        edge_kind > ND_E_KURAMOTO)
+        return fail(ND_ERR_UNSUPPORTED_COMPONENT, "nd_rhs_static_scratch: component not in the GB300 library");
+    if (nv <= 0 || ne < 0) return fail(ND_ERR_ARG, "nd_rhs_static_scratch: nv must be > 0 and ne >= 0");
+    const size_t elem = dtype == ND_F64 ? 8 : 4;
+    const int64_t max_edges = (int64_t)(kStaticScratchBytes / elem);
+    if (ne > max_edges)
+        return fail(ND_ERR_ARG, "nd_rhs_static_scratch: " + std::to_string(ne) + " edges exceed the static scratch (" +
+                                    std::to_string(max_edges) + " edges of this precision, " +
+                                    std::to_string(kStaticScratchBytes >> 20) + " MiB); use nd_create / nd_rhs");
+    if (nv > INT32_MAX) return fail(ND_ERR_ARG, "nd_rhs_static_scratch: more than 2^31-1 vertices");
+    if (!du || !u || !src_ptr || !dst_ptr || (ne > 0 && (!src || !dst || !dst_eid)))
+        return fail(ND_ERR_ARG, "nd_rhs_static_scratch: NULL buffer");
+    const int pdim_v = vertex_pdim(vertex_kind), pdim_e = edge_pdim(edge_kind);
+    if ((pdim_v > 0 || (pdim_e > 0 && ne > 0)) && !p) return fail(ND_ERR_ARG, "nd_rhs_static_scratch: p is NULL");
+    void* scratch = nullptr;
+    cudaError_t err = scratch_address(&scratch);
+    if (err != cudaSuccess) return cuda_fail(err, "nd_rhs_static_scratch: cudaGetSymbolAddress");
+    err = dtype == ND_F64 ? launch_static_dtype<double>(vertex_kind, edge_kind, nv, ne, src, dst, src_ptr, dst_ptr,
+                                                        dst_eid, du, u, p, scratch, (cudaStream_t)stream)
+                          : launch_static_dtype<float>(vertex_kind, edge_kind, nv, ne, src, dst, src_ptr, dst_ptr,
+                                                       dst_eid, du, u, p, scratch, (cudaStream_t)stream);
+    if (err != cudaSuccess) return cuda_fail(err, "nd_rhs_static_scratch kernel launch");
+    return ND_OK;
+}

@@ -83,6 +83,9 @@ SIGNATURES = {
     "nd_set_layout": (C.c_int, [C.c_void_p, C.c_int]),
     "nd_rhs": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
                          C.c_void_p, C.c_int64, C.c_double, C.c_void_p]),
+    "nd_rhs_static_scratch": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p]),
     # include/nd_gb300_selftest.h
     "nd_selftest_exact_add": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     "nd_selftest_exact_scan": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),

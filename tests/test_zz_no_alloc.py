@@ -1,0 +1,91 @@
+"""The allocation-free RHS entry point (nd_rhs_static_scratch) against the regular one.
+
+nd_rhs_static_scratch serves callers that cannot allocate device memory while they run
+the RHS (a step being recorded into a CUDA graph, a process whose device memory belongs
+to a caching allocator).  It takes the topology as device arrays and keeps its edge
+values in a fixed file-scope device array.  Here it must reproduce nd_rhs on the same
+network, on two calls in a row (the second call reuses the scratch the first one left).
+This file runs last so a failure here never hides the other tests.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import nd_gb300 as nd
+from nd_gb300 import _capi as capi
+from oracle import oracle as O
+
+from ndtest import random_inputs
+
+MAX_F64_EDGES = (64 << 20) // 8
+
+
+def csr_arrays(g):
+    """src_ptr, dst_ptr, dst_eid of a canonical edge list (numpy, host)."""
+    src_ptr = np.zeros(g.nv + 1, dtype=np.uint32)
+    np.add.at(src_ptr, g.src + 1, 1)
+    src_ptr = np.cumsum(src_ptr).astype(np.uint32)
+    order = np.argsort(g.dst, kind="stable")  # edge ids grouped by destination, ascending within
+    dst_ptr = np.zeros(g.nv + 1, dtype=np.uint32)
+    np.add.at(dst_ptr, g.dst + 1, 1)
+    dst_ptr = np.cumsum(dst_ptr).astype(np.uint32)
+    return src_ptr, dst_ptr, order.astype(np.int32)
+
+
+def static_rhs(lib, vk, ek, g, dev_arrays, du, u, p, dtype_code):
+    src, dst, sp, dp, de = dev_arrays
+    return lib.nd_rhs_static_scratch(dtype_code, vk, ek, g.nv, g.ne, src.data_ptr(), dst.data_ptr(), sp.data_ptr(),
+                                     dp.data_ptr(), de.data_ptr(), du.data_ptr(), u.data_ptr(),
+                                     p.data_ptr() if p is not None else None, None)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("vk,ek,make_vm,make_em", [
+    (O.V_DIFFUSION, O.E_DIFFUSION, nd.diffusion_vertex, nd.diffusion_edge),
+    (O.V_KURAMOTO, O.E_KURAMOTO, nd.kuramoto_first, nd.kuramoto_edge),
+    (O.V_SWING, O.E_KURAMOTO, nd.kuramoto_second, nd.static_line),
+])
+def test_static_scratch_rhs_matches_nd_rhs(cuda, vk, ek, make_vm, make_em):
+    import torch
+    lib = capi.load()
+    g = nd.barabasi_albert(200_000, 4, seed=41)
+    src_ptr, dst_ptr, dst_eid = csr_arrays(g)
+    dev_arrays = [torch.from_numpy(np.ascontiguousarray(x)).to(cuda) for x in
+                  (g.src.astype(np.int32), g.dst.astype(np.int32), src_ptr.view(np.int32), dst_ptr.view(np.int32),
+                   dst_eid)]
+    nw = nd.adapt(nd.Network(g, make_vm(), make_em()), torch.float64)
+    on = O.OracleNetwork.from_graph(g, vk, ek)
+    rng = np.random.default_rng(12)
+    for call in range(2):  # two calls in a row: the second reuses the scratch left by the first
+        u_h, p_h = random_inputs(on, vk, rng)
+        u = torch.from_numpy(u_h).to(cuda)
+        p = torch.from_numpy(p_h).to(cuda)
+        ref = torch.empty_like(u)
+        nw(ref, u, p, 0.0)
+        got = torch.full_like(u, float("nan"))
+        capi.check(static_rhs(lib, vk, ek, g, dev_arrays, got, u, p, capi.ND_F64))
+        torch.cuda.synchronize()
+        # same operations in the same order as nd_rhs: identical bits
+        np.testing.assert_array_equal(got.cpu().numpy(), ref.cpu().numpy())
+    # FP32: within the FP32 tolerance of the parity tests (the regular path adds long rows
+    # with compensated sums)
+    nw32 = nd.adapt(nd.Network(g, make_vm(), make_em()), torch.float32)
+    u32 = u.float()
+    p32 = p.float()
+    ref32 = torch.empty_like(u32)
+    nw32(ref32, u32, p32, 0.0)
+    got32 = torch.empty_like(u32)
+    capi.check(static_rhs(lib, vk, ek, g, dev_arrays, got32, u32, p32, capi.ND_F32))
+    terms = on.abs_terms(u32.double().cpu().numpy(), p32.double().cpu().numpy())
+    d = np.abs(got32.double().cpu().numpy() - ref32.double().cpu().numpy())
+    assert np.all(d <= 4e-6 * (terms + np.abs(ref32.double().cpu().numpy())))
+
+
+@pytest.mark.gpu
+def test_static_scratch_rejects_oversized_networks(cuda):
+    lib = capi.load()
+    code = lib.nd_rhs_static_scratch(capi.ND_F64, capi.ND_V_DIFFUSION, capi.ND_E_DIFFUSION, 10, MAX_F64_EDGES + 1,
+                                     None, None, None, None, None, None, None, None, None)
+    assert code == capi.ND_ERR_ARG
+    assert "exceed the static scratch" in capi.last_error()
