@@ -145,6 +145,27 @@ int nd_set_layout(nd_handle* h, int layout);
 int nd_rhs(nd_handle* h, int dtype, void* du, int64_t n_du, const void* u, int64_t n_u,
            const void* p, int64_t n_p, double t, void* stream);
 
+/* Result of a solve. */
+typedef struct nd_solve_stats {
+    int64_t naccept; /* accepted steps                               */
+    int64_t nreject; /* rejected steps                               */
+    int64_t nf;      /* RHS evaluations                              */
+    double t_final;  /* time reached                                 */
+    double dt_last;  /* last proposed step size                      */
+    int32_t status;  /* ND_OK, ND_ERR_MAXITERS or ND_ERR_NOT_CONVERGED */
+    int32_t reserved;
+} nd_solve_stats;
+
+/* Integrate du/dt = f(u, p, t) from t0 to t1 with Tsit5 (Tsitouras 2011) and adaptive
+ * steps on the GPU: `solve(ODEProblem(nw, u0, (t0, t1), p), Tsit5(); reltol, abstol)`
+ * (src/post_utils.jl:43-100; the stepper of OrdinaryDiffEqTsit5).  u (device, FP64, length
+ * dim) holds u0 on entry and u(t1) on return; the state, stage vectors, error norm and
+ * step control are FP64, the RHS runs in the handle's precision.  Error norm: RMS of
+ * err_i / (abstol + reltol max(|u_i|, |u_new_i|)); PI step control.  max_steps <= 0: no
+ * limit.  Synchronous: returns when the solve has finished (ordered after `stream`). */
+int nd_solve_tsit5(nd_handle* h, double* u, const void* p, double t0, double t1, double reltol, double abstol,
+                   int64_t max_steps, nd_solve_stats* stats, void* stream);
+
 /* Allocation-free RHS.  This entry point has no counterpart in the reference.  It is for
  * callers that must not allocate device memory while they evaluate the RHS, for example
  * code recording a solver step into a CUDA graph during a stream capture (where cudaMalloc

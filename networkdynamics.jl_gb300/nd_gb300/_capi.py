@@ -152,3 +152,12 @@ def load_graphgen():
                                             C.POINTER(C.c_double)]
     _graphgen = lib
     return lib
+
+
+class nd_solve_stats(C.Structure):
+    _fields_ = [("naccept", C.c_int64), ("nreject", C.c_int64), ("nf", C.c_int64), ("t_final", C.c_double),
+                ("dt_last", C.c_double), ("status", C.c_int32), ("reserved", C.c_int32)]
+
+
+SIGNATURES["nd_solve_tsit5"] = (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double,
+                                          C.c_double, C.c_int64, C.POINTER(nd_solve_stats), C.c_void_p])
