@@ -185,6 +185,62 @@ int nd_rhs_static_scratch(int dtype, int vertex_kind, int edge_kind, int64_t nv,
                           const int32_t* dst, const uint32_t* src_ptr, const uint32_t* dst_ptr,
                           const int32_t* dst_eid, void* du, const void* u, const void* p, void* stream);
 
+
+/* ---------------------------------------------------------------------------------
+ * Ensembles: many instances of one vertex / edge model pair on different graphs (the
+ * basin-stability and parameter-sweep workloads).  Instance i has vertices
+ * [v_offset[i], v_offset[i+1]) and edges [e_offset[i], e_offset[i+1]) of the packed
+ * numbering, its edges given with LOCAL 0-based endpoints in edges(g) order.  The packed
+ * u / du / p are the instances' reference layouts one after another (p: instance i's
+ * vertex parameters, then its edge parameters).  No counterpart in the reference, where
+ * an ensemble is a loop of solve() calls (EnsembleProblem in SciML).
+ * ------------------------------------------------------------------------------- */
+typedef struct nd_ensemble_desc {
+    int64_t n_instances;
+    const int64_t* v_offset; /* [n+1] host */
+    const int64_t* e_offset; /* [n+1] host */
+    const int64_t* src;      /* [e_offset[n]] host, local endpoints */
+    const int64_t* dst;
+    int32_t vertex_kind, edge_kind, coupling, flags;
+} nd_ensemble_desc;
+
+typedef struct nd_ensemble nd_ensemble;
+
+int nd_ensemble_create(const nd_ensemble_desc* desc, int dtype, nd_ensemble** out);
+int nd_ensemble_destroy(nd_ensemble* e);
+int nd_ensemble_get_info(const nd_ensemble* e, int64_t* dim, int64_t* pdim);
+
+/* du of every instance (each equal to nd_rhs on that instance). */
+int nd_ensemble_rhs(nd_ensemble* e, int dtype, void* du, const void* u, const void* p, void* stream);
+
+/* Every instance integrated from t0 to t1 by Tsit5 with its own adaptive steps (FP64
+ * state, error norm and control; RHS in the ensemble's precision), in one persistent
+ * kernel replayed from a CUDA graph.  u: packed FP64 device state (in: u0, out: u(t1)).
+ * status[i] (device int32): ND_OK, ND_ERR_MAXITERS (step budget max_steps, <= 0 = none)
+ * or ND_ERR_NOT_CONVERGED; nsteps[i] (device int64): steps taken.  threads per instance:
+ * 64/128/256/512, or 0 for the autotuned / default choice.  Stream-ordered. */
+int nd_ensemble_solve_tsit5(nd_ensemble* e, double* u, const void* p, double t0, double t1, double reltol,
+                            double abstol, int64_t max_steps, int threads, int32_t* status, int64_t* nsteps,
+                            void* stream);
+
+/* Autotuner: times a short solve (t0 .. t0 + t_probe) with each block size on a copy of
+ * u and keeps the fastest for threads = 0.  Synchronous. */
+int nd_ensemble_autotune(nd_ensemble* e, const double* u, const void* p, double t0, double t_probe, double reltol,
+                         double abstol, int* chosen, void* stream);
+int nd_ensemble_set_threads(nd_ensemble* e, int threads);
+
+/* Steady states of swing ensembles (the batched find_fixpoint,
+ * src/initialization.jl:44-144): Newton's method on the power balance at ω = 0, each
+ * step's linear system solved by conjugate gradients on the analytic Jacobian (the
+ * graph Laplacian weighted by K cos(θ_n - θ_v)), in the subspace orthogonal to the
+ * uniform phase shift.  u (packed FP64, device): initial θ in, steady state out (ω set
+ * to 0).  Stops at max |du| <= tol (the reference's residual maximum(abs.(resid))).
+ * Device outputs per instance: iters, resid, status (ND_OK / ND_ERR_MAXITERS /
+ * ND_ERR_NOT_CONVERGED) and, if not NULL, the CG iterations.  max_cg <= 0: 4 x the
+ * largest instance.  FP64 ensembles only.  Stream-ordered. */
+int nd_ensemble_fixpoint(nd_ensemble* e, double* u, const double* p, double tol, int max_newton, int max_cg,
+                         int32_t* iters, double* resid, int32_t* status, int32_t* cg_iters, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -161,3 +161,22 @@ class nd_solve_stats(C.Structure):
 
 SIGNATURES["nd_solve_tsit5"] = (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double,
                                           C.c_double, C.c_int64, C.POINTER(nd_solve_stats), C.c_void_p])
+
+
+class nd_ensemble_desc(C.Structure):
+    _fields_ = [("n_instances", C.c_int64), ("v_offset", C.POINTER(C.c_int64)), ("e_offset", C.POINTER(C.c_int64)),
+                ("src", C.POINTER(C.c_int64)), ("dst", C.POINTER(C.c_int64)), ("vertex_kind", C.c_int32),
+                ("edge_kind", C.c_int32), ("coupling", C.c_int32), ("flags", C.c_int32)]
+
+
+_vp, _i64, _d = C.c_void_p, C.c_int64, C.c_double
+SIGNATURES.update({
+    "nd_ensemble_create": (C.c_int, [C.POINTER(nd_ensemble_desc), C.c_int, C.POINTER(C.c_void_p)]),
+    "nd_ensemble_destroy": (C.c_int, [_vp]),
+    "nd_ensemble_get_info": (C.c_int, [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "nd_ensemble_rhs": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp]),
+    "nd_ensemble_solve_tsit5": (C.c_int, [_vp, _vp, _vp, _d, _d, _d, _d, _i64, C.c_int, _vp, _vp, _vp]),
+    "nd_ensemble_autotune": (C.c_int, [_vp, _vp, _vp, _d, _d, _d, _d, C.POINTER(C.c_int), _vp]),
+    "nd_ensemble_set_threads": (C.c_int, [_vp, C.c_int]),
+    "nd_ensemble_fixpoint": (C.c_int, [_vp, _vp, _vp, _d, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),
+})

@@ -1,0 +1,124 @@
+"""Ensembles of networks on the GPU: many instances of one component pair on different
+graphs (basin-stability perturbations, parameter sweeps), packed one after another.
+
+Each instance keeps the reference's flat layout, so ``ens.u_slice(i)`` / ``ens.p_slice(i)``
+of the packed vectors are exactly the ``u`` / ``p`` of ``Network(graphs[i], vm, em)``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _capi as capi
+from .components import EdgeModel, VertexModel
+from .network import _dtype_code
+
+
+@dataclass
+class EnsembleSolveResult:
+    u: object          # packed FP64 CUDA tensor
+    status: np.ndarray  # per instance nd_status
+    nsteps: np.ndarray  # per instance steps
+
+
+@dataclass
+class FixpointResult:
+    u: object
+    iters: np.ndarray
+    resid: np.ndarray
+    status: np.ndarray
+    cg_iters: np.ndarray
+
+
+class Ensemble:
+    def __init__(self, graphs, vertexm: VertexModel, edgem: EdgeModel, dtype):
+        import torch
+        if vertexm.kind is None or edgem.kind is None:
+            raise capi.UnsupportedComponentError(capi.ND_ERR_UNSUPPORTED_COMPONENT,
+                                                 "ensemble components must come from the GB300 library")
+        self.graphs = list(graphs)
+        self.vertexm, self.edgem = vertexm, edgem
+        self.n = len(self.graphs)
+        nvs = np.array([g.nv for g in self.graphs], dtype=np.int64)
+        nes = np.array([g.ne for g in self.graphs], dtype=np.int64)
+        self.v_offset = np.concatenate([[0], np.cumsum(nvs)]).astype(np.int64)
+        self.e_offset = np.concatenate([[0], np.cumsum(nes)]).astype(np.int64)
+        src = np.concatenate([g.src for g in self.graphs]).astype(np.int64) if nes.sum() else np.zeros(1, np.int64)
+        dst = np.concatenate([g.dst for g in self.graphs]).astype(np.int64) if nes.sum() else np.zeros(1, np.int64)
+        P = C.POINTER(C.c_int64)
+        desc = capi.nd_ensemble_desc(self.n, self.v_offset.ctypes.data_as(P), self.e_offset.ctypes.data_as(P),
+                                     src.ctypes.data_as(P), dst.ctypes.data_as(P), vertexm.kind, edgem.kind,
+                                     capi.ND_ANTISYMMETRIC, 0)
+        self._lib = capi.load()
+        h = C.c_void_p()
+        capi.check(self._lib.nd_ensemble_create(C.byref(desc), _dtype_code(dtype), C.byref(h)))
+        self._h = h
+        self.dtype_code = _dtype_code(dtype)
+        self.torch_dtype = torch.float64 if self.dtype_code == capi.ND_F64 else torch.float32
+        dim, pdim = C.c_int64(), C.c_int64()
+        capi.check(self._lib.nd_ensemble_get_info(h, C.byref(dim), C.byref(pdim)))
+        self.dim, self.pdim = dim.value, pdim.value
+        self.u_offset = self.v_offset * vertexm.dim
+        self.p_offset = self.v_offset * vertexm.pdim + self.e_offset * edgem.pdim
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None:
+            try:
+                self._lib.nd_ensemble_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def u_slice(self, i):
+        return slice(int(self.u_offset[i]), int(self.u_offset[i + 1]))
+
+    def p_slice(self, i):
+        return slice(int(self.p_offset[i]), int(self.p_offset[i + 1]))
+
+    def _stream(self, stream):
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream()
+        return C.c_void_p(s.cuda_stream)
+
+    def rhs(self, du, u, p, stream=None):
+        capi.check(self._lib.nd_ensemble_rhs(self._h, self.dtype_code, du.data_ptr(), u.data_ptr(),
+                                             p.data_ptr() if p is not None else None, self._stream(stream)))
+
+    def solve_tsit5(self, u0, p, tspan, reltol=1e-6, abstol=1e-8, max_steps=0, threads=0, stream=None):
+        import torch
+        u = u0.to(torch.float64).clone() if isinstance(u0, torch.Tensor) else torch.tensor(u0, dtype=torch.float64,
+                                                                                           device="cuda")
+        dev = u.device
+        status = torch.zeros(self.n, dtype=torch.int32, device=dev)
+        nsteps = torch.zeros(self.n, dtype=torch.int64, device=dev)
+        capi.check(self._lib.nd_ensemble_solve_tsit5(self._h, u.data_ptr(), p.data_ptr() if p is not None else None,
+                                                     float(tspan[0]), float(tspan[1]), float(reltol), float(abstol),
+                                                     int(max_steps), int(threads), status.data_ptr(),
+                                                     nsteps.data_ptr(), self._stream(stream)))
+        return EnsembleSolveResult(u, status, nsteps)
+
+    def autotune(self, u0, p, t0=0.0, t_probe=0.5, reltol=1e-6, abstol=1e-8, stream=None):
+        chosen = C.c_int()
+        capi.check(self._lib.nd_ensemble_autotune(self._h, u0.data_ptr(), p.data_ptr() if p is not None else None,
+                                                  float(t0), float(t_probe), float(reltol), float(abstol),
+                                                  C.byref(chosen), self._stream(stream)))
+        return chosen.value
+
+    def set_threads(self, threads):
+        capi.check(self._lib.nd_ensemble_set_threads(self._h, int(threads)))
+
+    def fixpoint(self, u0, p, tol=1e-10, max_newton=50, max_cg=0, stream=None):
+        import torch
+        u = u0.to(torch.float64).clone()
+        dev = u.device
+        iters = torch.zeros(self.n, dtype=torch.int32, device=dev)
+        resid = torch.zeros(self.n, dtype=torch.float64, device=dev)
+        status = torch.zeros(self.n, dtype=torch.int32, device=dev)
+        cg = torch.zeros(self.n, dtype=torch.int32, device=dev)
+        capi.check(self._lib.nd_ensemble_fixpoint(self._h, u.data_ptr(), p.data_ptr(), float(tol), int(max_newton),
+                                                  int(max_cg), iters.data_ptr(), resid.data_ptr(), status.data_ptr(),
+                                                  cg.data_ptr(), self._stream(stream)))
+        return FixpointResult(u, iters, resid, status, cg)

@@ -1,0 +1,131 @@
+"""Batched ensembles against the single-network path and the CPU oracle."""
+import numpy as np
+import pytest
+
+import nd_gb300 as nd
+from nd_gb300.ensemble import Ensemble
+from nd_gb300.solve import solve_tsit5
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def swing_params(g, rng):
+    P = rng.uniform(0.5, 1.5, g.nv) * np.where(np.arange(g.nv) % 2 == 0, 1, -1)
+    P -= P.mean()
+    pv = np.stack([np.ones(g.nv), np.full(g.nv, 0.1), P], 1).ravel()
+    return np.concatenate([pv, rng.uniform(5, 10, g.ne)])
+
+
+def make_graphs(rng, n, lo=20, hi=400):
+    gs = []
+    for i in range(n):
+        nv = int(rng.integers(lo, hi))
+        if i % 2:
+            gs.append(nd.random_geometric(nv, np.sqrt(6.0 / (np.pi * nv)), seed=100 + i))
+        else:
+            gs.append(nd.barabasi_albert(nv, 2, seed=200 + i))
+    return gs
+
+
+def packed(ens, parts):
+    return np.concatenate(parts)
+
+
+def test_ensemble_rhs_equals_per_instance_rhs(cuda):
+    import torch
+    rng = np.random.default_rng(1)
+    gs = make_graphs(rng, 12)
+    ens = Ensemble(gs, nd.kuramoto_second(), nd.static_line(), torch.float64)
+    us, ps = [], []
+    for g in gs:
+        u = np.empty(2 * g.nv)
+        u[0::2] = rng.uniform(-np.pi, np.pi, g.nv)
+        u[1::2] = rng.normal(size=g.nv)
+        us.append(u)
+        ps.append(swing_params(g, rng))
+    u = torch.from_numpy(np.concatenate(us)).to(cuda)
+    p = torch.from_numpy(np.concatenate(ps)).to(cuda)
+    du = torch.empty_like(u)
+    ens.rhs(du, u, p)
+    got = du.cpu().numpy()
+    for i, g in enumerate(gs):
+        nw = nd.adapt(nd.Network(g, nd.kuramoto_second(), nd.static_line()), torch.float64)
+        ref = torch.empty(nw.dim, dtype=torch.float64, device=cuda)
+        nw(ref, u[ens.u_slice(i)].contiguous(), p[ens.p_slice(i)].contiguous(), 0.0)
+        np.testing.assert_array_equal(got[ens.u_slice(i)], ref.cpu().numpy())
+
+
+def test_ensemble_tsit5_matches_single_and_oracle(cuda):
+    import torch
+    rng = np.random.default_rng(2)
+    gs = make_graphs(rng, 10, 20, 200)
+    us, ps = [], []
+    for g in gs:
+        u = np.zeros(2 * g.nv)
+        u[0::2] = rng.uniform(-0.5, 0.5, g.nv)
+        us.append(u)
+        ps.append(swing_params(g, rng))
+    u0 = torch.from_numpy(np.concatenate(us)).to(cuda)
+    p = torch.from_numpy(np.concatenate(ps)).to(cuda)
+    ens = Ensemble(gs, nd.kuramoto_second(), nd.static_line(), torch.float64)
+    res = ens.solve_tsit5(u0, p, (0.0, 3.0), reltol=1e-6, abstol=1e-8)
+    assert (res.status.cpu().numpy() == 0).all()
+    got = res.u.cpu().numpy()
+    for i, g in enumerate(gs):
+        on = O.OracleNetwork.from_graph(g, O.V_SWING, O.E_KURAMOTO)
+        ref, st = on.tsit5(us[i], ps[i], 0.0, 3.0, reltol=1e-6, abstol=1e-8)
+        assert abs(int(res.nsteps[i]) - (st.naccept + st.nreject)) <= 2
+        np.testing.assert_allclose(got[ens.u_slice(i)], ref, atol=1e-7, rtol=0)
+    # FP32 RHS, FP64 state: close to the FP64 ensemble
+    ens32 = Ensemble(gs, nd.kuramoto_second(), nd.static_line(), torch.float32)
+    r32 = ens32.solve_tsit5(u0, p.float(), (0.0, 3.0), reltol=1e-6, abstol=1e-8)
+    assert (r32.status.cpu().numpy() == 0).all()
+    assert np.max(np.abs(r32.u.cpu().numpy() - got)) < 1e-3
+    # the autotuner picks a legal block size and the solve with it agrees
+    chosen = ens.autotune(u0, p, 0.0, 0.2)
+    assert chosen in (64, 128, 256, 512)
+    res2 = ens.solve_tsit5(u0, p, (0.0, 3.0), reltol=1e-6, abstol=1e-8)
+    np.testing.assert_allclose(res2.u.cpu().numpy(), got, atol=1e-12, rtol=0)
+
+
+def test_ensemble_step_budget_reports_status(cuda):
+    import torch
+    rng = np.random.default_rng(3)
+    gs = make_graphs(rng, 4, 30, 60)
+    u0 = torch.from_numpy(np.concatenate([np.concatenate([[0.3, 0.0]] * g.nv) for g in gs])).to(cuda)
+    p = torch.from_numpy(np.concatenate([swing_params(g, rng) for g in gs])).to(cuda)
+    ens = Ensemble(gs, nd.kuramoto_second(), nd.static_line(), torch.float64)
+    res = ens.solve_tsit5(u0, p, (0.0, 50.0), reltol=1e-10, abstol=1e-12, max_steps=3)
+    assert (res.status.cpu().numpy() == nd.capi.ND_ERR_MAXITERS).all()
+    assert (res.nsteps.cpu().numpy() == 3).all()
+
+
+def test_fixpoint_known_answer_and_oracle(cuda):
+    import torch
+    # 4-node swing of test/initialization_test.jl:15-38 (asin(1/12) phase steps)
+    g4 = nd.cycle_graph(4)
+    P = np.array([1.0, -1.0, 1.0, -1.0])
+    p4 = np.concatenate([np.stack([np.ones(4), np.full(4, 0.1), P], 1).ravel(), np.full(4, 6.0)])
+    rng = np.random.default_rng(4)
+    gs = [g4] + [nd.barabasi_albert(200, 2, seed=300 + i) for i in range(6)]
+    ps = [p4] + [swing_params(g, rng) for g in gs[1:]]
+    ens = Ensemble(gs, nd.kuramoto_second(), nd.static_line(), torch.float64)
+    u0 = torch.zeros(ens.dim, dtype=torch.float64, device=cuda)
+    p = torch.from_numpy(np.concatenate(ps)).to(cuda)
+    r = ens.fixpoint(u0, p, tol=1e-10)
+    assert (r.status.cpu().numpy() == 0).all()
+    assert (r.resid.cpu().numpy() <= 1e-10).all()
+    u = r.u.cpu().numpy()
+    th4 = u[ens.u_slice(0)][0::2]
+    np.testing.assert_allclose(np.abs(np.diff(th4)), np.arcsin(1 / 12), atol=1e-12)
+    for i in range(1, len(gs)):
+        g = gs[i]
+        pv = ps[i][:3 * g.nv].reshape(-1, 3)
+        th_ref, it_ref, _ = O.newton_fixpoint(g.nv, g.src, g.dst, ps[i][3 * g.nv:], pv[:, 2], tol=1e-12)
+        th = u[ens.u_slice(i)][0::2]
+        np.testing.assert_allclose(th - th[0], th_ref - th_ref[0], atol=1e-9)
+        # the full RHS vanishes at the steady state
+        on = O.OracleNetwork.from_graph(g, O.V_SWING, O.E_KURAMOTO)
+        assert np.max(np.abs(on.rhs(u[ens.u_slice(i)], ps[i]))) <= 1e-10
+        assert int(r.iters[i]) <= it_ref + 2
