@@ -145,6 +145,12 @@ int nd_set_layout(nd_handle* h, int layout);
 int nd_rhs(nd_handle* h, int dtype, void* du, int64_t n_du, const void* u, int64_t n_u,
            const void* p, int64_t n_p, double t, void* stream);
 
+/* Analytic Jacobian-vector product jv = (∂f/∂u)(u, p, t) · v of the RHS, replacing the
+ * ForwardDiff Dual-number pass through the core loop (src/coreloop.jl:10-21) for the
+ * library components.  jv, u, v: device, length dim; p: device, length pdim; element type
+ * of the handle.  Stream-ordered. */
+int nd_jvp(nd_handle* h, int dtype, void* jv, const void* u, const void* p, const void* v, double t, void* stream);
+
 /* Result of a solve. */
 typedef struct nd_solve_stats {
     int64_t naccept; /* accepted steps                               */

@@ -1,0 +1,95 @@
+// Analytic Jacobian-vector product of the network RHS, jv = (∂f/∂u)(u, p) · v.
+//
+// The reference differentiates the core loop with ForwardDiff (Dual numbers through
+// src/coreloop.jl, cache promotion at :10-21; tested against finite differences in
+// test/AD_test.jl:54-60).  For the library components the derivative is written out:
+//   diffusion edge    d[w (u_s - u_d)]      = w (v_s - v_d)
+//   unit diffusion    d[u_s - u_d]          = v_s - v_d
+//   kuramoto / line   d[K sin(θ_s - θ_d)]   = K cos(θ_s - θ_d) (v_s - v_d)
+// and AntiSymmetric hands -d(y_dst) to the source, so at row v with neighbour n every
+// incidence contributes c (v_n - v_v) with c = w, 1 or K cos(θ_n - θ_v).  Vertices:
+//   diffusion / kuramoto   jv = Σ                  swing   jv_θ = v_ω,  jv_ω = (Σ - D v_ω) / M
+// One thread per row over the slot-ordered CSR, rows summed in edge order.
+#include <algorithm>
+
+#include "nd_components.cuh"
+#include "nd_internal.h"
+
+namespace nd {
+
+namespace {
+
+template <typename T, int VK, int EK>
+__global__ void jvp_kernel(int64_t nv, const uint32_t* __restrict__ slot_ptr, const int32_t* __restrict__ slot_vertex,
+                           const int2* __restrict__ incid, const T* __restrict__ u, const T* __restrict__ p,
+                           const T* __restrict__ vv, T* __restrict__ jv) {
+    using A = Arith<T>;
+    constexpr int DV = VertexDims<VK>::dim;
+    const T* pv = p;
+    const T* pe = p + nv * VertexDims<VK>::pdim;
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < nv; s += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t v = slot_vertex[s];
+        const T uv = u[v * DV], dv = vv[v * DV];
+        T acc = T(0);
+        for (uint32_t k = slot_ptr[s]; k < slot_ptr[s + 1]; ++k) {
+            const int2 inc = incid[k];
+            const int64_t n = inc.x;
+            const int32_t e = inc.y & 0x7fffffff;
+            T c;
+            if constexpr (EK == ND_E_DIFFUSION) c = pe[e];
+            else if constexpr (EK == ND_E_DIFFUSION_UNIT) c = T(1);
+            else c = A::mul(pe[e], A::cos_phase(A::sub(u[n * DV], uv)));
+            acc = A::add(acc, A::mul(c, A::sub(vv[n * DV], dv)));
+        }
+        if constexpr (VK == ND_V_SWING) {
+            const T M = pv[3 * v], D = pv[3 * v + 1];
+            jv[2 * v] = vv[2 * v + 1];
+            jv[2 * v + 1] = A::div(A::sub(acc, A::mul(D, vv[2 * v + 1])), M);
+        } else {
+            jv[v] = acc;
+        }
+    }
+}
+
+template <typename T>
+cudaError_t launch_jvp(const nd_handle* h, const void* u, const void* p, const void* v, void* jv, cudaStream_t s) {
+    const Topology& t = h->topo;
+    const unsigned grid = (unsigned)std::min<int64_t>((t.nv + 255) / 256, 152 * 16);
+    const int2* inc = reinterpret_cast<const int2*>(t.incid);
+#define ND_CASE(VK, EK)                                                                                        \
+    if (h->vertex_kind == VK && h->edge_kind == EK) {                                                           \
+        jvp_kernel<T, VK, EK><<<grid, 256, 0, s>>>(t.nv, t.slot_ptr, t.slot_vertex, inc, static_cast<const T*>(u), \
+                                                  static_cast<const T*>(p), static_cast<const T*>(v),           \
+                                                  static_cast<T*>(jv));                                         \
+        return cudaGetLastError();                                                                              \
+    }
+    ND_CASE(ND_V_DIFFUSION, ND_E_DIFFUSION)
+    ND_CASE(ND_V_DIFFUSION, ND_E_DIFFUSION_UNIT)
+    ND_CASE(ND_V_DIFFUSION, ND_E_KURAMOTO)
+    ND_CASE(ND_V_KURAMOTO, ND_E_DIFFUSION)
+    ND_CASE(ND_V_KURAMOTO, ND_E_DIFFUSION_UNIT)
+    ND_CASE(ND_V_KURAMOTO, ND_E_KURAMOTO)
+    ND_CASE(ND_V_SWING, ND_E_DIFFUSION)
+    ND_CASE(ND_V_SWING, ND_E_DIFFUSION_UNIT)
+    ND_CASE(ND_V_SWING, ND_E_KURAMOTO)
+#undef ND_CASE
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+}  // namespace nd
+
+using namespace nd;
+
+extern "C" int nd_jvp(nd_handle* h, int dtype, void* jv, const void* u, const void* p, const void* v, double t,
+                      void* stream) {
+    (void)t;
+    clear_error();
+    if (!h || !jv || !u || !v) return fail(ND_ERR_ARG, "nd_jvp: NULL argument");
+    if (dtype != h->dtype) return fail(ND_ERR_DTYPE, "nd_jvp: element type differs from the handle's");
+    if (h->pdim > 0 && !p) return fail(ND_ERR_ARG, "nd_jvp: p is NULL");
+    cudaError_t err = h->dtype == ND_F64 ? launch_jvp<double>(h, u, p, v, jv, (cudaStream_t)stream)
+                                         : launch_jvp<float>(h, u, p, v, jv, (cudaStream_t)stream);
+    return err == cudaSuccess ? ND_OK : cuda_fail(err, "nd_jvp");
+}

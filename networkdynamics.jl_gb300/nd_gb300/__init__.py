@@ -10,7 +10,7 @@ from .components import (EdgeModel, VertexModel, diffusion_edge, diffusion_edge_
                          kuramoto_edge, kuramoto_first, kuramoto_second, static_line, swing_vertex)
 from .graphs import Graph, barabasi_albert, complete_graph, cycle_graph, random_geometric, simple_graph, watts_strogatz
 from .network import (ExecutionStyle, GB300Aggregator, GB300Execution, Network, adapt, get_aggr_constructor,
-                      iscudacompatible)
+                      iscudacompatible, jvp)
 
 __all__ = [
     "capi", "ArgumentError", "NDError", "NotConvergedError", "UnsupportedComponentError",
@@ -19,5 +19,5 @@ __all__ = [
     "Graph", "barabasi_albert", "complete_graph", "cycle_graph", "random_geometric", "simple_graph",
     "watts_strogatz",
     "ExecutionStyle", "GB300Aggregator", "GB300Execution", "Network", "adapt", "get_aggr_constructor",
-    "iscudacompatible",
+    "iscudacompatible", "jvp",
 ]

@@ -231,6 +231,15 @@ class Network:
         return None
 
 
+def jvp(nw: Network, jv, u, p, v, t=0.0, stream=None):
+    """jv = (∂f/∂u)(u, p, t) · v with the analytic library derivatives (CUDA tensors)."""
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    capi.check(nw._lib.nd_jvp(nw.handle, _dtype_code(u.dtype), jv.data_ptr(), u.data_ptr(),
+                              p.data_ptr() if p is not None else None, v.data_ptr(), float(t),
+                              C.c_void_p(s.cuda_stream)))
+
+
 def adapt(nw: Network, dtype) -> Network:
     """Counterpart of ``adapt(CuArray{T}, nw)``: a new Network whose handle lives on the
     current CUDA device with caches for element type `dtype` (float32 / float64)."""
