@@ -63,13 +63,40 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def profiled_traffic(dtype_tag, nv):
-    """DRAM bytes per launch from the committed ncu summary, if one exists for this workload."""
+def kernel_bytes(g, s):
+    """Algorithmic bytes (and FP64 lane operations) of one launch of each RHS kernel for
+    diffusion edges with s-byte values.
+      edge phase  per edge: src, dst, bucket slot (4 B each); u_src, u_dst, w, y, ybkt (s each)
+      row phase   per row: slot vertex, slot pointer, dptr pair, sptr (20 B) and du (s);
+                  per destination-side incidence loc (4 B) + ybkt (s); per source-side y (s)
+      heavy rows  per row: slot vertex, slot pointer pair (12 B), u_v and du (s each);
+                  per incidence the (nbr, eid) pair (8 B), u_nbr and w (s each)
+      fused       the whole RHS (algorithmic_bytes)
+    Rows of degree > 512 are the heavy rows."""
+    nv, ne = g.nv, g.ne
+    ndst = np.bincount(g.dst, minlength=nv)
+    nsrc = np.bincount(g.src, minlength=nv)
+    heavy = (ndst + nsrc) > 512
+    light = ~heavy
+    nh, inc_h = int(heavy.sum()), int((ndst + nsrc)[heavy].sum())
+    rows = int(light.sum()) * (20 + s) + int(ndst[light].sum()) * (4 + s) + int(nsrc[light].sum()) * s
+    return {
+        "edge_phase": (ne * (12 + 5 * s), 2 * ne),
+        "row_phase": (rows, int((ndst + nsrc)[light].sum())),
+        "heavy_rows": (nh * (12 + 2 * s) + inc_h * (8 + 2 * s), 3 * inc_h),
+        "fused": (algorithmic_bytes(nv, ne, s), 3 * 2 * ne),
+    }
+
+
+def profiled_traffic(dtype_tag, nv, kind):
+    """DRAM bytes per launch of `kind` from the committed ncu summary of this workload
+    (a line `traffic_bytes_per_launch <kind>: <bytes>`), or None."""
     f = ROOT / "profiles" / f"rhs_ba{nv // 1_000_000}m_{dtype_tag}.txt"
     if not f.exists():
         return None
+    key = f"traffic_bytes_per_launch {kind}:"
     for line in f.read_text().splitlines():
-        if line.startswith("traffic_bytes_per_launch:"):
+        if line.startswith(key):
             try:
                 return float(line.split(":", 1)[1].strip())
             except ValueError:
@@ -253,6 +280,7 @@ def run_gb300(args, rank, world, local):
     for _ in range(max(args.warmup, 3)):
         nw(du, u, p, 0.0)
     torch.cuda.synchronize()
+    nw.kernel_times()  # reset the launch counters
     barrier(world)
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
@@ -260,14 +288,33 @@ def run_gb300(args, rank, world, local):
         t = time_device(nw, du, u, p, args.steps, stream)
         torch.cuda.synchronize()
         barrier(world)
+    counts = nw.kernel_times()
     t = max_over_ranks(t, world, dev)
     ms = 1e3 * t / args.steps
     value = world * ne * args.steps / t
     hbm, peak_kind = peaks()
     B = algorithmic_bytes(nv, ne, 8)
-    achieved = B / (t / args.steps) / 1e9
-    launches_per_step = 1  # one fused RHS kernel per evaluation
-    traffic = profiled_traffic("f64", nv)
+    # per-kernel device times: the same RHS again with every launch bracketed by CUDA events
+    kt = min(args.steps, 500)
+    nw.set_kernel_timing(True)
+    time_device(nw, du, u, p, kt, stream)
+    times = nw.kernel_times()
+    nw.set_kernel_timing(False)
+    kb = kernel_bytes(g, 8)
+    kernels = {}
+    for kind, (n, tot) in times.items():
+        if n == 0:
+            continue
+        avg = tot / 1e3 / n
+        kbytes, kops = kb[kind]
+        kernels[kind] = {"launches": n, "avg_ms": 1e3 * avg, "share": None, "bytes_per_launch": kbytes,
+                         "achieved_gbs": kbytes / avg / 1e9, "fp64_lane_ops_per_launch": kops}
+    total_ms = sum(k["avg_ms"] * k["launches"] for k in kernels.values())
+    for k in kernels.values():
+        k["share"] = k["avg_ms"] * k["launches"] / total_ms if total_ms else None
+    dom = max(kernels, key=lambda k: kernels[k]["avg_ms"] * kernels[k]["launches"])
+    achieved = kernels[dom]["achieved_gbs"]
+    traffic = profiled_traffic("f64", nv, dom)
     line = {
         "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -278,11 +325,16 @@ def run_gb300(args, rank, world, local):
                    "l2": "no flush: inputs+topology %.2f GB > 129 MB L2" % (B / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "edges_per_s": value, "incidences_per_s": 2 * value, "rhs_evals_per_s": world * args.steps / t,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": traffic, "peak_kind": peak_kind,
-                     "note": "whole RHS (all launches of one step) timed with CUDA events; algorithmic "
-                             "bytes = 8(2N+E) + 4(N+1) + 16E"},
-        "gpu_launches": launches_per_step * args.steps,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
+                     "rhs_achieved_gbs": B / (t / args.steps) / 1e9, "rhs_frac": B / (t / args.steps) / 1e9 / hbm,
+                     "kernels": kernels,
+                     "note": "achieved = algorithmic bytes of one launch of the dominant kernel / its mean "
+                             "CUDA-event duration (%d event-bracketed RHS calls after the timed region); "
+                             "rhs_achieved_gbs = whole-RHS algorithmic bytes 8(2N+E) + 4(N+1) + 16E / "
+                             "timed ms_per_step" % kt},
+        "gpu_launches": sum(n for n, _ in counts.values()),
+        "gpu_launches_by_kernel": {k: n for k, (n, _) in counts.items() if n},
     }
     # the other FP64 summation modes, for comparison (same workload, fewer steps)
     ks = min(args.steps, 200)
@@ -292,7 +344,6 @@ def run_gb300(args, rank, world, local):
         nw(du, u, p, 0.0)
         tm = time_device(nw, du, u, p, ks, stream)
         modes[mode] = {"ms_per_step": 1e3 * tm / ks, "edges_per_s": ne * ks / tm}
-        line["gpu_launches"] += launches_per_step * (ks + 1)
     nw.set_sum_order("sequential")
     line["f64_modes"] = modes
     # FP32 variant (compensated sums at hubs)
@@ -312,7 +363,6 @@ def run_gb300(args, rank, world, local):
         line["f32"] = {"value": world * ne * args.steps / t32, "unit": "edges/s", "ms_per_step": 1e3 * t32 / args.steps,
                        "achieved_gbs": B32 / (t32 / args.steps) / 1e9,
                        "frac": B32 / (t32 / args.steps) / 1e9 / hbm, "max_abs_err_vs_f64": err}
-        line["gpu_launches"] += launches_per_step * args.steps
         del nw32, u32, p32, du32
     # end to end through the public API with pinned host buffers
     if not args.no_e2e:
@@ -341,7 +391,6 @@ def run_gb300(args, rank, world, local):
         line["e2e"] = {"value": world * ne * ke / te, "unit": "edges/s", "steps": ke,
                        "h2d_bytes_per_step": int(uh.numel() * 8 + ph.numel() * 8),
                        "d2h_bytes_per_step": int(duh.numel() * 8)}
-        line["gpu_launches"] += launches_per_step * ke
         ok = np.array_equal(duh.numpy(), du.cpu().numpy())
         line["e2e"]["result_matches_device"] = bool(ok)
     line["clocks"] = clk.summary()

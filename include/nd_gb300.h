@@ -132,6 +132,24 @@ int nd_set_sum_order(nd_handle* h, int order);
 enum nd_layout { ND_LAYOUT_AUTO = 0, ND_LAYOUT_FUSED = 1 };
 int nd_set_layout(nd_handle* h, int layout);
 
+/* Kernel accounting (no reference counterpart; a tracing aid like the reference's
+ * benchmark timers, benchmark/benchmark_utils.jl).  Every nd_rhs call counts the kernels
+ * it launches by kind.  With nd_set_kernel_timing(h, 1) it also brackets each launch with
+ * two CUDA events on the launching stream (heavy rows: the handle's side stream); the
+ * events make a captured graph record them too, so leave timing off while capturing.
+ * nd_kernel_times synchronizes the recorded events and writes, for kinds 0..n-1, the
+ * launches since the last call and their summed device time in ms (0 when timing was
+ * off), then resets both.  Recorded events stay in the handle's pool until that call. */
+enum nd_kernel_kind {
+    ND_KERNEL_EDGE_PHASE = 0, /* one thread per edge: edge outputs y, bucketed by destination */
+    ND_KERNEL_ROW_PHASE = 1,  /* row sums over y + vertex functions (light and medium rows) */
+    ND_KERNEL_HEAVY_ROWS = 2, /* rows of degree > 512, a block per row on the side stream */
+    ND_KERNEL_FUSED = 3,      /* single-kernel RHS (ND_LAYOUT_FUSED or non-canonical edges) */
+    ND_KERNEL_KINDS = 4
+};
+int nd_set_kernel_timing(nd_handle* h, int on);
+int nd_kernel_times(nd_handle* h, int64_t* launches, double* ms, int n);
+
 /* One network right-hand side du = f(u, p, t), the method
  * `(nw::Network)(du, u, p, t)` (src/coreloop.jl:1-102) for RET=:du and no perturbation,
  * with SequentialAggregator(+) semantics (src/aggregators.jl:133-151).
@@ -246,6 +264,36 @@ int nd_ensemble_set_threads(nd_ensemble* e, int threads);
  * largest instance.  FP64 ensembles only.  Stream-ordered. */
 int nd_ensemble_fixpoint(nd_ensemble* e, double* u, const double* p, double tol, int max_newton, int max_cg,
                          int32_t* iters, double* resid, int32_t* status, int32_t* cg_iters, void* stream);
+
+/* ---------------------------------------------------------------------------------
+ * Learned warm start (no reference counterpart: find_fixpoint, src/initialization.jl:44-144,
+ * starts Newton from the guess its caller passes; a prediction of this network is such a
+ * guess).  A message-passing network on one fixed graph maps per-instance vertex power
+ * injections P [batch][nv] and line weights K [batch][ne] (edges in the given order) to
+ * steady-state phases θ [batch][nv], centred per instance; the steady-state frequencies
+ * of swing vertices are 0.  FP32 throughout, hidden width 64, `layers` residual
+ * message-passing layers.  Parameters, gradients and Adam moments live on the device;
+ * every pointer below is a device pointer (params copies accept host pointers too).
+ * ------------------------------------------------------------------------------- */
+typedef struct nd_mpnn nd_mpnn;
+
+/* Seeded Glorot-uniform initialisation.  hidden must be 64, layers 1..16. */
+int nd_mpnn_create(int64_t nv, int64_t ne, const int64_t* src, const int64_t* dst, int layers, int hidden,
+                   uint64_t seed, nd_mpnn** out);
+int nd_mpnn_destroy(nd_mpnn* m);
+int nd_mpnn_num_params(const nd_mpnn* m, int64_t* n);
+int nd_mpnn_get_params(const nd_mpnn* m, float* dst, void* stream);
+int nd_mpnn_set_params(nd_mpnn* m, const float* src, void* stream);
+int nd_mpnn_get_grads(const nd_mpnn* m, float* dst, void* stream);
+/* θ = network(P, K) for `batch` instances. */
+int nd_mpnn_forward(nd_mpnn* m, int64_t batch, const float* P, const float* K, float* theta, void* stream);
+/* Mean squared error of the centred prediction against the centred θ*; writes the loss
+ * (device float) and the gradient of every parameter (read by nd_mpnn_get_grads). */
+int nd_mpnn_loss_grad(nd_mpnn* m, int64_t batch, const float* P, const float* K, const float* theta_star,
+                      float* loss, void* stream);
+/* One Adam step on the last gradients (bias-corrected moments). */
+int nd_mpnn_adam(nd_mpnn* m, double lr, double beta1, double beta2, double eps, void* stream);
+int nd_mpnn_reset_optimizer(nd_mpnn* m, void* stream);
 
 #ifdef __cplusplus
 }

@@ -243,6 +243,37 @@ int build_topology(int64_t nv, int64_t ne, const int64_t* src, const int64_t* ds
     return ND_OK;
 }
 
+cudaEvent_t Tracer::event() {
+    if (next == pool.size()) {
+        cudaEvent_t ev = nullptr;
+        if (cudaEventCreate(&ev) != cudaSuccess) return nullptr;
+        pool.push_back(ev);
+    }
+    return pool[next++];
+}
+
+void Tracer::release() {
+    for (cudaEvent_t ev : pool) cudaEventDestroy(ev);
+    pool.clear();
+    marks.clear();
+    next = 0;
+}
+
+// Count one launch of kind `kind` and, with timing on, bracket it with two events on `s`.
+template <typename F>
+static cudaError_t traced(nd_handle* h, int kind, cudaStream_t s, F&& launch) {
+    Tracer& tr = h->tracer;
+    ++tr.launches[kind];
+    if (!tr.timing) return launch();
+    cudaEvent_t start = tr.event(), stop = tr.event();
+    if (!start || !stop) return cudaErrorMemoryAllocation;
+    cudaError_t err = cudaEventRecord(start, s);
+    if (err == cudaSuccess) err = launch();
+    if (err == cudaSuccess) err = cudaEventRecord(stop, s);
+    if (err == cudaSuccess) tr.marks.push_back({kind, start, stop});
+    return err;
+}
+
 }  // namespace nd
 
 using namespace nd;
@@ -309,6 +340,7 @@ int nd_destroy(nd_handle* h) {
     if (prev != h->device) cudaSetDevice(h->device);
     if (h->side) cudaStreamSynchronize(h->side);
     free_topology(&h->topo);
+    h->tracer.release();
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
     if (h->side) cudaStreamDestroy(h->side);
@@ -401,25 +433,62 @@ int nd_rhs(nd_handle* h, int dtype, void* du, int64_t n_du, const void* u, int64
     a.heavy_separate = 0;
     cudaStream_t s = (cudaStream_t)stream;
     const bool edge = el.enabled && h->edge_path;
-    cudaError_t err;
-    if (h->topo.n_heavy > 0 && h->side) {
+    const bool split = h->topo.n_heavy > 0 && h->side;
+    a.heavy_separate = split ? 1 : 0;
+    const int64_t main_rows = (split ? 0 : h->topo.n_heavy) + h->topo.n_windows;
+    cudaError_t err = cudaSuccess;
+    if (split) {
         // Heavy rows run concurrently on the handle's side stream, one per SM, computed
         // from u and p directly (they need nothing from the other kernels); fork / join
         // with events so the call stays ordered on the caller's stream (and capturable).
-        a.heavy_separate = 1;
         RhsArgs hv = a;
         hv.heavy_only = 1;
         if ((err = cudaEventRecord(h->ev_fork, s)) != cudaSuccess ||
             (err = cudaStreamWaitEvent(h->side, h->ev_fork, 0)) != cudaSuccess ||
-            (err = launch_rhs(h->dtype, hv, h->side)) != cudaSuccess ||
-            (err = (edge ? launch_rhs_edge(h->dtype, a, s) : launch_rhs(h->dtype, a, s))) != cudaSuccess ||
-            (err = cudaEventRecord(h->ev_join, h->side)) != cudaSuccess ||
-            (err = cudaStreamWaitEvent(s, h->ev_join, 0)) != cudaSuccess)
+            (err = traced(h, kKernelHeavyRows, h->side, [&] { return launch_rhs(h->dtype, hv, h->side); })) !=
+                cudaSuccess)
             return cuda_fail(err, "nd_rhs kernel launch");
-        return ND_OK;
     }
-    err = edge ? launch_rhs_edge(h->dtype, a, s) : launch_rhs(h->dtype, a, s);
+    if (edge) {
+        if (el.n_chunks > 0)
+            err = traced(h, kKernelEdgePhase, s, [&] { return launch_rhs_edge(h->dtype, a, s, kPhaseEdge); });
+        if (err == cudaSuccess && main_rows > 0)
+            err = traced(h, kKernelRowPhase, s, [&] { return launch_rhs_edge(h->dtype, a, s, kPhaseRow); });
+    } else if (main_rows > 0) {
+        err = traced(h, kKernelFused, s, [&] { return launch_rhs(h->dtype, a, s); });
+    }
+    if (err == cudaSuccess && split) {
+        if ((err = cudaEventRecord(h->ev_join, h->side)) == cudaSuccess) err = cudaStreamWaitEvent(s, h->ev_join, 0);
+    }
     if (err != cudaSuccess) return cuda_fail(err, "nd_rhs kernel launch");
+    return ND_OK;
+}
+
+int nd_set_kernel_timing(nd_handle* h, int on) {
+    clear_error();
+    if (!h) return fail(ND_ERR_ARG, "nd_set_kernel_timing: NULL handle");
+    h->tracer.timing = on != 0;
+    return ND_OK;
+}
+
+int nd_kernel_times(nd_handle* h, int64_t* launches, double* ms, int n) {
+    clear_error();
+    if (!h || n < 0 || (n > 0 && (!launches || !ms))) return fail(ND_ERR_ARG, "nd_kernel_times: bad arguments");
+    double total[kKernelKinds] = {0, 0, 0, 0};
+    for (const Tracer::Mark& m : h->tracer.marks) {
+        float t = 0.f;
+        cudaError_t err = cudaEventSynchronize(m.stop);
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&t, m.start, m.stop);
+        if (err != cudaSuccess) return cuda_fail(err, "nd_kernel_times");
+        total[m.kind] += t;
+    }
+    for (int k = 0; k < n; ++k) {
+        launches[k] = k < kKernelKinds ? h->tracer.launches[k] : 0;
+        ms[k] = k < kKernelKinds ? total[k] : 0.0;
+    }
+    for (int k = 0; k < kKernelKinds; ++k) h->tracer.launches[k] = 0;
+    h->tracer.marks.clear();
+    h->tracer.next = 0;
     return ND_OK;
 }
 

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "nd_gb300.h"
 
@@ -132,8 +133,29 @@ struct RhsArgs {
 
 // Launch the fused RHS for the given element type.
 cudaError_t launch_rhs(int dtype, const RhsArgs& a, cudaStream_t stream);
-// Launch the two-phase (edge-centric) RHS.
-cudaError_t launch_rhs_edge(int dtype, const RhsArgs& a, cudaStream_t stream);
+// Launch the two-phase (edge-centric) RHS: phase E, phase R or both (kPhase* bits).
+enum : int { kPhaseEdge = 1, kPhaseRow = 2, kPhaseBoth = 3 };
+cudaError_t launch_rhs_edge(int dtype, const RhsArgs& a, cudaStream_t stream, int phases = kPhaseBoth);
+
+// Kernel kinds that nd_rhs launches, for launch counting and optional per-kernel timing.
+enum KernelKind : int { kKernelEdgePhase = 0, kKernelRowPhase = 1, kKernelHeavyRows = 2, kKernelFused = 3, kKernelKinds = 4 };
+
+// Launch counter and CUDA-event timer for the kernels of one handle.  Timing is off by
+// default; when on, each launch is bracketed by two events on its stream, and
+// nd_kernel_times sums the bracketed durations.
+struct Tracer {
+    bool timing = false;
+    int64_t launches[kKernelKinds] = {0, 0, 0, 0};
+    struct Mark {
+        int kind;
+        cudaEvent_t start, stop;
+    };
+    std::vector<cudaEvent_t> pool;
+    size_t next = 0;
+    std::vector<Mark> marks;
+    cudaEvent_t event();  // an event from the pool (created on demand), nullptr on failure
+    void release();       // destroy every pooled event
+};
 
 cudaError_t launch_exact_selftest(const double* a, const double* b, double* out, int64_t n, cudaStream_t s);
 cudaError_t launch_scan_selftest(const double* terms, const int64_t* seg, const double* s0, double* out,
@@ -152,4 +174,5 @@ struct nd_handle {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int64_t dim, pdim;
     nd::Topology topo;
+    nd::Tracer tracer;
 };

@@ -204,10 +204,11 @@ __global__ void __launch_bounds__(kBlock, 8) row_phase_kernel(RhsArgs a) {
 }
 
 template <typename T, int VK, int EK>
-cudaError_t launch_typed(const RhsArgs& a, cudaStream_t s) {
-    if (a.n_chunks > 0) edge_phase_kernel<T, VK, EK><<<(unsigned)a.n_chunks, kBlock, 0, s>>>(a);
+cudaError_t launch_typed(const RhsArgs& a, cudaStream_t s, int phases) {
+    if ((phases & kPhaseEdge) && a.n_chunks > 0)
+        edge_phase_kernel<T, VK, EK><<<(unsigned)a.n_chunks, kBlock, 0, s>>>(a);
     const int grid = (a.heavy_separate ? 0 : a.n_heavy) + a.n_windows;
-    if (grid == 0) return cudaGetLastError();
+    if (!(phases & kPhaseRow) || grid == 0) return cudaGetLastError();
     if constexpr (sizeof(T) == 4) {
         row_phase_kernel<T, VK, kModeTree><<<grid, kBlock, 0, s>>>(a);
     } else {
@@ -221,9 +222,9 @@ cudaError_t launch_typed(const RhsArgs& a, cudaStream_t s) {
 }
 
 template <typename T>
-cudaError_t launch_dtype(const RhsArgs& a, cudaStream_t s) {
+cudaError_t launch_dtype(const RhsArgs& a, cudaStream_t s, int phases) {
 #define ND_CASE(VK, EK) \
-    if (a.vertex_kind == VK && a.edge_kind == EK) return launch_typed<T, VK, EK>(a, s);
+    if (a.vertex_kind == VK && a.edge_kind == EK) return launch_typed<T, VK, EK>(a, s, phases);
     ND_CASE(ND_V_DIFFUSION, ND_E_DIFFUSION)
     ND_CASE(ND_V_DIFFUSION, ND_E_DIFFUSION_UNIT)
     ND_CASE(ND_V_DIFFUSION, ND_E_KURAMOTO)
@@ -239,8 +240,8 @@ cudaError_t launch_dtype(const RhsArgs& a, cudaStream_t s) {
 
 }  // namespace
 
-cudaError_t launch_rhs_edge(int dtype, const RhsArgs& a, cudaStream_t s) {
-    return dtype == ND_F64 ? launch_dtype<double>(a, s) : launch_dtype<float>(a, s);
+cudaError_t launch_rhs_edge(int dtype, const RhsArgs& a, cudaStream_t s, int phases) {
+    return dtype == ND_F64 ? launch_dtype<double>(a, s, phases) : launch_dtype<float>(a, s, phases);
 }
 
 }  // namespace nd

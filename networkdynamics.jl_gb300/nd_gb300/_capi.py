@@ -37,6 +37,8 @@ ND_ORDER_SEQUENTIAL = 0
 ND_ORDER_TREE = 1
 ND_ORDER_SEQUENTIAL_HW = 2
 
+KERNEL_KINDS = ("edge_phase", "row_phase", "heavy_rows", "fused")
+
 
 class NDError(RuntimeError):
     """A failing libnd_b200 call; ``code`` is the nd_status value."""
@@ -81,6 +83,8 @@ SIGNATURES = {
     "nd_get_info": (C.c_int, [C.c_void_p, C.POINTER(nd_info)]),
     "nd_set_sum_order": (C.c_int, [C.c_void_p, C.c_int]),
     "nd_set_layout": (C.c_int, [C.c_void_p, C.c_int]),
+    "nd_set_kernel_timing": (C.c_int, [C.c_void_p, C.c_int]),
+    "nd_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.c_int]),
     "nd_rhs": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
                          C.c_void_p, C.c_int64, C.c_double, C.c_void_p]),
     "nd_rhs_static_scratch": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
@@ -180,4 +184,15 @@ SIGNATURES.update({
     "nd_ensemble_autotune": (C.c_int, [_vp, _vp, _vp, _d, _d, _d, _d, C.POINTER(C.c_int), _vp]),
     "nd_ensemble_set_threads": (C.c_int, [_vp, C.c_int]),
     "nd_ensemble_fixpoint": (C.c_int, [_vp, _vp, _vp, _d, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),
+    "nd_mpnn_create": (C.c_int, [_i64, _i64, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_int, C.c_int,
+                                 C.c_uint64, C.POINTER(C.c_void_p)]),
+    "nd_mpnn_destroy": (C.c_int, [_vp]),
+    "nd_mpnn_num_params": (C.c_int, [_vp, C.POINTER(C.c_int64)]),
+    "nd_mpnn_get_params": (C.c_int, [_vp, _vp, _vp]),
+    "nd_mpnn_set_params": (C.c_int, [_vp, _vp, _vp]),
+    "nd_mpnn_get_grads": (C.c_int, [_vp, _vp, _vp]),
+    "nd_mpnn_forward": (C.c_int, [_vp, _i64, _vp, _vp, _vp, _vp]),
+    "nd_mpnn_loss_grad": (C.c_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp]),
+    "nd_mpnn_adam": (C.c_int, [_vp, _d, _d, _d, _d, _vp]),
+    "nd_mpnn_reset_optimizer": (C.c_int, [_vp, _vp]),
 })

@@ -197,6 +197,18 @@ class Network:
         code = {"auto": 0, "fused": 1}[layout]
         capi.check(capi.load().nd_set_layout(self.handle, code))
 
+    def set_kernel_timing(self, on: bool) -> None:
+        """Bracket every kernel that the RHS launches with CUDA events (off by default)."""
+        capi.check(capi.load().nd_set_kernel_timing(self.handle, int(bool(on))))
+
+    def kernel_times(self) -> dict:
+        """{kind: (launches, total ms)} since the last read (waits for recorded events)."""
+        n = len(capi.KERNEL_KINDS)
+        launches = (C.c_int64 * n)()
+        ms = (C.c_double * n)()
+        capi.check(capi.load().nd_kernel_times(self.handle, launches, ms, n))
+        return {k: (int(launches[i]), float(ms[i])) for i, k in enumerate(capi.KERNEL_KINDS)}
+
     def __del__(self):
         h = getattr(self, "_handle", None)
         if h is not None and getattr(self, "_lib", None) is not None:

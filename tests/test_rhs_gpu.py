@@ -230,6 +230,33 @@ def test_two_phase_equals_fused_layout(cuda, vk, ek):
     check_f64(gpu_rhs(nw, u, p, cuda, np.float64), on.rhs(u, p), on.abs_terms(u, p), exact=ek != O.E_KURAMOTO)
 
 
+def test_kernel_counts_and_timing(cuda):
+    """Each RHS launches edge phase + row phase (+ heavy rows on the side stream); the
+    timer brackets each of them and leaves the results unchanged."""
+    g = nd.barabasi_albert(200_000, 4, seed=31)
+    assert g.degree().max() > 512
+    nw = make(g, O.V_DIFFUSION, O.E_DIFFUSION, np.float64)
+    on = O.OracleNetwork.from_graph(g, O.V_DIFFUSION, O.E_DIFFUSION)
+    u, p = random_inputs(on, O.V_DIFFUSION, np.random.default_rng(2))
+    nw.kernel_times()
+    ref = gpu_rhs(nw, u, p, cuda, np.float64)
+    counts = nw.kernel_times()
+    assert counts["edge_phase"][0] == 1 and counts["row_phase"][0] == 1 and counts["heavy_rows"][0] == 1
+    assert counts["fused"][0] == 0 and all(ms == 0.0 for _, ms in counts.values())
+    nw.set_kernel_timing(True)
+    for _ in range(3):
+        out = gpu_rhs(nw, u, p, cuda, np.float64)
+        np.testing.assert_array_equal(out, ref)
+    times = nw.kernel_times()
+    for k in ("edge_phase", "row_phase", "heavy_rows"):
+        assert times[k][0] == 3 and times[k][1] > 0.0
+    nw.set_layout("fused")
+    gpu_rhs(nw, u, p, cuda, np.float64)
+    times = nw.kernel_times()
+    assert times["fused"][0] == 1 and times["edge_phase"][0] == 0 and times["heavy_rows"][0] == 1
+    nw.set_kernel_timing(False)
+
+
 def test_non_canonical_edge_list_uses_fused_path(cuda):
     """Edges in arbitrary order and orientation (a directed edge list) are summed in the
     order the reference's output buffer has for them."""
