@@ -294,6 +294,9 @@ int nd_mpnn_loss_grad(nd_mpnn* m, int64_t batch, const float* P, const float* K,
 /* One Adam step on the last gradients (bias-corrected moments). */
 int nd_mpnn_adam(nd_mpnn* m, double lr, double beta1, double beta2, double eps, void* stream);
 int nd_mpnn_reset_optimizer(nd_mpnn* m, void* stream);
+/* Weighted-mean steps per message (default 1): each layer's message is M^hops h, so the
+ * receptive field is layers x hops vertices deep. */
+int nd_mpnn_set_hops(nd_mpnn* m, int hops);
 
 #ifdef __cplusplus
 }

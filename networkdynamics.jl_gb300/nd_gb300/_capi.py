@@ -195,4 +195,5 @@ SIGNATURES.update({
     "nd_mpnn_loss_grad": (C.c_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp]),
     "nd_mpnn_adam": (C.c_int, [_vp, _d, _d, _d, _d, _vp]),
     "nd_mpnn_reset_optimizer": (C.c_int, [_vp, _vp]),
+    "nd_mpnn_set_hops": (C.c_int, [_vp, C.c_int]),
 })

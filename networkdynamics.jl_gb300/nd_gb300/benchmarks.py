@@ -1,0 +1,245 @@
+"""Secondary GPU benchmarks of the package (the headline RHS benchmark is bench.py).
+
+    python -m nd_gb300.benchmarks warmstart [--train 20000 --test 2000 --nv 2000]
+    python -m nd_gb300.benchmarks ensemble  [--instances 4096]
+    python -m nd_gb300.benchmarks swing     [--nv 100000]
+
+Each prints one JSON object.  All inputs are seeded synthetic instances of the stated
+shapes; no dataset is read.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import sys
+import time
+
+import numpy as np
+
+
+def _sync():
+    import torch
+    torch.cuda.synchronize()
+
+
+_T0 = time.perf_counter()
+
+
+def _log(msg):
+    print(f"[{time.perf_counter() - _T0:8.1f} s] {msg}", file=sys.stderr, flush=True)
+
+
+def warmstart(n_train=20000, n_test=2000, nv=2000, m=2, layers=4, epochs=30, batch=64, lr=2e-3, lr_final=5e-5,
+              seed=0, tol=1e-10):
+    """Swing steady states on BA(nv, m): solve n_train + n_test instances from the cold
+    start, train the MPNN on the first n_train, compare cold and warm starts on the rest."""
+    import nd_gb300 as nd
+    from nd_gb300 import warmstart as W
+    g = nd.barabasi_albert(nv, m, seed=seed + 1)
+    P, K = W.swing_instances(g, n_train + n_test, seed + 2)
+    t0 = time.perf_counter()
+    train = W.fixpoints(g, P[:n_train], K[:n_train], tol=tol)
+    t_gen = time.perf_counter() - t0
+    _log(f"training data: {n_train} steady states in {t_gen:.1f} s")
+    ok = train.status == 0
+    model = nd.MPNN(g, layers=layers, seed=seed + 3)
+    _sync()
+    t0 = time.perf_counter()
+    hist = model.fit(P[:n_train][ok], K[:n_train][ok], train.theta[ok], epochs=epochs, batch=batch, lr=lr,
+                     lr_final=lr_final, seed=seed + 4)
+    _sync()
+    t_train = time.perf_counter() - t0
+    _log(f"trained {epochs} epochs in {t_train:.1f} s, loss {hist[0]:.3e} -> {hist[-1]:.3e}")
+    res = W.warm_vs_cold(model, g, P[n_train:], K[n_train:], tol=tol)
+    res.update({
+        "workload": f"swing steady states on Barabasi-Albert N={nv}, m={m}; P, K resampled per instance",
+        "train_instances": int(ok.sum()), "data_generation_seconds": t_gen,
+        "data_generation_newton_iters_mean": float(train.iters.mean()),
+        "train_seconds": t_train, "epochs": epochs, "batch": batch, "loss_first_epoch": hist[0],
+        "loss_last_epoch": hist[-1], "model": f"MPNN {layers} layers x 64 hidden, FP32",
+        "tolerance": tol,
+    })
+    return res
+
+
+def ensemble(n=4096, nv_lo=50, nv_hi=5000, t_end=50.0, reltol=1e-6, abstol=1e-6, seed=0, baseline_sample=16):
+    """Basin-stability ensemble: n swing instances on random geometric graphs (mean degree
+    ~6), each from its steady state plus one perturbed vertex, integrated to t_end by the
+    batched Tsit5 with an FP64 and an FP32 RHS; the per-instance FP64 GPU solve of
+    solve_tsit5 is timed on a sample of the instances as the plain baseline.
+
+    Sparse geometric graphs have bottleneck lines that often cannot carry the drawn
+    injections, and such an instance has no steady state.  Its parameters are drawn again
+    (twice), then its injections are halved until the Newton solve converges; the counts
+    are reported."""
+    import torch
+
+    import nd_gb300 as nd
+    from nd_gb300 import warmstart as W
+    from nd_gb300.ensemble import Ensemble
+    from nd_gb300.solve import solve_tsit5
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(nv_lo, nv_hi + 1, n)
+    graphs = [nd.random_geometric(int(k), float(np.sqrt(6.0 / (np.pi * k))), seed=seed + 10 + i)
+              for i, k in enumerate(sizes)]
+    _log(f"{n} graphs, {int(sizes.sum())} vertices")
+    draw = np.zeros(n, dtype=np.int64)   # parameter draw of each instance
+    scale = np.ones(n)                    # factor on its injections
+
+    def params(i):
+        P, K = W.swing_instances(graphs[i], 1, seed + 100000 + 7919 * int(draw[i]) + i)
+        return W.swing_flat_params(graphs[i], scale[i] * P, K)
+
+    ps = [params(i) for i in range(n)]
+    e64 = Ensemble(graphs, nd.kuramoto_second(), nd.static_line(), torch.float64)
+    _log("ensemble built")
+    for attempt in range(12):
+        p64 = torch.from_numpy(np.concatenate(ps)).cuda()
+        fx = e64.fixpoint(torch.zeros(e64.dim, dtype=torch.float64, device="cuda"), p64, tol=1e-10,
+                          max_newton=12, max_cg=4000)
+        status_fx = fx.status.cpu().numpy()
+        bad = np.nonzero(status_fx != 0)[0]
+        _log(f"fixpoints: {n - bad.size} of {n} converged (round {attempt})")
+        if bad.size == 0:
+            break
+        for i in bad:
+            if draw[i] < 2:
+                draw[i] += 1
+            else:
+                scale[i] *= 0.5
+            ps[i] = params(i)
+    u0 = fx.u.clone()
+    # one perturbed vertex per instance: Δθ ~ U(-π, π), Δω ~ U(-10, 10)
+    uh = u0.cpu().numpy()
+    for i, g in enumerate(graphs):
+        v = int(rng.integers(0, g.nv))
+        s = int(e64.u_offset[i]) + 2 * v
+        uh[s] += rng.uniform(-np.pi, np.pi)
+        uh[s + 1] += rng.uniform(-10.0, 10.0)
+    u0 = torch.from_numpy(uh).cuda()
+    out = {"workload": f"{n} swing instances on random geometric graphs, N ~ U[{nv_lo}, {nv_hi}], mean degree ~6; "
+                       f"steady state + one perturbed vertex; Tsit5 to T={t_end}, reltol {reltol}, abstol {abstol}",
+           "vertices": int(sizes.sum()), "edges": int(sum(g.ne for g in graphs)),
+           "fixpoints_converged": int((status_fx == 0).sum()),
+           "instances_redrawn": int((draw > 0).sum()), "instances_with_scaled_injections": int((scale < 1).sum()),
+           "injection_scale_min": float(scale.min())}
+    finals = {}
+    for name, dt in (("f64", torch.float64), ("f32", torch.float32)):
+        ens = e64 if dt == torch.float64 else Ensemble(graphs, nd.kuramoto_second(), nd.static_line(), dt)
+        p = p64 if dt == torch.float64 else p64.float()
+        threads = ens.autotune(u0, p, 0.0, 0.5, reltol, abstol)
+        _log(f"{name}: autotuned {threads} threads per instance")
+        ens.solve_tsit5(u0, p, (0.0, 0.5), reltol, abstol)  # warm-up (graph capture)
+        _sync()
+        t0 = time.perf_counter()
+        r = ens.solve_tsit5(u0, p, (0.0, t_end), reltol, abstol)
+        _sync()
+        el = time.perf_counter() - t0
+        _log(f"{name}: solved in {el:.2f} s")
+        finals[name] = r.u.cpu().numpy()
+        st = r.status.cpu().numpy()
+        out[name] = {"seconds": el, "solves_per_s": n / el, "threads_per_instance": threads,
+                     "steps_mean": float(r.nsteps.double().mean().item()), "ok": int((st == 0).sum())}
+    err = np.abs(finals["f32"] - finals["f64"])
+    per_inst = np.maximum.reduceat(err, e64.u_offset[:-1].astype(np.int64))
+    out["f32_final_state_err_vs_f64"] = {"max": float(err.max()), "median_instance": float(np.median(per_inst)),
+                                         "instances_within_1e-6": int((per_inst <= 1e-6).sum())}
+    # synchronised / desynchronised verdict per instance: max |ω| at T below 0.1
+    verdict = {}
+    for name in ("f64", "f32"):
+        w = np.abs(finals[name][1::2])
+        per = np.maximum.reduceat(w, (e64.u_offset[:-1] // 2).astype(np.int64))
+        verdict[name] = per < 0.1
+    out["sync_fraction_f64"] = float(verdict["f64"].mean())
+    out["sync_verdict_agreement_f32_vs_f64"] = float((verdict["f64"] == verdict["f32"]).mean())
+    # the plain per-instance FP64 GPU solve on a sample of the instances
+    idx = rng.choice(n, size=min(baseline_sample, n), replace=False)
+    t_plain = 0.0
+    for i in idx:
+        g = graphs[i]
+        net = nd.adapt(nd.Network(g, nd.kuramoto_second(), nd.static_line()), torch.float64)
+        ui = u0[e64.u_slice(i)].clone()
+        pi = p64[e64.p_slice(i)].clone()
+        solve_tsit5(net, ui, pi, (0.0, 0.5), reltol, abstol)  # warm-up
+        _sync()
+        t0 = time.perf_counter()
+        solve_tsit5(net, ui, pi, (0.0, t_end), reltol, abstol)
+        _sync()
+        t_plain += time.perf_counter() - t0
+    plain = len(idx) / t_plain
+    _log(f"plain per-instance FP64: {len(idx)} solves in {t_plain:.2f} s")
+    out["plain_f64_per_instance"] = {"solves_per_s": plain, "sample": int(len(idx)),
+                                     "note": "solve_tsit5 of one Network at a time, sampled instances"}
+    out["f32_batched_vs_plain_f64"] = out["f32"]["solves_per_s"] / plain
+    out["f64_batched_vs_plain_f64"] = out["f64"]["solves_per_s"] / plain
+    return out
+
+
+def swing(nv=100000, m=2, t_end=20.0, steps=200, seed=0):
+    """Swing network on BA(nv, m): FP64 / FP32 RHS evaluations per second and a Tsit5 solve
+    to t_end (reltol 1e-6) from a random state."""
+    import torch
+
+    import nd_gb300 as nd
+    from nd_gb300 import warmstart as W
+    from nd_gb300.solve import solve_tsit5
+    g = nd.barabasi_albert(nv, m, seed=seed + 1)
+    P, K = W.swing_instances(g, 1, seed + 2)
+    p = W.swing_flat_params(g, P, K)
+    rng = np.random.default_rng(seed + 3)
+    u = np.empty(2 * nv)
+    u[0::2] = rng.uniform(-np.pi, np.pi, nv)
+    u[1::2] = rng.normal(size=nv)
+    net = nd.Network(g, nd.kuramoto_second(), nd.static_line())
+    out = {"workload": f"swing on Barabasi-Albert N={nv}, m={m}; K ~ U(5,10), P = ±U(0.5,1.5) zero-sum, M=1, D=0.1"}
+    for name, dt in (("f64", torch.float64), ("f32", torch.float32)):
+        nw = nd.adapt(net, dt)
+        ut = torch.from_numpy(u).to("cuda", dt)
+        pt = torch.from_numpy(p).to("cuda", dt)
+        du = torch.empty_like(ut)
+        for _ in range(3):
+            nw(du, ut, pt)
+        _sync()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(steps):
+            nw(du, ut, pt)
+        b.record()
+        b.synchronize()
+        ms = a.elapsed_time(b) / steps
+        out[name] = {"rhs_ms": ms, "rhs_per_s": 1e3 / ms, "edges_per_s": g.ne * 1e3 / ms}
+    nw = nd.adapt(net, torch.float64)
+    ut = torch.from_numpy(u).cuda()
+    pt = torch.from_numpy(p).cuda()
+    _sync()
+    t0 = time.perf_counter()
+    uT, st = solve_tsit5(nw, ut, pt, (0.0, t_end), 1e-6, 1e-8)
+    _sync()
+    out["tsit5_f64"] = {"seconds": time.perf_counter() - t0, "naccept": st.naccept, "nreject": st.nreject,
+                        "t_end": t_end}
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("which", choices=["warmstart", "ensemble", "swing"])
+    ap.add_argument("--train", type=int, default=20000)
+    ap.add_argument("--test", type=int, default=2000)
+    ap.add_argument("--nv", type=int, default=None)
+    ap.add_argument("--epochs", type=int, default=30)
+    ap.add_argument("--instances", type=int, default=4096)
+    ap.add_argument("--sample", type=int, default=16)
+    ap.add_argument("--t-end", type=float, default=50.0)
+    a = ap.parse_args()
+    if a.which == "warmstart":
+        r = warmstart(a.train, a.test, a.nv or 2000, epochs=a.epochs)
+    elif a.which == "ensemble":
+        r = ensemble(a.instances, baseline_sample=a.sample, t_end=a.t_end)
+    else:
+        r = swing(a.nv or 100000)
+    print(json.dumps(r), flush=True)
+
+
+if __name__ == "__main__":
+    main()
