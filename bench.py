@@ -309,10 +309,15 @@ def run_gb300(args, rank, world, local):
         kbytes, kops = kb[kind]
         kernels[kind] = {"launches": n, "avg_ms": 1e3 * avg, "share": None, "bytes_per_launch": kbytes,
                          "achieved_gbs": kbytes / avg / 1e9, "fp64_lane_ops_per_launch": kops}
-    total_ms = sum(k["avg_ms"] * k["launches"] for k in kernels.values())
-    for k in kernels.values():
-        k["share"] = k["avg_ms"] * k["launches"] / total_ms if total_ms else None
-    dom = max(kernels, key=lambda k: kernels[k]["avg_ms"] * kernels[k]["launches"])
+    # heavy rows run on the handle's side stream, overlapped with the other kernels: the
+    # dominant kernel is the longest one on the caller's stream (the critical path), and
+    # shares are over those kernels (the ncu launch list serialises every launch)
+    main = [k for k in kernels if k != "heavy_rows"]
+    total_ms = sum(kernels[k]["avg_ms"] * kernels[k]["launches"] for k in main)
+    for kind, k in kernels.items():
+        k["stream"] = "side (overlapped)" if kind == "heavy_rows" else "caller"
+        k["share"] = k["avg_ms"] * k["launches"] / total_ms if (total_ms and kind in main) else None
+    dom = max(main, key=lambda k: kernels[k]["avg_ms"] * kernels[k]["launches"])
     achieved = kernels[dom]["achieved_gbs"]
     traffic = profiled_traffic("f64", nv, dom)
     line = {
@@ -364,34 +369,60 @@ def run_gb300(args, rank, world, local):
                        "achieved_gbs": B32 / (t32 / args.steps) / 1e9,
                        "frac": B32 / (t32 / args.steps) / 1e9 / hbm, "max_abs_err_vs_f64": err}
         del nw32, u32, p32, du32
-    # end to end through the public API with pinned host buffers
+    # end to end through the public API with pinned host buffers: every step copies its
+    # inputs (u, p) host->device and its result du device->host.  Two buffer sets and
+    # three streams pipeline step k's RHS with step k+1's upload and step k-1's download.
     if not args.no_e2e:
         ke = min(args.steps, 200)
         uh = torch.from_numpy(u_h).pin_memory()
         ph = torch.from_numpy(w_h).pin_memory()
-        duh = torch.empty(nv, dtype=torch.float64).pin_memory()
-        for _ in range(2):
-            u.copy_(uh, non_blocking=True)
-            p.copy_(ph, non_blocking=True)
-            nw(du, u, p, 0.0)
-            duh.copy_(du, non_blocking=True)
+        duh = [torch.empty(nv, dtype=torch.float64).pin_memory() for _ in range(2)]
+        ub = [u, torch.empty_like(u)]
+        pb = [p, torch.empty_like(p)]
+        dub = [du, torch.empty_like(du)]
+        s_up = torch.cuda.Stream(dev)
+        s_down = torch.cuda.Stream(dev)
+        ev = lambda: torch.cuda.Event()  # noqa: E731
+        uploaded = [ev(), ev()]
+        computed = [ev(), ev()]
+        downloaded = [ev(), ev()]
+
+        def e2e_steps(k):
+            for i in range(k):
+                b = i & 1
+                with torch.cuda.stream(s_up):
+                    if i >= 2:
+                        s_up.wait_event(computed[b])  # buffers b are free once step i-2's RHS ran
+                    ub[b].copy_(uh, non_blocking=True)
+                    pb[b].copy_(ph, non_blocking=True)
+                    uploaded[b].record(s_up)
+                stream.wait_event(uploaded[b])
+                if i >= 2:
+                    stream.wait_event(downloaded[b])  # du buffer b was read back
+                nw(dub[b], ub[b], pb[b], 0.0, stream=stream)
+                computed[b].record(stream)
+                with torch.cuda.stream(s_down):
+                    s_down.wait_event(computed[b])
+                    duh[b].copy_(dub[b], non_blocking=True)
+                    downloaded[b].record(s_down)
+            stream.wait_stream(s_down)
+
+        e2e_steps(4)
         torch.cuda.synchronize()
         barrier(world)
         start = torch.cuda.Event(enable_timing=True)
         stop = torch.cuda.Event(enable_timing=True)
         start.record(stream)
-        for _ in range(ke):
-            u.copy_(uh, non_blocking=True)
-            p.copy_(ph, non_blocking=True)
-            nw(du, u, p, 0.0)
-            duh.copy_(du, non_blocking=True)
+        e2e_steps(ke)
         stop.record(stream)
         stop.synchronize()
         te = max_over_ranks(start.elapsed_time(stop) / 1e3, world, dev)
         line["e2e"] = {"value": world * ne * ke / te, "unit": "edges/s", "steps": ke,
                        "h2d_bytes_per_step": int(uh.numel() * 8 + ph.numel() * 8),
-                       "d2h_bytes_per_step": int(duh.numel() * 8)}
-        ok = np.array_equal(duh.numpy(), du.cpu().numpy())
+                       "d2h_bytes_per_step": int(duh[0].numel() * 8),
+                       "pipeline": "2 buffer sets; upload, RHS and download on 3 streams"}
+        torch.cuda.synchronize()
+        ok = np.array_equal(duh[(ke - 1) & 1].numpy(), dub[(ke - 1) & 1].cpu().numpy())
         line["e2e"]["result_matches_device"] = bool(ok)
     line["clocks"] = clk.summary()
     if rank == 0 and world == 1 and not args.no_cpu:

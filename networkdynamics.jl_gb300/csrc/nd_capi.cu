@@ -146,9 +146,9 @@ int build_topology(int64_t nv, int64_t ne, const int64_t* src, const int64_t* ds
         incid[fill[d]++] = Incidence{s, (int32_t)e};                // d receives y_dst
     }
     // Degree buckets (see nd_internal.h).  The windowed rows, medium rows by degree then
-    // light rows in ascending vertex order, are cut into windows of at most kWindow rows
-    // and kWindowIncidences incidences and sorted by degree (descending, stable) inside
-    // each window.
+    // light rows in runs of consecutive vertices, are cut into windows of at most kWindow
+    // rows and kWindowIncidences incidences and sorted by degree (descending, stable)
+    // inside each window.
     std::vector<int32_t> light, medium, heavy;
     light.reserve(nv);
     for (int64_t v = 0; v < nv; ++v) {
@@ -159,6 +159,11 @@ int build_topology(int64_t nv, int64_t ne, const int64_t* src, const int64_t* ds
     auto by_degree = [&](int32_t a, int32_t b) { return deg[a] > deg[b]; };
     std::stable_sort(medium.begin(), medium.end(), by_degree);
     std::stable_sort(heavy.begin(), heavy.end(), by_degree);
+    // Light rows by degree inside runs of kLightRun consecutive vertices: the rows of a warp
+    // then have (nearly) equal length, so their per-thread sums keep all lanes busy, while
+    // du and u accesses stay within the run.
+    for (size_t r0 = 0; r0 < light.size(); r0 += (size_t)kLightRun)
+        std::stable_sort(light.begin() + r0, light.begin() + std::min(light.size(), r0 + (size_t)kLightRun), by_degree);
     std::vector<int32_t> windowed;
     windowed.reserve(medium.size() + light.size());
     windowed.insert(windowed.end(), medium.begin(), medium.end());
@@ -170,7 +175,8 @@ int build_topology(int64_t nv, int64_t ne, const int64_t* src, const int64_t* ds
         uint32_t inc = 0;
         for (size_t i = 0; i < windowed.size(); ++i) {
             const uint32_t d = deg[windowed[i]];
-            if (i - w0 == (size_t)kWindow || inc + d > (uint32_t)kWindowIncidences) {
+            // windows never mix medium and light rows
+            if (i - w0 == (size_t)kWindow || inc + d > (uint32_t)kWindowIncidences || (i == medium.size() && i > w0)) {
                 std::stable_sort(windowed.begin() + w0, windowed.begin() + i, by_degree);
                 win_ptr.push_back((int32_t)i);
                 w0 = i;
@@ -206,6 +212,9 @@ int build_topology(int64_t nv, int64_t ne, const int64_t* src, const int64_t* ds
     t.n_medium = (int32_t)medium.size();
     t.n_heavy = (int32_t)heavy.size();
     t.n_windows = (int32_t)win_ptr.size() - 1;
+    t.n_medium_windows = 0;
+    while (t.n_medium_windows < t.n_windows && win_ptr[(size_t)t.n_medium_windows] < (int32_t)medium.size())
+        ++t.n_medium_windows;
     auto upload = [&](void** dptr, const void* hptr, size_t bytes) -> cudaError_t {
         cudaError_t err = cudaMalloc(dptr, std::max<size_t>(bytes, 16));
         if (err != cudaSuccess) return err;
@@ -415,6 +424,7 @@ int nd_rhs(nd_handle* h, int dtype, void* du, int64_t n_du, const void* u, int64
     a.n_medium = h->topo.n_medium;
     a.n_heavy = h->topo.n_heavy;
     a.n_windows = h->topo.n_windows;
+    a.n_medium_windows = h->topo.n_medium_windows;
     a.vertex_kind = h->vertex_kind;
     a.edge_kind = h->edge_kind;
     a.mode = h->rhs_mode;
@@ -433,7 +443,7 @@ int nd_rhs(nd_handle* h, int dtype, void* du, int64_t n_du, const void* u, int64
     a.heavy_separate = 0;
     cudaStream_t s = (cudaStream_t)stream;
     const bool edge = el.enabled && h->edge_path;
-    const bool split = h->topo.n_heavy > 0 && h->side;
+    const bool split = h->topo.n_heavy > 0;  // heavy rows: their own kernel, on the side stream
     a.heavy_separate = split ? 1 : 0;
     const int64_t main_rows = (split ? 0 : h->topo.n_heavy) + h->topo.n_windows;
     cudaError_t err = cudaSuccess;

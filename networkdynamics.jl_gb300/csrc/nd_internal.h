@@ -40,12 +40,14 @@ inline int edge_pdim(int ek) { return ek == ND_E_DIFFUSION_UNIT ? 0 : 1; }
 // evaluates all edge terms of up to kWindow rows / kWindowIncidences incidences in
 // parallel, then sums one row per thread; rows are sorted by degree inside a window so
 // the lanes of a warp walk rows of nearly equal length.  Medium rows (degree above
-// kLightMaxDeg) come first, globally sorted by degree; light rows follow in vertex order.
+// kLightMaxDeg) come first, globally sorted by degree; light rows follow in runs of
+// kLightRun consecutive vertices, sorted by degree inside each run.
 // Longer rows (power-law hubs) get a block each and are summed by an exact parallel scan:
 // a per-thread chain that long would wait on the shared FP64 pipe at every step.
 constexpr int kLightMaxDeg = 32;
 constexpr int kMediumMaxDeg = 512;
 constexpr int kWindow = 256;
+constexpr int kLightRun = 8192;
 
 // Device-resident topology of one network.
 // Rows are stored in processing order ("slots"): heavy rows (by degree, descending), then
@@ -88,6 +90,7 @@ struct Topology {
     Incidence* incid = nullptr;      // [2ne] incidences in slot order, each row by edge id (fused path)
     int32_t* win_ptr = nullptr;      // [n_windows+1] first slot of each light window
     int32_t n_light = 0, n_medium = 0, n_heavy = 0, n_windows = 0;
+    int32_t n_medium_windows = 0;    // the first windows, which hold exactly the medium rows
     EdgeLayout edge;
 };
 
@@ -114,7 +117,7 @@ struct RhsArgs {
     const int32_t* slot_vertex;
     const Incidence* incid;
     const int32_t* win_ptr;
-    int32_t n_light, n_medium, n_heavy, n_windows;
+    int32_t n_light, n_medium, n_heavy, n_windows, n_medium_windows;
     int32_t vertex_kind, edge_kind;
     int32_t mode;
     int32_t heavy_only;      // launch_rhs: only the heavy rows, one per SM

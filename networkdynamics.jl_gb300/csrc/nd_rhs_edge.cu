@@ -28,9 +28,7 @@ using namespace dev;
 
 template <typename T>
 struct SmemR {
-    static constexpr int kWin = kWindowIncidences * (int)sizeof(T) + 4 * kWindow * 4 + kWindowIncidences;
-    static constexpr int kHeavy = kTile * (int)sizeof(double);
-    static constexpr int kBytes = kWin > kHeavy ? kWin : kHeavy;
+    static constexpr int kBytes = kWindowIncidences * (int)sizeof(T) + 4 * kWindow * 4 + kWindowIncidences;
 };
 
 template <typename T>
@@ -40,98 +38,85 @@ __device__ __forceinline__ T negate(T x) {
 }
 
 // ---- phase E -------------------------------------------------------------------------------
+template <typename T>
+struct Pair;
+template <>
+struct Pair<double> {
+    using type = double2;
+};
+template <>
+struct Pair<float> {
+    using type = float2;
+};
+
+// A thread evaluates two consecutive edges per step, so the in-order streams (src, dst,
+// bucket slot, parameter, y) move as 8- or 16-byte vectors.
 template <typename T, int VK, int EK>
 __global__ void __launch_bounds__(kBlock) edge_phase_kernel(RhsArgs a) {
+    using P2 = typename Pair<T>::type;
     constexpr int DV = VertexDims<VK>::dim;
     const T* __restrict__ u = static_cast<const T*>(a.u);
     const T* __restrict__ pe = static_cast<const T*>(a.p) + a.nv * VertexDims<VK>::pdim;
     T* __restrict__ y = static_cast<T*>(a.y);
     T* __restrict__ ybkt = static_cast<T*>(a.ybkt);
     const uint64_t keep = policy_evict_last(), stream = policy_evict_first();
-    const int64_t e0 = (int64_t)blockIdx.x * kEdgeChunk;
+    const int64_t e0 = (int64_t)blockIdx.x * kEdgeChunk;  // even: kEdgeChunk is
     const int64_t e1 = min(e0 + (int64_t)kEdgeChunk, a.ne);
-#pragma unroll 4
-    for (int64_t e = e0 + threadIdx.x; e < e1; e += kBlock) {
+    // the parameter block starts after nv * pdim vertex parameters: pairs of it are
+    // vector-aligned only when that offset is even
+    const bool wvec = EK == ND_E_DIFFUSION_UNIT || (reinterpret_cast<uintptr_t>(pe) % sizeof(P2)) == 0;
+    const int64_t npair = (e1 - e0) >> 1;
+#pragma unroll 2
+    for (int64_t k = threadIdx.x; k < npair; k += kBlock) {
+        const int64_t e = e0 + 2 * k;
+        const int2 s = ld_hint(reinterpret_cast<const int2*>(a.esrc + e), stream);
+        const int2 d = ld_hint(reinterpret_cast<const int2*>(a.edst + e), stream);
+        const int2 q = ld_hint(reinterpret_cast<const int2*>(a.q + e), stream);
+        T w0, w1;
+        if constexpr (EK == ND_E_DIFFUSION_UNIT) {
+            w0 = w1 = T(0);
+        } else if (wvec) {
+            const P2 w = ld_hint(reinterpret_cast<const P2*>(pe + e), stream);
+            w0 = w.x;
+            w1 = w.y;
+        } else {
+            w0 = ld_hint(pe + e, stream);
+            w1 = ld_hint(pe + e + 1, stream);
+        }
+        const T us0 = ld_hint(u + (int64_t)s.x * DV, keep);
+        const T us1 = ld_hint(u + (int64_t)s.y * DV, keep);
+        const T ud0 = ld_hint(u + (int64_t)d.x * DV, keep);
+        const T ud1 = ld_hint(u + (int64_t)d.y * DV, keep);
+        P2 yv;
+        yv.x = edge_g_w<T, EK>(us0, ud0, w0);
+        yv.y = edge_g_w<T, EK>(us1, ud1, w1);
+        *reinterpret_cast<P2*>(y + e) = yv;
+        ybkt[q.x] = yv.x;
+        ybkt[q.y] = yv.y;
+    }
+    if (((e1 - e0) & 1) && threadIdx.x == 0) {  // odd tail of the last chunk
+        const int64_t e = e1 - 1;
         const int32_t s = ld_hint(a.esrc + e, stream);
         const int32_t d = ld_hint(a.edst + e, stream);
-        const int32_t q = ld_hint(a.q + e, stream);
-        const T us = ld_hint(u + (int64_t)s * DV, keep);
-        const T ud = ld_hint(u + (int64_t)d * DV, keep);
         const T w = edge_param<T, EK>(pe, (int32_t)e, stream);
-        const T yv = edge_g_w<T, EK>(us, ud, w);
+        const T yv = edge_g_w<T, EK>(ld_hint(u + (int64_t)s * DV, keep), ld_hint(u + (int64_t)d * DV, keep), w);
         y[e] = yv;
-        ybkt[q] = yv;
+        ybkt[ld_hint(a.q + e, stream)] = yv;
     }
 }
 
 // Term j (0-based, in row order) of a row whose destination-side entries start at dp
-// (nd of them) and whose source block starts at sp.
-template <typename T>
+// (nd of them) and whose source block starts at sp.  kNeg: the source-side terms come
+// negated (their value in the reference's output buffer); without it they come as stored
+// and the caller subtracts them.
+template <typename T, bool kNeg = true>
 __device__ __forceinline__ T row_term(const RhsArgs& a, uint32_t dp, int nd, uint32_t sp, int j, uint64_t pol) {
     const T* __restrict__ y = static_cast<const T*>(a.y);
     const T* __restrict__ ybkt = static_cast<const T*>(a.ybkt);
     if (j < nd) return ld_hint(ybkt + ld_hint(a.loc + dp + j, pol), pol);
-    return negate(ld_hint(y + sp + (j - nd), pol));
-}
-
-// ---- phase R: heavy rows, a block per row ---------------------------------------------------
-template <typename T, int VK, int MODE>
-__device__ __forceinline__ void heavy_row_r(const RhsArgs& a, int slot, unsigned char* smem) {
-    using A = Arith<T>;
-    const T* __restrict__ u = static_cast<const T*>(a.u);
-    const T* __restrict__ p = static_cast<const T*>(a.p);
-    const uint64_t stream = policy_evict_first();
-    const int64_t v = __ldg(a.slot_vertex + slot);
-    const uint32_t dp = __ldg(a.dptr + v), sp = __ldg(a.sptr + v);
-    const int nd = (int)(__ldg(a.dptr + v + 1) - dp);
-    const int deg = nd + (int)(__ldg(a.sptr + v + 1) - sp);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if constexpr (sizeof(T) == 8 && MODE != kModeTree) {
-        double* tile = reinterpret_cast<double*>(smem);
-        double S = 0.0;
-        for (int base = 0; base < deg; base += kTile) {
-            const int n = min(kTile, deg - base);
-#pragma unroll 4
-            for (int i = tid; i < n; i += kBlock) tile[i] = row_term<T>(a, dp, nd, sp, base + i, stream);
-            __syncthreads();
-            if (warp == 0) {
-                if constexpr (MODE == kModeNative) {
-                    if (lane == 0)
-                        for (int i = 0; i < n; ++i) S = __dadd_rn(S, tile[i]);
-                } else {
-                    S = exact_scan_wide(S, tile, n, lane);
-                }
-            }
-            __syncthreads();
-        }
-        if (tid == 0) vertex_f<T, VK>(static_cast<T*>(a.du), u, p, v, (T)S);
-    } else {
-        T* red = reinterpret_cast<T*>(smem);
-        T acc = T(0), comp = T(0);
-#pragma unroll 4
-        for (int j = tid; j < deg; j += kBlock) {
-            const T term = row_term<T>(a, dp, nd, sp, j, stream);
-            if constexpr (sizeof(T) == 4) {
-                const T yk = A::sub(term, comp);
-                const T s = A::add(acc, yk);
-                comp = A::sub(A::sub(s, acc), yk);
-                acc = s;
-            } else {
-                acc = A::add(acc, term);
-            }
-        }
-        if constexpr (sizeof(T) == 4) acc = A::sub(acc, comp);
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) acc = A::add(acc, __shfl_xor_sync(kFull, acc, off));
-        if (lane == 0) red[warp] = acc;
-        __syncthreads();
-        if (tid == 0) {
-            T s = red[0];
-#pragma unroll
-            for (int w = 1; w < kWarpsPerBlock; ++w) s = A::add(s, red[w]);
-            vertex_f<T, VK>(static_cast<T*>(a.du), u, p, v, s);
-        }
-    }
+    const T v = ld_hint(y + sp + (j - nd), pol);
+    if constexpr (kNeg) return negate(v);
+    else return v;
 }
 
 // ---- phase R: a block per window of rows ----------------------------------------------------
@@ -167,16 +152,29 @@ __device__ __forceinline__ void window_r(const RhsArgs& a, int win, unsigned cha
         for (int j = beg; j < end; ++j) s_owner[j] = (uint8_t)tid;
     }
     __syncthreads();
+    // FP64 stages the source-side terms un-negated: the row adds its destination-side terms
+    // and subtracts its source-side ones, x - y being x + (-y) exactly (IEEE 754), so no
+    // separate negation runs on the scarce FP64 pipe.
+    constexpr bool kNegTerms = sizeof(T) != 8;
 #pragma unroll 4
     for (int k = tid; k < n; k += kBlock) {
         const int t = s_owner[k];
-        s_term[k] = row_term<T>(a, s_dp[t], s_nd[t], s_sp[t], k - s_start[t], stream);
+        s_term[k] = row_term<T, kNegTerms>(a, s_dp[t], s_nd[t], s_sp[t], k - s_start[t], stream);
     }
     __syncthreads();
     if (!has_row) return;
     T acc = T(0);
     if constexpr (sizeof(T) == 8) {
-        for (int j = beg; j < end; ++j) acc = __dadd_rn(acc, s_term[j]);
+        const int mid = beg + s_nd[tid];
+        int j = beg;
+        if (mid > beg) {
+            // the reference starts from 0: 0 + t is t, except that both zeros give +0
+            const double t = s_term[beg];
+            acc = (__double_as_longlong(t) << 1) == 0 ? 0.0 : t;
+            j = beg + 1;
+        }
+        for (; j < mid; ++j) acc = __dadd_rn(acc, s_term[j]);
+        for (; j < end; ++j) acc = __dsub_rn(acc, s_term[j]);
     } else {
         if (end - beg > kLightMaxDeg) {
             T comp = T(0);
@@ -194,20 +192,73 @@ __device__ __forceinline__ void window_r(const RhsArgs& a, int win, unsigned cha
     vertex_f<T, VK>(static_cast<T*>(a.du), u, p, v, acc);
 }
 
+// ---- phase R: medium rows, a thread per row reading its terms from global memory -------------
+// Medium rows (degree kLightMaxDeg+1 .. kMediumMaxDeg) are sorted by degree over all of
+// them, so the 32 rows of a warp have nearly equal length and every lane of each add is
+// busy; loads are issued kBatch terms ahead of the adds.
+template <typename T, int VK>
+__device__ __forceinline__ void medium_rows_r(const RhsArgs& a, int blk) {
+    using A = Arith<T>;
+    constexpr int kBatch = 8;
+    const int slot = a.n_heavy + blk * kBlock + (int)threadIdx.x;
+    if (slot >= a.n_heavy + a.n_medium) return;
+    const T* __restrict__ y = static_cast<const T*>(a.y);
+    const T* __restrict__ ybkt = static_cast<const T*>(a.ybkt);
+    const uint64_t stream = policy_evict_first();
+    const int64_t v = __ldg(a.slot_vertex + slot);
+    const uint32_t dp = __ldg(a.dptr + v), sp = __ldg(a.sptr + v);
+    const int nd = (int)(__ldg(a.dptr + v + 1) - dp);
+    const int ns = (int)(__ldg(a.sptr + v + 1) - sp);
+    T acc = T(0), comp = T(0);
+    // F32: compensated sum of the buffer values (source side negated); FP64: the
+    // sequential sum, source-side terms subtracted (x - y == x + (-y))
+    auto add = [&](T t, bool src) {
+        if constexpr (sizeof(T) == 8) {
+            acc = src ? __dsub_rn(acc, t) : __dadd_rn(acc, t);
+        } else {
+            const T yk = A::sub(src ? -t : t, comp);
+            const T s2 = A::add(acc, yk);
+            comp = A::sub(A::sub(s2, acc), yk);
+            acc = s2;
+        }
+    };
+    for (int j0 = 0; j0 < nd; j0 += kBatch) {
+        T t[kBatch];
+#pragma unroll
+        for (int k = 0; k < kBatch; ++k)
+            t[k] = j0 + k < nd ? ld_hint(ybkt + ld_hint(a.loc + dp + j0 + k, stream), stream) : T(0);
+#pragma unroll
+        for (int k = 0; k < kBatch; ++k)
+            if (j0 + k < nd) add(t[k], false);
+    }
+    for (int j0 = 0; j0 < ns; j0 += kBatch) {
+        T t[kBatch];
+#pragma unroll
+        for (int k = 0; k < kBatch; ++k) t[k] = j0 + k < ns ? ld_hint(y + sp + j0 + k, stream) : T(0);
+#pragma unroll
+        for (int k = 0; k < kBatch; ++k)
+            if (j0 + k < ns) add(t[k], true);
+    }
+    if constexpr (sizeof(T) == 4) acc = A::sub(acc, comp);
+    vertex_f<T, VK>(static_cast<T*>(a.du), static_cast<const T*>(a.u), static_cast<const T*>(a.p), v, acc);
+}
+
+// Blocks: [medium rows, kBlock per block] [light windows].  Heavy rows are always launched
+// separately (launch_rhs with heavy_only).
 template <typename T, int VK, int MODE>
 __global__ void __launch_bounds__(kBlock, 8) row_phase_kernel(RhsArgs a) {
     __shared__ __align__(16) unsigned char smem[SmemR<T>::kBytes];
-    const int nh = a.heavy_separate ? 0 : a.n_heavy;
+    const int nm = (a.n_medium + kBlock - 1) / kBlock;
     const int b = blockIdx.x;
-    if (b < nh) heavy_row_r<T, VK, MODE>(a, b, smem);
-    else window_r<T, VK, MODE>(a, b - nh, smem);
+    if (b < nm) medium_rows_r<T, VK>(a, b);
+    else window_r<T, VK, MODE>(a, a.n_medium_windows + (b - nm), smem);
 }
 
 template <typename T, int VK, int EK>
 cudaError_t launch_typed(const RhsArgs& a, cudaStream_t s, int phases) {
     if ((phases & kPhaseEdge) && a.n_chunks > 0)
         edge_phase_kernel<T, VK, EK><<<(unsigned)a.n_chunks, kBlock, 0, s>>>(a);
-    const int grid = (a.heavy_separate ? 0 : a.n_heavy) + a.n_windows;
+    const int grid = (a.n_medium + kBlock - 1) / kBlock + (a.n_windows - a.n_medium_windows);
     if (!(phases & kPhaseRow) || grid == 0) return cudaGetLastError();
     if constexpr (sizeof(T) == 4) {
         row_phase_kernel<T, VK, kModeTree><<<grid, kBlock, 0, s>>>(a);

@@ -48,6 +48,16 @@ __device__ __forceinline__ uint32_t ld_hint(const uint32_t* ptr, uint64_t pol) {
     asm("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(r) : "l"(ptr), "l"(pol));
     return r;
 }
+__device__ __forceinline__ double2 ld_hint(const double2* ptr, uint64_t pol) {
+    double2 r;
+    asm("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(r.x), "=d"(r.y) : "l"(ptr), "l"(pol));
+    return r;
+}
+__device__ __forceinline__ float2 ld_hint(const float2* ptr, uint64_t pol) {
+    float2 r;
+    asm("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(r.x), "=f"(r.y) : "l"(ptr), "l"(pol));
+    return r;
+}
 __device__ __forceinline__ float ld_hint(const float* ptr, uint64_t pol) {
     float r;
     asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(r) : "l"(ptr), "l"(pol));
@@ -175,12 +185,14 @@ __device__ __forceinline__ double exact_scan_smem(double S, const double* __rest
 }
 
 // The same sum with a sliding window of 8 terms per lane (256 per step): each lane scales
-// and prefix-sums its 8 terms locally, one warp scan adds the lanes before it, and every
-// position checks that its running sum stays strictly inside S's binade.  The window then
-// slides to just past the first position that failed (a binade change or a tie), which is
-// added with the hardware adder.  Long hub rows change binade every ~50-100 terms, so a
-// step advances far at the cost of a single warp scan.
+// its 8 terms (resolving ties against the running sum's parity) and prefix-sums them
+// locally, one warp scan adds the lanes before it, and every position checks that its
+// running sum stays strictly inside S's binade.  The window then slides to just past the
+// first position that failed (a binade change), which is added with the hardware adder.
+// Long hub rows change binade every ~100 terms, so a step advances far at the cost of a
+// single warp scan.
 constexpr int kScanPer = 8;
+constexpr int kScanFallback = 16;
 static __device__ __forceinline__ double exact_scan_wide(double S, const double* __restrict__ tile, int n, int lane) {
     int pos = 0;
     while (pos < n) {
@@ -194,16 +206,58 @@ static __device__ __forceinline__ double exact_scan_wide(double S, const double*
         const int end = min(n, pos + 32 * kScanPer);
         const int base = pos + lane * kScanPer;
         int64_t pre[kScanPer];
-        unsigned okmask = 0;
-        int64_t run = 0;
+        unsigned okmask = 0, tiemask = 0;
 #pragma unroll
         for (int i = 0; i < kScanPer; ++i) {
             bool ok = true, tie = false;
             const int q = base + i;
-            const int64_t R = q < end ? scaled_term(tile[q], eS, ok, tie) : 0;
-            run += R;
+            pre[i] = q < end ? scaled_term(tile[q], eS, ok, tie) : 0;
+            okmask |= (unsigned)ok << i;
+            tiemask |= (unsigned)tie << i;
+        }
+        if (__any_sync(kFull, tiemask != 0)) {
+            // Ties round to even against the running sum, whose parity evolves as
+            // p -> p ^ (R & 1) for an ordinary step and p -> 0 after a tie.  Each lane
+            // composes its steps into p -> (p & ka) ^ kb, a warp scan composes the lanes,
+            // and each lane replays its steps from the parity before its first one.
+            unsigned ka = 1u, kb = 0u;
+#pragma unroll
+            for (int i = 0; i < kScanPer; ++i) {
+                if ((tiemask >> i) & 1u) ka = kb = 0u;
+                else kb ^= (unsigned)(pre[i] & 1);
+            }
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const unsigned pa = __shfl_up_sync(kFull, ka, off), pb = __shfl_up_sync(kFull, kb, off);
+                if (lane >= off) {
+                    kb = (pb & ka) ^ kb;
+                    ka = pa & ka;
+                }
+            }
+            unsigned xa = __shfl_up_sync(kFull, ka, 1), xb = __shfl_up_sync(kFull, kb, 1);
+            if (lane == 0) {
+                xa = 1u;
+                xb = 0u;
+            }
+            unsigned par = ((unsigned)(sb & 1) & xa) ^ xb;
+#pragma unroll
+            for (int i = 0; i < kScanPer; ++i) {
+                if ((tiemask >> i) & 1u) {
+                    const uint64_t mag = (uint64_t)(pre[i] < 0 ? -pre[i] : pre[i]);
+                    const uint64_t c = (par ^ (unsigned)(mag & 1)) & 1u;  // 1: away from zero
+                    pre[i] = (exact::to_bits(tile[base + i]) & exact::kSign) ? -(int64_t)(mag + c)
+                                                                              : (int64_t)(mag + c);
+                    par = 0u;
+                } else {
+                    par ^= (unsigned)(pre[i] & 1);
+                }
+            }
+        }
+        int64_t run = 0;
+#pragma unroll
+        for (int i = 0; i < kScanPer; ++i) {
+            run += pre[i];
             pre[i] = run;
-            okmask |= (unsigned)(ok && !tie) << i;
         }
         int64_t x = run;
 #pragma unroll
@@ -238,10 +292,10 @@ static __device__ __forceinline__ double exact_scan_wide(double S, const double*
             S = __dadd_rn(S, tile[P]);
             const int advanced = P + 1 - pos;
             pos = P + 1;
-            // A sum hovering near zero changes binade every few terms and the scan stalls;
-            // then a short run of hardware adds on lane 0 is cheaper per term.
+            // A sum hovering at a binade boundary changes binade every few terms and the
+            // scan stalls; then a short run of hardware adds on lane 0 is cheaper per term.
             if (advanced < kScanPer && pos < n) {
-                const int stop = min(n, pos + 64);
+                const int stop = min(n, pos + kScanFallback);
                 if (lane == 0)
                     for (int i = pos; i < stop; ++i) S = __dadd_rn(S, tile[i]);
                 S = __shfl_sync(kFull, S, 0);
