@@ -1,0 +1,145 @@
+"""
+    NetworkDynamicsGB300
+
+Julia side of the GB300 network right-hand side: an `ExecutionStyle` / aggregator pair
+that NetworkDynamics.jl's `Network` constructor accepts like its own
+(`execution=GB300Execution(), aggregator=GB300Aggregator(+)`), and whose RHS `ccall`s
+`libnd_b200.so` (C ABI in `include/nd_gb300.h`).
+
+Plug points used (paths relative to the NetworkDynamics.jl source tree):
+- `ExecutionStyle{buffered}` (src/executionstyles.jl:13): `GB300Execution <: ExecutionStyle{false}`;
+- the curried aggregator constructor called as `aggregator(im, edgebatches)`
+  (src/construction.jl:198) and `get_aggr_constructor` (src/aggregators.jl:287-292);
+- `Adapt.adapt_structure(CuArray{T}, nw)` (ext/NetworkDynamicsCUDAExt.jl:16-45), which adapts
+  `nw.layer` field by field and so reaches `Adapt.adapt_structure(to, ::GB300Aggregator)`;
+- `iscudacompatible` (src/executionstyles.jl:50-52, src/aggregators.jl:294-295).
+
+Only the hand-written component library runs on this path; any other component function
+raises an `ArgumentError` when the aggregator is built.  There is no CPU fallback.
+"""
+module NetworkDynamicsGB300
+
+using NetworkDynamics: NetworkDynamics, Network, ExecutionStyle, AntiSymmetric, executionstyle
+using CUDA: CUDA, CuArray, CuPtr
+using Adapt: Adapt
+
+export GB300Execution, GB300Aggregator, register_gb300_vertex!, register_gb300_edge!
+
+const libnd = get(ENV, "ND_GB300_LIB", joinpath(@__DIR__, "..", "nd_gb300", "lib", "libnd_b200.so"))
+
+# status codes and enums of include/nd_gb300.h
+const ND_OK = Cint(0)
+const ND_ERR_ARG = Cint(-1)
+const ND_ERR_UNSUPPORTED_COMPONENT = Cint(-2)
+const ND_ERR_DTYPE = Cint(-3)
+const ND_F32 = Cint(1)
+const ND_F64 = Cint(2)
+const ND_ANTISYMMETRIC = Cint(1)
+
+struct nd_network_desc
+    nv::Int64
+    ne::Int64
+    src::Ptr{Int64}
+    dst::Ptr{Int64}
+    vertex_kind::Int32
+    edge_kind::Int32
+    coupling::Int32
+    flags::Int32
+end
+
+"""
+    GB300Execution()
+
+Unbuffered execution style whose RHS is one call into libnd_b200.so.
+"""
+struct GB300Execution <: ExecutionStyle{false} end
+
+# Known component functions -> library kinds (nd_vertex_kind / nd_edge_kind).  Models
+# built from the component library register their functions here.
+const VERTEX_KINDS = IdDict{Any,Cint}()
+const EDGE_KINDS = IdDict{Any,Cint}()
+register_gb300_vertex!(f, kind::Integer) = (VERTEX_KINDS[f] = Cint(kind); f)
+register_gb300_edge!(g, kind::Integer) = (EDGE_KINDS[g] = Cint(kind); g)
+
+mutable struct GB300Aggregator{F}
+    f::F
+    nv::Int
+    src::Vector{Int64}       # 0-based, edges(g) order
+    dst::Vector{Int64}
+    vertex_kind::Cint
+    edge_kind::Cint
+    handle::Ptr{Cvoid}       # C_NULL until adapted to the device
+    dtype::Cint
+end
+
+"""
+    GB300Aggregator(+)
+
+Curried like every NetworkDynamics aggregator: returns the `(im, batches)` constructor the
+`Network` calls with its index layout.  Only `+` is supported (as for SparseAggregator).
+"""
+function GB300Aggregator(f)
+    f === (+) || throw(ArgumentError("GB300Aggregator only works with + as reducer."))
+    (im, batches) -> GB300Aggregator(im, batches, f)
+end
+
+function GB300Aggregator(im, batches, f)
+    nw_vm = unique(map(m -> m.f, im.vertexm))
+    length(nw_vm) == 1 || throw(ArgumentError("GB300Execution needs one homogeneous vertex batch"))
+    vk = get(VERTEX_KINDS, only(nw_vm), Cint(0))
+    vk == 0 && throw(ArgumentError("vertex function $(only(nw_vm)) is not in the GB300 component library; \
+                                    GB300Execution has no CPU fallback"))
+    length(batches) == 1 || throw(ArgumentError("GB300Execution needs one homogeneous edge batch"))
+    g = only(batches).compg
+    g isa AntiSymmetric || throw(ArgumentError("only AntiSymmetric edges are in the GB300 library"))
+    ek = get(EDGE_KINDS, g.g, Cint(0))
+    ek == 0 && throw(ArgumentError("edge function $(g.g) is not in the GB300 component library; \
+                                    GB300Execution has no CPU fallback"))
+    src = Int64[e.src - 1 for e in im.edgevec]
+    dst = Int64[e.dst - 1 for e in im.edgevec]
+    GB300Aggregator{typeof(f)}(f, length(im.v_data), src, dst, vk, ek, C_NULL, Cint(0))
+end
+
+NetworkDynamics.get_aggr_constructor(a::GB300Aggregator) = GB300Aggregator(a.f)
+NetworkDynamics.iscudacompatible(::GB300Execution) = true
+NetworkDynamics.iscudacompatible(::Type{<:GB300Execution}) = true
+NetworkDynamics.iscudacompatible(::GB300Aggregator) = true
+
+last_error() = unsafe_string(ccall((:nd_last_error, libnd), Cstring, ()))
+
+function check(code::Cint)
+    code == ND_OK && return nothing
+    msg = last_error()
+    code in (ND_ERR_ARG, ND_ERR_DTYPE, ND_ERR_UNSUPPORTED_COMPONENT) && throw(ArgumentError(msg))
+    error("libnd_b200: [$code] $msg")
+end
+
+# adapt(CuArray{T}, nw) reaches the aggregator through @adapt_structure NetworkLayer: build
+# the device handle for element type T (the reference's cache typing at adapt time).
+function Adapt.adapt_structure(::Type{<:CuArray{T}}, a::GB300Aggregator) where {T<:Union{Float32,Float64}}
+    dtype = T === Float64 ? ND_F64 : ND_F32
+    desc = nd_network_desc(a.nv, length(a.src), pointer(a.src), pointer(a.dst), a.vertex_kind, a.edge_kind,
+                           ND_ANTISYMMETRIC, 0)
+    out = GB300Aggregator{typeof(a.f)}(a.f, a.nv, a.src, a.dst, a.vertex_kind, a.edge_kind, C_NULL, dtype)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve a check(ccall((:nd_create, libnd), Cint, (Ref{nd_network_desc}, Cint, Ref{Ptr{Cvoid}}),
+                               desc, dtype, h))
+    out.handle = h[]
+    finalizer(x -> x.handle == C_NULL || ccall((:nd_destroy, libnd), Cint, (Ptr{Cvoid},), x.handle), out)
+    out
+end
+
+# The RHS: one stream-ordered call on CUDA.jl's task-local stream.
+function (nw::Network{<:GB300Execution})(du::CuArray{T}, u::CuArray{T}, p, t) where {T}
+    a = nw.layer.aggregator
+    a.handle == C_NULL && throw(ArgumentError("adapt the network with adapt(CuArray{$T}, nw) first"))
+    dtype = T === Float64 ? ND_F64 : T === Float32 ? ND_F32 : Cint(0)
+    pp, np = p === nothing || isempty(p) ? (CuPtr{T}(0), 0) : (pointer(p), length(p))
+    check(ccall((:nd_rhs, libnd), Cint,
+                (Ptr{Cvoid}, Cint, CuPtr{T}, Int64, CuPtr{T}, Int64, CuPtr{T}, Int64, Cdouble, Ptr{Cvoid}),
+                a.handle, dtype, pointer(du), length(du), pointer(u), length(u), pp, np, Float64(t),
+                CUDA.stream().handle))
+    nothing
+end
+
+end # module
