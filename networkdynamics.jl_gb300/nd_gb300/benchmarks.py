@@ -142,8 +142,6 @@ def ensemble(n=4096, nv_lo=50, nv_hi=5000, t_end=50.0, reltol=1e-6, abstol=1e-6,
                      "steps_mean": float(r.nsteps.double().mean().item()), "ok": int((st == 0).sum())}
     err = np.abs(finals["f32"] - finals["f64"])
     per_inst = np.maximum.reduceat(err, e64.u_offset[:-1].astype(np.int64))
-    out["f32_final_state_err_vs_f64"] = {"max": float(err.max()), "median_instance": float(np.median(per_inst)),
-                                         "instances_within_1e-6": int((per_inst <= 1e-6).sum())}
     # synchronised / desynchronised verdict per instance: max |ω| at T below 0.1
     verdict = {}
     for name in ("f64", "f32"):
@@ -152,9 +150,17 @@ def ensemble(n=4096, nv_lo=50, nv_hi=5000, t_end=50.0, reltol=1e-6, abstol=1e-6,
         verdict[name] = per < 0.1
     out["sync_fraction_f64"] = float(verdict["f64"].mean())
     out["sync_verdict_agreement_f32_vs_f64"] = float((verdict["f64"] == verdict["f32"]).mean())
+    sync = verdict["f64"]
+    out["f32_final_state_err_vs_f64"] = {
+        "max": float(err.max()), "median_instance": float(np.median(per_inst)),
+        "instances_within_1e-6": int((per_inst <= 1e-6).sum()),
+        "synchronised_max": float(per_inst[sync].max()) if sync.any() else None,
+        "synchronised_median": float(np.median(per_inst[sync])) if sync.any() else None,
+        "desynchronised_median": float(np.median(per_inst[~sync])) if (~sync).any() else None}
     # the plain per-instance FP64 GPU solve on a sample of the instances
     idx = rng.choice(n, size=min(baseline_sample, n), replace=False)
     t_plain = 0.0
+    d64, d32 = [], []  # final-state differences of the batched solves from the plain one
     for i in idx:
         g = graphs[i]
         net = nd.adapt(nd.Network(g, nd.kuramoto_second(), nd.static_line()), torch.float64)
@@ -163,13 +169,20 @@ def ensemble(n=4096, nv_lo=50, nv_hi=5000, t_end=50.0, reltol=1e-6, abstol=1e-6,
         solve_tsit5(net, ui, pi, (0.0, 0.5), reltol, abstol)  # warm-up
         _sync()
         t0 = time.perf_counter()
-        solve_tsit5(net, ui, pi, (0.0, t_end), reltol, abstol)
+        uT, _ = solve_tsit5(net, ui, pi, (0.0, t_end), reltol, abstol)
         _sync()
         t_plain += time.perf_counter() - t0
+        ref = uT.cpu().numpy()
+        sl = e64.u_slice(i)
+        d64.append(float(np.abs(finals["f64"][sl] - ref).max()))
+        d32.append(float(np.abs(finals["f32"][sl] - ref).max()))
     plain = len(idx) / t_plain
     _log(f"plain per-instance FP64: {len(idx)} solves in {t_plain:.2f} s")
-    out["plain_f64_per_instance"] = {"solves_per_s": plain, "sample": int(len(idx)),
-                                     "note": "solve_tsit5 of one Network at a time, sampled instances"}
+    out["plain_f64_per_instance"] = {
+        "solves_per_s": plain, "sample": int(len(idx)),
+        "note": "solve_tsit5 of one Network at a time, sampled instances",
+        "final_state_diff_batched_f64_vs_plain": {"median": float(np.median(d64)), "max": float(np.max(d64))},
+        "final_state_diff_batched_f32_vs_plain": {"median": float(np.median(d32)), "max": float(np.max(d32))}}
     out["f32_batched_vs_plain_f64"] = out["f32"]["solves_per_s"] / plain
     out["f64_batched_vs_plain_f64"] = out["f64"]["solves_per_s"] / plain
     return out
