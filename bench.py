@@ -31,6 +31,7 @@ sys.path.insert(0, str(ROOT / "networkdynamics.jl_gb300"))
 sys.path.insert(0, str(ROOT))
 
 METRIC = "RHS edges/s (% HBM peak) @10M-vertex"
+HEAVY_MIN_DEGREE = 2049  # rows this long run in the heavy-row kernel (kMediumMaxDeg + 1)
 NV_DEFAULT = 10_000_000
 M_BA = 4
 SEED = 1
@@ -72,11 +73,11 @@ def kernel_bytes(g, s):
       heavy rows  per row: slot vertex, slot pointer pair (12 B), u_v and du (s each);
                   per incidence the (nbr, eid) pair (8 B), u_nbr and w (s each)
       fused       the whole RHS (algorithmic_bytes)
-    Rows of degree > 512 are the heavy rows."""
+    Rows of degree > 2048 are the heavy rows."""
     nv, ne = g.nv, g.ne
     ndst = np.bincount(g.dst, minlength=nv)
     nsrc = np.bincount(g.src, minlength=nv)
-    heavy = (ndst + nsrc) > 512
+    heavy = (ndst + nsrc) > HEAVY_MIN_DEGREE - 1
     light = ~heavy
     nh, inc_h = int(heavy.sum()), int((ndst + nsrc)[heavy].sum())
     rows = int(light.sum()) * (20 + s) + int(ndst[light].sum()) * (4 + s) + int(nsrc[light].sum()) * s

@@ -142,8 +142,8 @@ int nd_set_layout(nd_handle* h, int layout);
  * off), then resets both.  Recorded events stay in the handle's pool until that call. */
 enum nd_kernel_kind {
     ND_KERNEL_EDGE_PHASE = 0, /* one thread per edge: edge outputs y, bucketed by destination */
-    ND_KERNEL_ROW_PHASE = 1,  /* row sums over y + vertex functions (light and medium rows) */
-    ND_KERNEL_HEAVY_ROWS = 2, /* rows of degree > 512, a block per row on the side stream */
+    ND_KERNEL_ROW_PHASE = 1,  /* row sums over y + vertex functions (rows of degree <= 2048) */
+    ND_KERNEL_HEAVY_ROWS = 2, /* rows of degree > 2048, a block per row on the side stream */
     ND_KERNEL_FUSED = 3,      /* single-kernel RHS (ND_LAYOUT_FUSED or non-canonical edges) */
     ND_KERNEL_KINDS = 4
 };

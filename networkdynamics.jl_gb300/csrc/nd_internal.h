@@ -45,7 +45,7 @@ inline int edge_pdim(int ek) { return ek == ND_E_DIFFUSION_UNIT ? 0 : 1; }
 // Longer rows (power-law hubs) get a block each and are summed by an exact parallel scan:
 // a per-thread chain that long would wait on the shared FP64 pipe at every step.
 constexpr int kLightMaxDeg = 32;
-constexpr int kMediumMaxDeg = 512;
+constexpr int kMediumMaxDeg = 2048;
 constexpr int kWindow = 256;
 constexpr int kLightRun = 8192;
 

@@ -201,10 +201,67 @@ __global__ void __launch_bounds__(kBlock, 8) rhs_kernel(RhsArgs a) {
 // shared with other blocks each of its steps waits for their instructions.
 constexpr int kHeavySoloSmem = 160 * 1024;
 
+// FP64 sequential sum of a heavy row in the solo kernel: warp 0 adds tile k of the row's
+// terms (exact scan, or the hardware DADD chain in the native mode) while warps 1..7
+// evaluate tile k + 1 into the other half of a double buffer, so the serial chain never
+// waits for its terms after the first tile.
+constexpr int kSoloTile = 8192;
+
+template <int VK, int EK, int MODE>
+__device__ __forceinline__ void solo_row_fp64(const RhsArgs& a, int slot, double* buf) {
+    constexpr int DV = VertexDims<VK>::dim;
+    const double* __restrict__ u = static_cast<const double*>(a.u);
+    const double* __restrict__ p = static_cast<const double*>(a.p);
+    const double* __restrict__ pe = p + a.nv * VertexDims<VK>::pdim;
+    const int2* __restrict__ incid = reinterpret_cast<const int2*>(a.incid);
+    const uint64_t keep = policy_evict_last(), stream = policy_evict_first();
+    const int64_t v = __ldg(a.slot_vertex + slot);
+    const uint32_t beg = __ldg(a.slot_ptr + slot), end = __ldg(a.slot_ptr + slot + 1);
+    const double uv = __ldg(u + v * DV);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int ntiles = (int)((end - beg + kSoloTile - 1) / kSoloTile);
+    auto load = [&](int k, int first, int stride) {
+        const uint32_t base = beg + (uint32_t)k * kSoloTile;
+        const int n = (int)min((uint32_t)kSoloTile, end - base);
+        double* dst = buf + (k & 1) * kSoloTile;
+#pragma unroll 4
+        for (int i = first; i < n; i += stride) {
+            const int2 inc = ld_hint(incid + base + i, stream);
+            const double un = ld_hint(u + (int64_t)inc.x * DV, keep);
+            const double w = edge_param<double, EK>(pe, inc.y & 0x7fffffff, stream);
+            dst[i] = incidence_term_w<double, EK>(uv, un, w, inc.y < 0);
+        }
+    };
+    if (ntiles > 0) load(0, tid, kBlock);
+    __syncthreads();
+    double S = 0.0;
+    for (int k = 0; k < ntiles; ++k) {
+        if (warp == 0) {
+            const double* cur = buf + (k & 1) * kSoloTile;
+            const int n = (int)min((uint32_t)kSoloTile, end - (beg + (uint32_t)k * kSoloTile));
+            if constexpr (MODE == kModeNative) {
+                if (lane == 0)
+                    for (int i = 0; i < n; ++i) S = __dadd_rn(S, cur[i]);
+            } else {
+                S = exact_scan_wide(S, cur, n, lane);
+            }
+        } else if (k + 1 < ntiles) {
+            load(k + 1, tid - 32, kBlock - 32);
+        }
+        __syncthreads();
+    }
+    if (tid == 0) vertex_f<double, VK>(static_cast<double*>(a.du), u, p, v, S);
+}
+
 template <typename T, int VK, int EK, int MODE>
 __global__ void __launch_bounds__(kBlock, 1) heavy_solo_kernel(RhsArgs a) {
     extern __shared__ __align__(16) unsigned char smem_dyn[];
-    block_row<T, VK, EK, MODE>(a, blockIdx.x, smem_dyn);
+    if constexpr (sizeof(T) == 8 && MODE != kModeTree) {
+        static_assert(2 * kSoloTile * sizeof(double) <= kHeavySoloSmem, "solo double buffer");
+        solo_row_fp64<VK, EK, MODE>(a, blockIdx.x, reinterpret_cast<double*>(smem_dyn));
+    } else {
+        block_row<T, VK, EK, MODE>(a, blockIdx.x, smem_dyn);
+    }
 }
 
 template <typename T, int VK, int EK, int MODE>

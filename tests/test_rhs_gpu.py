@@ -196,9 +196,9 @@ def test_full_size_ba10m_properties(cuda):
 @pytest.mark.parametrize("vk,ek", [(O.V_DIFFUSION, O.E_DIFFUSION), (O.V_SWING, O.E_KURAMOTO)])
 def test_exact_integer_sums_equal_hardware_sums(cuda, vk, ek):
     """The integer-exact adds / hub scan and hardware DADD chains give identical bits
-    (both are the sequential order); heavy rows (degree > 512) included."""
-    g = nd.barabasi_albert(300_000, 4, seed=21)
-    assert g.degree().max() > 512
+    (both are the sequential order); heavy rows (degree > 2048) included."""
+    g = nd.barabasi_albert(1_000_000, 4, seed=21)
+    assert g.degree().max() > 2048
     nw = make(g, vk, ek, np.float64)
     on = O.OracleNetwork.from_graph(g, vk, ek)
     u, p = random_inputs(on, vk, np.random.default_rng(4))
@@ -214,7 +214,8 @@ def test_exact_integer_sums_equal_hardware_sums(cuda, vk, ek):
 def test_two_phase_equals_fused_layout(cuda, vk, ek):
     """The edge-centric two-phase kernels and the fused kernel give identical bits, in every
     summation order (heavy rows included)."""
-    g = nd.barabasi_albert(200_000, 4, seed=31)
+    g = nd.barabasi_albert(1_000_000, 4, seed=31)
+    assert g.degree().max() > 2048
     nw = make(g, vk, ek, np.float64)
     on = O.OracleNetwork.from_graph(g, vk, ek)
     u, p = random_inputs(on, vk, np.random.default_rng(8))
@@ -233,8 +234,8 @@ def test_two_phase_equals_fused_layout(cuda, vk, ek):
 def test_kernel_counts_and_timing(cuda):
     """Each RHS launches edge phase + row phase (+ heavy rows on the side stream); the
     timer brackets each of them and leaves the results unchanged."""
-    g = nd.barabasi_albert(200_000, 4, seed=31)
-    assert g.degree().max() > 512
+    g = nd.barabasi_albert(1_000_000, 4, seed=31)
+    assert g.degree().max() > 2048
     nw = make(g, O.V_DIFFUSION, O.E_DIFFUSION, np.float64)
     on = O.OracleNetwork.from_graph(g, O.V_DIFFUSION, O.E_DIFFUSION)
     u, p = random_inputs(on, O.V_DIFFUSION, np.random.default_rng(2))
