@@ -134,14 +134,18 @@ __global__ void __launch_bounds__(kBlock) row_phase_kernel(RhsArgs a) {
             }
         }
     };
+    // The adds of a batch stop at the longest remaining run in the warp (a warp-uniform
+    // bound), so a warp issues no add for batch slots that none of its rows has.
     for (int j0 = 0; j0 < nd; j0 += kBatch) {
         T t[kBatch];
 #pragma unroll
         for (int k = 0; k < kBatch; ++k)
             t[k] = j0 + k < nd ? ld_hint(ybkt + ld_hint(a.loc + dp + j0 + k, stream), stream) : T(0);
+        const int lim = __reduce_max_sync(__activemask(), (unsigned)min(kBatch, nd - j0));
 #pragma unroll
         for (int k = 0; k < kBatch; ++k) {
-            if (j0 + k >= nd) break;
+            if (k >= lim) break;
+            if (j0 + k >= nd) continue;
             if (sizeof(T) == 8 && k == 0 && j0 == 0) {
                 const double t0 = (double)t[0];
                 acc = (T)((__double_as_longlong(t0) << 1) == 0 ? 0.0 : t0);
@@ -154,9 +158,12 @@ __global__ void __launch_bounds__(kBlock) row_phase_kernel(RhsArgs a) {
         T t[kBatch];
 #pragma unroll
         for (int k = 0; k < kBatch; ++k) t[k] = j0 + k < ns ? ld_hint(y + sp + j0 + k, stream) : T(0);
+        const int lim = __reduce_max_sync(__activemask(), (unsigned)min(kBatch, ns - j0));
 #pragma unroll
-        for (int k = 0; k < kBatch; ++k)
+        for (int k = 0; k < kBatch; ++k) {
+            if (k >= lim) break;
             if (j0 + k < ns) add(t[k], true);
+        }
     }
     if constexpr (sizeof(T) == 4) acc = A::sub(acc, comp);
     vertex_f<T, VK>(static_cast<T*>(a.du), static_cast<const T*>(a.u), static_cast<const T*>(a.p), v, acc);

@@ -193,8 +193,10 @@ __device__ __forceinline__ double exact_scan_smem(double S, const double* __rest
 // single warp scan.
 constexpr int kScanPer = 8;
 constexpr int kScanFallback = 16;
+constexpr int kScanFallbackMax = 1024;
 static __device__ __forceinline__ double exact_scan_wide(double S, const double* __restrict__ tile, int n, int lane) {
     int pos = 0;
+    int fallback = kScanFallback;  // length of the next run of hardware adds after a stall
     while (pos < n) {
         const uint64_t sb = exact::to_bits(S);
         const int eS = (int)((sb >> 52) & 0x7ff);
@@ -293,16 +295,23 @@ static __device__ __forceinline__ double exact_scan_wide(double S, const double*
             const int advanced = P + 1 - pos;
             pos = P + 1;
             // A sum hovering at a binade boundary changes binade every few terms and the
-            // scan stalls; then a short run of hardware adds on lane 0 is cheaper per term.
+            // scan stalls; then a run of hardware adds on lane 0 is cheaper per term.  The
+            // run doubles while the stalls persist (up to kScanFallbackMax terms) and drops
+            // back once a step advances far, so a row never costs much more than a plain
+            // chain of adds.
             if (advanced < kScanPer && pos < n) {
-                const int stop = min(n, pos + kScanFallback);
+                const int stop = min(n, pos + fallback);
                 if (lane == 0)
                     for (int i = pos; i < stop; ++i) S = __dadd_rn(S, tile[i]);
                 S = __shfl_sync(kFull, S, 0);
                 pos = stop;
+                fallback = min(2 * fallback, kScanFallbackMax);
+            } else if (advanced >= 64) {
+                fallback = kScanFallback;
             }
         } else {
             pos = end;
+            fallback = kScanFallback;
         }
     }
     return S;
