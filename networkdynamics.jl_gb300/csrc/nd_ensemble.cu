@@ -118,9 +118,27 @@ __device__ void instance_rhs(const EnsArgs& a, const Inst& s, const TU* __restri
         const uint32_t beg = a.row_ptr[s.vbase + v], end = a.row_ptr[s.vbase + v + 1];
         const T uv = (T)yi[v * DV];
         T acc = T(0);
-        for (uint32_t k = beg; k < end; ++k) {
-            const int32_t nb = a.nbr[k], ebits = a.eid[k];
-            acc = A::add(acc, incidence_term<T, EK>(uv, (T)yi[(int64_t)nb * DV], pe, ebits));
+        if constexpr (sizeof(T) < sizeof(TU)) {
+            // FP32 RHS on the FP64 state: the difference u_n - u_v is taken in the state's
+            // precision and rounded once, so phases that have wound far from zero keep
+            // their full resolution before the FP32 wrap and sine.  Both sides of an
+            // AntiSymmetric edge then contribute g applied to that difference.
+            const TU uvd = yi[v * DV];
+            for (uint32_t k = beg; k < end; ++k) {
+                const int32_t nb = a.nbr[k], ebits = a.eid[k];
+                const T d = (T)(yi[(int64_t)nb * DV] - uvd);
+                const int32_t e = ebits & 0x7fffffff;
+                T term;
+                if constexpr (EK == ND_E_DIFFUSION) term = A::mul(pe[e], d);
+                else if constexpr (EK == ND_E_DIFFUSION_UNIT) term = d;
+                else term = A::mul(pe[e], A::sin_phase(d));
+                acc = A::add(acc, term);
+            }
+        } else {
+            for (uint32_t k = beg; k < end; ++k) {
+                const int32_t nb = a.nbr[k], ebits = a.eid[k];
+                acc = A::add(acc, incidence_term<T, EK>(uv, (T)yi[(int64_t)nb * DV], pe, ebits));
+            }
         }
         // vertex f into a local buffer of the instance's dim
         T out[DV];
