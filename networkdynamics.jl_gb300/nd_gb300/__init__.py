@@ -11,6 +11,7 @@ from .components import (EdgeModel, VertexModel, diffusion_edge, diffusion_edge_
 from .graphs import Graph, barabasi_albert, complete_graph, cycle_graph, random_geometric, simple_graph, watts_strogatz
 from .network import (ExecutionStyle, GB300Aggregator, GB300Execution, Network, adapt, get_aggr_constructor,
                       iscudacompatible, jvp)
+from .fixpoint import find_fixpoint
 from .mpnn import MPNN
 
 __all__ = [
@@ -20,5 +21,5 @@ __all__ = [
     "Graph", "barabasi_albert", "complete_graph", "cycle_graph", "random_geometric", "simple_graph",
     "watts_strogatz",
     "ExecutionStyle", "GB300Aggregator", "GB300Execution", "Network", "adapt", "get_aggr_constructor",
-    "iscudacompatible", "jvp", "MPNN",
+    "iscudacompatible", "jvp", "MPNN", "find_fixpoint",
 ]

@@ -129,3 +129,27 @@ def test_fixpoint_known_answer_and_oracle(cuda):
         on = O.OracleNetwork.from_graph(g, O.V_SWING, O.E_KURAMOTO)
         assert np.max(np.abs(on.rhs(u[ens.u_slice(i)], ps[i]))) <= 1e-10
         assert int(r.iters[i]) <= it_ref + 2
+
+
+def test_find_fixpoint_known_answer_and_errors(cuda):
+    """find_fixpoint on one network: the 4-node swing of test/initialization_test.jl:15-38
+    (neighbouring phases differ by asin(1/12)), and NotConvergedError when the lines cannot
+    carry the injections (the reference raises NetworkInitError)."""
+    g4 = nd.cycle_graph(4)
+    net = nd.Network(g4, nd.kuramoto_second(), nd.static_line())
+    P = np.array([1.0, -1.0, 1.0, -1.0])
+    p = np.concatenate([np.stack([np.ones(4), np.full(4, 0.1), P], 1).ravel(), np.full(4, 6.0)])
+    u = nd.find_fixpoint(net, p).cpu().numpy()
+    np.testing.assert_allclose(np.abs(np.diff(u[0::2])), np.arcsin(1 / 12), atol=1e-12)
+    np.testing.assert_array_equal(u[1::2], 0.0)
+    on = O.OracleNetwork.from_graph(g4, O.V_SWING, O.E_KURAMOTO)
+    assert np.max(np.abs(on.rhs(u, p))) <= 1e-10
+    # a warm start from the answer converges at once
+    u2 = nd.find_fixpoint(net, p, x0=u).cpu().numpy()
+    np.testing.assert_allclose(u2[0::2] - u2[0], u[0::2] - u[0], atol=1e-12)
+    p_bad = p.copy()
+    p_bad[2::3][:4] = [20.0, -20.0, 20.0, -20.0]
+    with pytest.raises(nd.NotConvergedError):
+        nd.find_fixpoint(net, p_bad, max_newton=20)
+    with pytest.raises(nd.ArgumentError):
+        nd.find_fixpoint(nd.Network(g4, nd.kuramoto_first(), nd.kuramoto_edge()), np.zeros(8))
