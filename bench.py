@@ -366,9 +366,15 @@ def run_gb300(args, rank, world, local):
         ref = torch.empty_like(u)
         nw(ref, u, p, 0.0)
         err = (du32.double() - ref).abs().max().item()
+        nw32.kernel_times()
+        nw32.set_kernel_timing(True)
+        time_device(nw32, du32, u32, p32, min(args.steps, 200), stream)
+        kt32 = nw32.kernel_times()
+        nw32.set_kernel_timing(False)
         line["f32"] = {"value": world * ne * args.steps / t32, "unit": "edges/s", "ms_per_step": 1e3 * t32 / args.steps,
                        "achieved_gbs": B32 / (t32 / args.steps) / 1e9,
-                       "frac": B32 / (t32 / args.steps) / 1e9 / hbm, "max_abs_err_vs_f64": err}
+                       "frac": B32 / (t32 / args.steps) / 1e9 / hbm, "max_abs_err_vs_f64": err,
+                       "kernels_avg_ms": {k: tot / n for k, (n, tot) in kt32.items() if n}}
         del nw32, u32, p32, du32
     # end to end through the public API with pinned host buffers: every step copies its
     # inputs (u, p) host->device and its result du device->host.  Two buffer sets and

@@ -212,9 +212,6 @@ int build_topology(int64_t nv, int64_t ne, const int64_t* src, const int64_t* ds
     t.n_medium = (int32_t)medium.size();
     t.n_heavy = (int32_t)heavy.size();
     t.n_windows = (int32_t)win_ptr.size() - 1;
-    t.n_medium_windows = 0;
-    while (t.n_medium_windows < t.n_windows && win_ptr[(size_t)t.n_medium_windows] < (int32_t)medium.size())
-        ++t.n_medium_windows;
     auto upload = [&](void** dptr, const void* hptr, size_t bytes) -> cudaError_t {
         cudaError_t err = cudaMalloc(dptr, std::max<size_t>(bytes, 16));
         if (err != cudaSuccess) return err;
@@ -424,7 +421,6 @@ int nd_rhs(nd_handle* h, int dtype, void* du, int64_t n_du, const void* u, int64
     a.n_medium = h->topo.n_medium;
     a.n_heavy = h->topo.n_heavy;
     a.n_windows = h->topo.n_windows;
-    a.n_medium_windows = h->topo.n_medium_windows;
     a.vertex_kind = h->vertex_kind;
     a.edge_kind = h->edge_kind;
     a.mode = h->rhs_mode;

@@ -90,7 +90,6 @@ struct Topology {
     Incidence* incid = nullptr;      // [2ne] incidences in slot order, each row by edge id (fused path)
     int32_t* win_ptr = nullptr;      // [n_windows+1] first slot of each light window
     int32_t n_light = 0, n_medium = 0, n_heavy = 0, n_windows = 0;
-    int32_t n_medium_windows = 0;    // the first windows, which hold exactly the medium rows
     EdgeLayout edge;
 };
 
@@ -117,11 +116,11 @@ struct RhsArgs {
     const int32_t* slot_vertex;
     const Incidence* incid;
     const int32_t* win_ptr;
-    int32_t n_light, n_medium, n_heavy, n_windows, n_medium_windows;
+    int32_t n_light, n_medium, n_heavy, n_windows;
     int32_t vertex_kind, edge_kind;
     int32_t mode;
     int32_t heavy_only;      // launch_rhs: only the heavy rows, one per SM
-    int32_t heavy_separate;  // launch_rhs_edge: heavy rows are launched elsewhere
+    int32_t heavy_separate;  // heavy rows are launched separately (heavy_only), not by this launch
     // edge-centric layout (see EdgeLayout)
     int64_t ne, n_chunks;
     const int32_t* esrc;
