@@ -80,9 +80,11 @@ __global__ void __launch_bounds__(kBlock) edge_phase_kernel(RhsArgs a) {
         P2 yv;
         yv.x = edge_g_w<T, EK>(us0, ud0, w0);
         yv.y = edge_g_w<T, EK>(us1, ud1, w1);
-        *reinterpret_cast<P2*>(y + e) = yv;
-        ybkt[q.x] = yv.x;
-        ybkt[q.y] = yv.y;
+        // the outputs stream through L2 ahead of the row phase: evict them first so the
+        // gathered u stays resident
+        st_hint(reinterpret_cast<P2*>(y + e), yv, stream);
+        st_hint(ybkt + q.x, yv.x, stream);
+        st_hint(ybkt + q.y, yv.y, stream);
     }
     if (((e1 - e0) & 1) && threadIdx.x == 0) {  // odd tail of the last chunk
         const int64_t e = e1 - 1;

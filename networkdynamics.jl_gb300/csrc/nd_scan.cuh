@@ -63,6 +63,21 @@ __device__ __forceinline__ float ld_hint(const float* ptr, uint64_t pol) {
     asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(r) : "l"(ptr), "l"(pol));
     return r;
 }
+// Stores with an L2 eviction-priority hint (streamed outputs: evict_first).
+__device__ __forceinline__ void st_hint(double* ptr, double v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;" ::"l"(ptr), "d"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st_hint(float* ptr, float v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(ptr), "f"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st_hint(double2* ptr, double2 v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.v2.f64 [%0], {%1, %2}, %3;" ::"l"(ptr), "d"(v.x), "d"(v.y), "l"(pol)
+                 : "memory");
+}
+__device__ __forceinline__ void st_hint(float2* ptr, float2 v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(ptr), "f"(v.x), "f"(v.y), "l"(pol)
+                 : "memory");
+}
 
 // Edge parameter of edge e (0 for the parameter-free unit diffusion edge).
 template <typename T, int EK>
