@@ -33,10 +33,8 @@ namespace mpnn {
 constexpr int kH = 64;
 constexpr float kWeightScale = 10.0f;
 constexpr int kBlock = 256;
-constexpr int kTileRows = 64;                // rows per block in the dense layer kernels
 constexpr int kGradBlocks = 304;             // blocks of the weight-gradient reductions
 constexpr int kPartialStride = 2 * kH * kH + kH;
-constexpr int kDenseSmem = (2 * kH * kH + kTileRows * (2 * kH + 1)) * (int)sizeof(float);
 
 __host__ __device__ inline int64_t off_win() { return 0; }
 __host__ __device__ inline int64_t off_bin() { return 2 * kH; }
@@ -114,61 +112,87 @@ __global__ void aggregate_kernel(int64_t R, int64_t nv, int64_t ne, const uint32
     }
 }
 
-// One residual layer forward for a tile of 64 rows: a = tanh([h | m] · Wᵀ + b), h' = h + a.
-// Shared memory: Wt[128][64] (Wt[i][o] = W_s[o][i] for i < 64, W_m[o][i-64] above) and the
-// input tile [64][129].  Each thread computes 16 units of one row.
+// The dense layers are register-tiled FP32 products over tiles of kTileRowsD rows: thread
+// (ty, tx) of a 16 x 16 block computes rows 8 ty .. 8 ty + 7 and units 4 tx .. 4 tx + 3,
+// reading for every k eight tile values (broadcast along the warp) and one float4 of the
+// weights, i.e. 32 FMAs per 9 shared-memory loads.  Tiles are loaded with float4 reads.
+constexpr int kTileRowsD = 128;
+constexpr int kLdA = 2 * kH + 4;  // padded row stride of the [h | m] tile
+constexpr int kLdG = kH + 4;      // padded row stride of a dz tile
+constexpr int kFwdSmem = (2 * kH * kH + kTileRowsD * kLdA) * (int)sizeof(float);
+constexpr int kBwdSmem = (2 * kH * kH + kTileRowsD * kLdG) * (int)sizeof(float);
+
+// One residual layer forward for a tile of rows: a = tanh([h | m] · Wᵀ + b), h' = h + a.
+// Shared memory: Bt[128][64] (Bt[k][n] = W_s[n][k] for k < 64, W_m[n][k - 64] above) and the
+// input tile [kTileRowsD][kLdA].
 __global__ void __launch_bounds__(kBlock) layer_forward_kernel(int64_t R, const float* __restrict__ h,
                                                                const float* __restrict__ m,
                                                                const float* __restrict__ Wl, float* __restrict__ a,
                                                                float* __restrict__ hn) {
     extern __shared__ __align__(16) float smem[];
-    float* Wt = smem;                  // [2H][H]
-    float* tile = smem + 2 * kH * kH;  // [kTileRows][2H + 1]
+    float* Bt = smem;                  // [2H][H]
+    float* As = smem + 2 * kH * kH;    // [kTileRowsD][kLdA]
     const float* Ws = Wl;
     const float* Wm = Wl + kH * kH;
     const float* bias = Wl + 2 * kH * kH;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     for (int t = tid; t < 2 * kH * kH; t += kBlock) {
-        const int i = t / kH, o = t - (t / kH) * kH;
-        Wt[t] = i < kH ? Ws[o * kH + i] : Wm[o * kH + (i - kH)];
+        const int k = t / kH, n = t - (t / kH) * kH;
+        Bt[t] = k < kH ? Ws[n * kH + k] : Wm[n * kH + (k - kH)];
     }
-    const int rr = tid >> 2, c0 = (tid & 3) * 16;
-    float bj[16];
-#pragma unroll
-    for (int c = 0; c < 16; ++c) bj[c] = bias[c0 + c];
-    for (int64_t r0 = (int64_t)blockIdx.x * kTileRows; r0 < R; r0 += (int64_t)gridDim.x * kTileRows) {
+    const float4 bj = reinterpret_cast<const float4*>(bias)[tx];
+    for (int64_t r0 = (int64_t)blockIdx.x * kTileRowsD; r0 < R; r0 += (int64_t)gridDim.x * kTileRowsD) {
         __syncthreads();
-        for (int t = tid; t < kTileRows * 2 * kH; t += kBlock) {
-            const int row = t / (2 * kH), i = t - row * (2 * kH);
+        // 128 rows x 32 float4 (16 of h, 16 of m)
+#pragma unroll 4
+        for (int f = tid; f < kTileRowsD * 32; f += kBlock) {
+            const int row = f >> 5, qd = f & 31;
             const int64_t r = r0 + row;
-            float v = 0.f;
-            if (r < R) v = i < kH ? h[r * kH + i] : m[r * kH + (i - kH)];
-            tile[row * (2 * kH + 1) + i] = v;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (r < R)
+                v = qd < 16 ? reinterpret_cast<const float4*>(h + r * kH)[qd]
+                            : reinterpret_cast<const float4*>(m + r * kH)[qd - 16];
+            *reinterpret_cast<float4*>(As + row * kLdA + 4 * qd) = v;
         }
         __syncthreads();
-        float acc[16];
+        float acc[8][4];
 #pragma unroll
-        for (int c = 0; c < 16; ++c) acc[c] = bj[c];
-        const float* trow = tile + rr * (2 * kH + 1);
-        for (int i = 0; i < 2 * kH; ++i) {
-            const float xi = trow[i];
-            const float4* w4 = reinterpret_cast<const float4*>(Wt + i * kH + c0);
+        for (int i = 0; i < 8; ++i) {
+            acc[i][0] = bj.x;
+            acc[i][1] = bj.y;
+            acc[i][2] = bj.z;
+            acc[i][3] = bj.w;
+        }
+        const float* arow = As + (ty * 8) * kLdA;
+#pragma unroll 4
+        for (int k = 0; k < 2 * kH; ++k) {
+            const float4 bv = reinterpret_cast<const float4*>(Bt + k * kH)[tx];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const float4 w = w4[q];
-                acc[4 * q] = fmaf(xi, w.x, acc[4 * q]);
-                acc[4 * q + 1] = fmaf(xi, w.y, acc[4 * q + 1]);
-                acc[4 * q + 2] = fmaf(xi, w.z, acc[4 * q + 2]);
-                acc[4 * q + 3] = fmaf(xi, w.w, acc[4 * q + 3]);
+            for (int i = 0; i < 8; ++i) {
+                const float av = arow[i * kLdA + k];
+                acc[i][0] = fmaf(av, bv.x, acc[i][0]);
+                acc[i][1] = fmaf(av, bv.y, acc[i][1]);
+                acc[i][2] = fmaf(av, bv.z, acc[i][2]);
+                acc[i][3] = fmaf(av, bv.w, acc[i][3]);
             }
         }
-        const int64_t r = r0 + rr;
-        if (r < R) {
 #pragma unroll
-            for (int c = 0; c < 16; ++c) {
-                const float av = tanhf(acc[c]);
-                a[r * kH + c0 + c] = av;
-                hn[r * kH + c0 + c] = trow[c0 + c] + av;
+        for (int i = 0; i < 8; ++i) {
+            const int row = ty * 8 + i;
+            const int64_t r = r0 + row;
+            if (r < R) {
+                const float4 hv = *reinterpret_cast<const float4*>(As + row * kLdA + 4 * tx);
+                float4 av, nv;
+                av.x = tanhf(acc[i][0]);
+                av.y = tanhf(acc[i][1]);
+                av.z = tanhf(acc[i][2]);
+                av.w = tanhf(acc[i][3]);
+                nv.x = hv.x + av.x;
+                nv.y = hv.y + av.y;
+                nv.z = hv.z + av.z;
+                nv.w = hv.w + av.w;
+                reinterpret_cast<float4*>(a + r * kH)[tx] = av;
+                reinterpret_cast<float4*>(hn + r * kH)[tx] = nv;
             }
         }
     }
@@ -254,106 +278,129 @@ __global__ void tanh_back_kernel(int64_t n, const float* __restrict__ dh, const 
         dz[t] = dh[t] * (1.f - a[t] * a[t]);
 }
 
-// Input gradients of one layer for a tile of 64 rows: [g_h | g_m] = dz · [W_s | W_m];
-// dh += g_h (the residual path already holds dh'), dmsc = g_m ⊙ inv_s (the scaled message
-// gradient, aggregated into dh afterwards).  Each thread computes 32 of the 128 outputs.
+// Input gradients of one layer for a tile of rows: g_h = dz · W_s and g_m = dz · W_m (the
+// weights are [out][in], so dz · W needs no transpose); dh += g_h (the residual path already
+// holds dh'), dmsc = g_m ⊙ inv_s (the scaled message gradient, aggregated into dh
+// afterwards).  Register-tiled like the forward layer, the two products one after the other.
 __global__ void __launch_bounds__(kBlock) layer_backward_kernel(int64_t R, const float* __restrict__ dz,
                                                                 const float* __restrict__ Wl,
                                                                 const float* __restrict__ inv_s,
                                                                 float* __restrict__ dh, float* __restrict__ dmsc) {
     extern __shared__ __align__(16) float smem[];
-    float* Wc = smem;                  // [H][2H]: Wc[o][j] = W_s[o][j] (j < H), W_m[o][j - H]
-    float* tile = smem + 2 * kH * kH;  // [kTileRows][H + 1]
-    const float* Ws = Wl;
-    const float* Wm = Wl + kH * kH;
-    const int tid = threadIdx.x;
-    for (int t = tid; t < 2 * kH * kH; t += kBlock) {
-        const int o = t / (2 * kH), j = t - o * (2 * kH);
-        Wc[t] = j < kH ? Ws[o * kH + j] : Wm[o * kH + (j - kH)];
-    }
-    const int rr = tid >> 2, c0 = (tid & 3) * 32;
-    for (int64_t r0 = (int64_t)blockIdx.x * kTileRows; r0 < R; r0 += (int64_t)gridDim.x * kTileRows) {
+    float* Bw = smem;                  // [2][H][H]: W_s then W_m, as stored
+    float* As = smem + 2 * kH * kH;    // [kTileRowsD][kLdG]
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    for (int t = tid; t < 2 * kH * kH / 4; t += kBlock)
+        reinterpret_cast<float4*>(Bw)[t] = reinterpret_cast<const float4*>(Wl)[t];
+    for (int64_t r0 = (int64_t)blockIdx.x * kTileRowsD; r0 < R; r0 += (int64_t)gridDim.x * kTileRowsD) {
         __syncthreads();
-        for (int t = tid; t < kTileRows * kH; t += kBlock) {
-            const int row = t / kH, o = t - row * kH;
+#pragma unroll 4
+        for (int f = tid; f < kTileRowsD * 16; f += kBlock) {
+            const int row = f >> 4, qd = f & 15;
             const int64_t r = r0 + row;
-            tile[row * (kH + 1) + o] = r < R ? dz[r * kH + o] : 0.f;
+            const float4 v = r < R ? reinterpret_cast<const float4*>(dz + r * kH)[qd] : make_float4(0.f, 0.f, 0.f, 0.f);
+            *reinterpret_cast<float4*>(As + row * kLdG + 4 * qd) = v;
         }
         __syncthreads();
-        float acc[32];
+        const float* arow = As + (ty * 8) * kLdG;
+#pragma unroll 1
+        for (int part = 0; part < 2; ++part) {
+            const float* B = Bw + part * kH * kH;
+            float acc[8][4];
 #pragma unroll
-        for (int c = 0; c < 32; ++c) acc[c] = 0.f;
-        const float* trow = tile + rr * (kH + 1);
-        for (int o = 0; o < kH; ++o) {
-            const float d = trow[o];
-            const float4* w4 = reinterpret_cast<const float4*>(Wc + o * 2 * kH + c0);
+            for (int i = 0; i < 8; ++i) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = 0.f;
+#pragma unroll 4
+            for (int k = 0; k < kH; ++k) {
+                const float4 bv = reinterpret_cast<const float4*>(B + k * kH)[tx];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const float4 w = w4[q];
-                acc[4 * q] = fmaf(d, w.x, acc[4 * q]);
-                acc[4 * q + 1] = fmaf(d, w.y, acc[4 * q + 1]);
-                acc[4 * q + 2] = fmaf(d, w.z, acc[4 * q + 2]);
-                acc[4 * q + 3] = fmaf(d, w.w, acc[4 * q + 3]);
+                for (int i = 0; i < 8; ++i) {
+                    const float av = arow[i * kLdG + k];
+                    acc[i][0] = fmaf(av, bv.x, acc[i][0]);
+                    acc[i][1] = fmaf(av, bv.y, acc[i][1]);
+                    acc[i][2] = fmaf(av, bv.z, acc[i][2]);
+                    acc[i][3] = fmaf(av, bv.w, acc[i][3]);
+                }
             }
-        }
-        const int64_t r = r0 + rr;
-        if (r < R) {
-            if (c0 < kH) {
 #pragma unroll
-                for (int c = 0; c < 32; ++c) dh[r * kH + c0 + c] += acc[c];
-            } else {
-                const float sc = inv_s[r];
-#pragma unroll
-                for (int c = 0; c < 32; ++c) dmsc[r * kH + (c0 - kH) + c] = acc[c] * sc;
+            for (int i = 0; i < 8; ++i) {
+                const int64_t r = r0 + ty * 8 + i;
+                if (r >= R) continue;
+                if (part == 0) {
+                    float4* o = reinterpret_cast<float4*>(dh + r * kH) + tx;
+                    float4 v = *o;
+                    v.x += acc[i][0];
+                    v.y += acc[i][1];
+                    v.z += acc[i][2];
+                    v.w += acc[i][3];
+                    *o = v;
+                } else {
+                    const float sc = inv_s[r];
+                    reinterpret_cast<float4*>(dmsc + r * kH)[tx] =
+                        make_float4(acc[i][0] * sc, acc[i][1] * sc, acc[i][2] * sc, acc[i][3] * sc);
+                }
             }
         }
     }
 }
 
 // Per-block partials of one layer's weight gradients over its row range:
-// [o][i] Σ dz_o h_i, then [o][i] Σ dz_o m_i, then [o] Σ dz_o.  Thread t owns unit o = t / 4
-// and inputs i0..i0+15, i0 = 16 (t % 4).
+// [o][i] Σ dz_o h_i, then [o][i] Σ dz_o m_i, then [o] Σ dz_o.  Thread (to, ti) owns units
+// 4 to .. 4 to + 3 and inputs 4 ti .. 4 ti + 3 of both matrices: per row three float4 loads
+// from the staged tiles feed 32 FMAs.
 __global__ void __launch_bounds__(kBlock) layer_wgrad_kernel(int64_t R, const float* __restrict__ dz,
                                                              const float* __restrict__ h,
                                                              const float* __restrict__ m,
                                                              float* __restrict__ partial) {
-    constexpr int kRows = 32;
-    __shared__ float sdz[kRows][kH + 1], sh[kRows][kH], sm[kRows][kH];
-    const int tid = threadIdx.x;
-    const int o = tid >> 2, i0 = (tid & 3) * 16;
+    constexpr int kRows = 64;
+    __shared__ __align__(16) float sdz[kRows][kH], sh[kRows][kH], sm[kRows][kH];
+    const int tid = threadIdx.x, ti = tid & 15, to = tid >> 4;
     const int64_t per = (R + gridDim.x - 1) / gridDim.x;
     const int64_t r0 = (int64_t)blockIdx.x * per, r1 = imin64(R, r0 + per);
-    float gs[16], gm[16], gb = 0.f;
+    float gs[4][4], gm[4][4], gb[4];
 #pragma unroll
-    for (int c = 0; c < 16; ++c) gs[c] = gm[c] = 0.f;
+    for (int x = 0; x < 4; ++x) {
+        gb[x] = 0.f;
+#pragma unroll
+        for (int z = 0; z < 4; ++z) gs[x][z] = gm[x][z] = 0.f;
+    }
     for (int64_t rb = r0; rb < r1; rb += kRows) {
         const int nr = (int)imin64(kRows, r1 - rb);
         __syncthreads();
-        for (int t = tid; t < kRows * kH; t += kBlock) {
-            const int row = t / kH, i = t - row * kH;
+        for (int f = tid; f < kRows * 16; f += kBlock) {
+            const int row = f >> 4, qd = f & 15;
             const bool in = row < nr;
-            sdz[row][i] = in ? dz[(rb + row) * kH + i] : 0.f;
-            sh[row][i] = in ? h[(rb + row) * kH + i] : 0.f;
-            sm[row][i] = in ? m[(rb + row) * kH + i] : 0.f;
+            const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            reinterpret_cast<float4*>(sdz[row])[qd] = in ? reinterpret_cast<const float4*>(dz + (rb + row) * kH)[qd] : z4;
+            reinterpret_cast<float4*>(sh[row])[qd] = in ? reinterpret_cast<const float4*>(h + (rb + row) * kH)[qd] : z4;
+            reinterpret_cast<float4*>(sm[row])[qd] = in ? reinterpret_cast<const float4*>(m + (rb + row) * kH)[qd] : z4;
         }
         __syncthreads();
         for (int row = 0; row < nr; ++row) {
-            const float d = sdz[row][o];
-            gb += d;
+            const float4 d = reinterpret_cast<const float4*>(sdz[row])[to];
+            const float4 hv = reinterpret_cast<const float4*>(sh[row])[ti];
+            const float4 mv = reinterpret_cast<const float4*>(sm[row])[ti];
+            const float dd[4] = {d.x, d.y, d.z, d.w};
+            const float hh[4] = {hv.x, hv.y, hv.z, hv.w};
+            const float mm[4] = {mv.x, mv.y, mv.z, mv.w};
 #pragma unroll
-            for (int c = 0; c < 16; ++c) {
-                gs[c] = fmaf(d, sh[row][i0 + c], gs[c]);
-                gm[c] = fmaf(d, sm[row][i0 + c], gm[c]);
+            for (int x = 0; x < 4; ++x) {
+                gb[x] += dd[x];
+#pragma unroll
+                for (int z = 0; z < 4; ++z) {
+                    gs[x][z] = fmaf(dd[x], hh[z], gs[x][z]);
+                    gm[x][z] = fmaf(dd[x], mm[z], gm[x][z]);
+                }
             }
         }
     }
     float* out = partial + (int64_t)blockIdx.x * kPartialStride;
 #pragma unroll
-    for (int c = 0; c < 16; ++c) {
-        out[o * kH + i0 + c] = gs[c];
-        out[kH * kH + o * kH + i0 + c] = gm[c];
+    for (int x = 0; x < 4; ++x) {
+        const int o = 4 * to + x;
+        reinterpret_cast<float4*>(out + o * kH)[ti] = make_float4(gs[x][0], gs[x][1], gs[x][2], gs[x][3]);
+        reinterpret_cast<float4*>(out + kH * kH + o * kH)[ti] = make_float4(gm[x][0], gm[x][1], gm[x][2], gm[x][3]);
+        if (ti == 0) out[2 * kH * kH + o] = gb[x];
     }
-    if (i0 == 0) out[2 * kH * kH + o] = gb;
 }
 
 // Per-block partials of the encoder gradients: [o][k] Σ dz_o x_k (k < 2), then [o] Σ dz_o.
@@ -487,15 +534,15 @@ cudaError_t set_dense_smem() {
     static std::once_flag once;
     static cudaError_t status = cudaSuccess;
     std::call_once(once, [] {
-        status = cudaFuncSetAttribute(layer_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kDenseSmem);
+        status = cudaFuncSetAttribute(layer_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kFwdSmem);
         if (status == cudaSuccess)
             status =
-                cudaFuncSetAttribute(layer_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kDenseSmem);
+                cudaFuncSetAttribute(layer_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kBwdSmem);
     });
     return status;
 }
 
-unsigned dense_grid(int64_t R) { return (unsigned)std::min<int64_t>((R + kTileRows - 1) / kTileRows, 152 * 3); }
+unsigned dense_grid(int64_t R) { return (unsigned)std::min<int64_t>((R + kTileRowsD - 1) / kTileRowsD, 152 * 2); }
 
 // Forward pass over `batch` instances; with a target also the loss terms and dy.
 cudaError_t forward(nd_mpnn* m, int64_t batch, const float* P, const float* K, const float* target, float* theta,
@@ -517,7 +564,7 @@ cudaError_t forward(nd_mpnn* m, int64_t batch, const float* P, const float* K, c
                                                                  nullptr, m->inv_s, src, dst, 0);
             src = dst;
         }
-        layer_forward_kernel<<<dense_grid(R), kBlock, kDenseSmem, s>>>(
+        layer_forward_kernel<<<dense_grid(R), kBlock, kFwdSmem, s>>>(
             R, hl, ml, m->params + off_layer(l), m->a + (int64_t)l * R * kH, m->h + (int64_t)(l + 1) * R * kH);
     }
     decode_kernel<<<grid_for(R * 32), kBlock, 0, s>>>(R, m->h + (int64_t)L * R * kH, m->params, L, m->y);
@@ -541,7 +588,7 @@ cudaError_t backward(nd_mpnn* m, int64_t batch, const float* K, cudaStream_t s) 
         layer_wgrad_kernel<<<kGradBlocks, kBlock, 0, s>>>(R, m->dz, hl, ml, m->partial);
         reduce_partials_kernel<<<grid_for(kPartialStride), kBlock, 0, s>>>(kGradBlocks, kPartialStride, m->partial,
                                                                           G + off_layer(l));
-        layer_backward_kernel<<<dense_grid(R), kBlock, kDenseSmem, s>>>(R, m->dz, m->params + off_layer(l), m->inv_s,
+        layer_backward_kernel<<<dense_grid(R), kBlock, kBwdSmem, s>>>(R, m->dz, m->params + off_layer(l), m->inv_s,
                                                                         m->dh, m->dmsc);
         // dh += (Mᵀ)^hops dm with Mᵀ x = A (x / s) (the weights are symmetric); dmsc already
         // holds dm / s, dz is free again as the second ping-pong buffer
