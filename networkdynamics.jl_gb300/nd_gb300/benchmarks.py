@@ -29,7 +29,7 @@ def _log(msg):
     print(f"[{time.perf_counter() - _T0:8.1f} s] {msg}", file=sys.stderr, flush=True)
 
 
-def warmstart(n_train=20000, n_test=2000, nv=2000, m=2, layers=4, epochs=30, batch=64, lr=2e-3, lr_final=5e-5,
+def warmstart(n_train=20000, n_test=2000, nv=2000, m=2, layers=4, epochs=80, batch=64, lr=2e-3, lr_final=5e-5,
               seed=0, tol=1e-10):
     """Swing steady states on BA(nv, m): solve n_train + n_test instances from the cold
     start, train the MPNN on the first n_train, compare cold and warm starts on the rest."""
@@ -240,7 +240,7 @@ def main():
     ap.add_argument("--train", type=int, default=20000)
     ap.add_argument("--test", type=int, default=2000)
     ap.add_argument("--nv", type=int, default=None)
-    ap.add_argument("--epochs", type=int, default=30)
+    ap.add_argument("--epochs", type=int, default=80)
     ap.add_argument("--instances", type=int, default=4096)
     ap.add_argument("--sample", type=int, default=16)
     ap.add_argument("--t-end", type=float, default=50.0)

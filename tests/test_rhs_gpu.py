@@ -82,6 +82,22 @@ def test_f32_against_f64_oracle(cuda, gname, vk, ek):
     assert np.all(np.abs(got - ref) <= bound), np.max(np.abs(got - ref) / bound)
 
 
+@pytest.mark.parametrize("layout", ["auto", "fused"])
+def test_f32_heavy_rows_against_f64_oracle(cuda, layout):
+    """FP32 with rows above the heavy-row degree (compensated block sums), on both layouts."""
+    g = nd.simple_graph(6001, [(0, i) for i in range(1, 6001)] + [(i, i + 1) for i in range(1, 6000, 7)])
+    for vk, ek in [(O.V_DIFFUSION, O.E_DIFFUSION), (O.V_SWING, O.E_KURAMOTO)]:
+        nw = make(g, vk, ek, np.float32)
+        nw.set_layout(layout)
+        on = O.OracleNetwork.from_graph(g, vk, ek)
+        u, p = random_inputs(on, vk, np.random.default_rng(9))
+        u32, p32 = u.astype(np.float32), p.astype(np.float32)
+        ref = on.rhs(u32.astype(np.float64), p32.astype(np.float64))
+        got = gpu_rhs(nw, u32, p32, cuda, np.float32).astype(np.float64)
+        terms = on.abs_terms(u32.astype(np.float64), p32.astype(np.float64))
+        assert np.all(np.abs(got - ref) <= 4e-6 * (terms + np.abs(ref)))
+
+
 def test_tree_order_is_deterministic_and_close(cuda):
     g = nd.barabasi_albert(50_000, 4, seed=11)
     nw = make(g, O.V_DIFFUSION, O.E_DIFFUSION, np.float64)
