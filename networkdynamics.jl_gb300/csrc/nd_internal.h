@@ -66,7 +66,7 @@ constexpr int kWindowIncidences = 2048;  // light window: at most this many inci
 //      while the rows of that range run) and then -y over its source block.
 // Each edge's function is evaluated once instead of twice, and the edge parameters and
 // the incidence stream are read in order instead of gathered.
-constexpr int kEdgeChunk = 4096;  // edges per phase-E block
+constexpr int kEdgeChunk = 2048;  // edges per phase-E block
 constexpr int kBuckets = 64;
 
 struct EdgeLayout {

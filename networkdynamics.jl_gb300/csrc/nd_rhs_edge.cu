@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(kBlock) edge_phase_kernel(RhsArgs a) {
     // vector-aligned only when that offset is even
     const bool wvec = EK == ND_E_DIFFUSION_UNIT || (reinterpret_cast<uintptr_t>(pe) % sizeof(P2)) == 0;
     const int64_t npair = (e1 - e0) >> 1;
-#pragma unroll 2
+#pragma unroll 4
     for (int64_t k = threadIdx.x; k < npair; k += kBlock) {
         const int64_t e = e0 + 2 * k;
         const int2 s = ld_hint(reinterpret_cast<const int2*>(a.esrc + e), stream);
