@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(kBlock) edge_phase_kernel(RhsArgs a) {
 template <typename T, int VK>
 __global__ void __launch_bounds__(kBlock) row_phase_kernel(RhsArgs a) {
     using A = Arith<T>;
-    constexpr int kBatch = 16;
+    constexpr int kBatch = 12;
     const int64_t slot = (int64_t)a.n_heavy + (int64_t)blockIdx.x * kBlock + threadIdx.x;
     if (slot >= a.nv) return;
     const T* __restrict__ y = static_cast<const T*>(a.y);
