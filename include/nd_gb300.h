@@ -50,17 +50,32 @@ enum nd_dtype { ND_F32 = 1, ND_F64 = 2 };
 enum nd_vertex_kind {
     ND_V_DIFFUSION = 1, /* diffusionvertex!  dv = Σe                 test/ComponentLibrary.jl:42-46   dim 1, pdim 0          */
     ND_V_KURAMOTO = 2,  /* kuramoto_vertex!  dθ = ω + Σe             test/ComponentLibrary.jl:69-72   dim 1, pdim 1 (ω)      */
-    ND_V_SWING = 3      /* kuramoto_inertia! dθ = ω, dω = (Pm-Dω+Σe)/M test/ComponentLibrary.jl:59-67 dim 2, pdim 3 (M,D,Pm) */
+    ND_V_SWING = 3,     /* kuramoto_inertia! dθ = ω, dω = (Pm-Dω+Σe)/M test/ComponentLibrary.jl:59-67 dim 2, pdim 3 (M,D,Pm) */
+    ND_V_SWING_UNIT = 4 /* kuramoto_inertia! of the benchmarks: dθ = ω, dω = (P - 1.0ω) + Σe
+                           benchmark/benchmark_models.jl:37-42                                 dim 2, pdim 1 (P)      */
 };
 enum nd_edge_kind {
     ND_E_DIFFUSION = 1,      /* diffusionedge!   e = w·(vs-vd)   test/ComponentLibrary.jl:8-13   pdim 1 (w) */
     ND_E_DIFFUSION_UNIT = 2, /* diffusion_edge!  e = vs-vd       test/diffusion_test.jl:57-60    pdim 0     */
-    ND_E_KURAMOTO = 3        /* kuramoto_edge! / static power line  e = K·sin(vs-vd)
+    ND_E_KURAMOTO = 3,       /* kuramoto_edge! / static power line  e = K·sin(vs-vd)
                                 test/ComponentLibrary.jl:51-57, :96-115                          pdim 1 (K) */
+    /* Edges with states (ODE edges).  States (e1, e2); outputs Fiducial(dst=1, src=2):
+     * y_dst = e1, y_src = e2. */
+    ND_E_DIFFUSION_ODE = 4,      /* diffusion_dedge!  de1 = 1/τ·(sin(vs-vd) - e1), de2 = 1/τ·(sin(vd-vs) - e2)
+                                    test/ComponentLibrary.jl:30-40                  dim 2, pdim 1 (τ)  */
+    ND_E_DIFFUSION_ODE_FIXED = 5 /* the same with the rate fixed: de = 100.0·(sin(..) - e)
+                                    benchmark/benchmark_models.jl:11-16             dim 2, pdim 0      */
 };
-/* Output wrapper of the edge (src/component_functions.jl:101-203).  The library edges are
- * AntiSymmetric: y_dst = g(...), y_src = -y_dst. */
-enum nd_coupling { ND_ANTISYMMETRIC = 1 };
+/* Output wrapper of the edge (src/component_functions.jl:101-203):
+ *   ND_ANTISYMMETRIC  y_dst = g(...), y_src = -y_dst          (:117-126)
+ *   ND_SYMMETRIC      y_dst = g(...), y_src = y_dst           (:142-151)
+ *   ND_DIRECTED       y_dst = g(...), y_src = 0               (:167-175)
+ *   ND_FIDUCIAL       separate src / dst outputs: Fiducial(src, dst) of StateMasks
+ *                     (:190-203), the outputs of the ODE kinds, and the two-sided
+ *                     diffusionedge_fid! (test/ComponentLibrary.jl:22-28: y_dst = w·(vs-vd),
+ *                     y_src = -y_dst), the only static kind that takes ND_FIDUCIAL.
+ * Static kinds take the first three; ND_FIDUCIAL is the only coupling of the ODE kinds. */
+enum nd_coupling { ND_ANTISYMMETRIC = 1, ND_SYMMETRIC = 2, ND_DIRECTED = 3, ND_FIDUCIAL = 4 };
 
 /* Summation order of the per-vertex edge aggregation. */
 enum nd_sum_order {
@@ -73,8 +88,10 @@ enum nd_sum_order {
 
 /* Network description, the information Network(g, vertexm, edgem) holds
  * (src/construction.jl:31-236).  Edges are given in Graphs.jl `edges(g)` order with
- * 0-based endpoints; edge k owns parameter slot k of the edge parameter block.  One
- * homogeneous vertex batch and one homogeneous edge batch. */
+ * 0-based endpoints; edge k owns parameter slot k of the edge parameter block (and, for
+ * ODE edges, states 2k, 2k+1 of the edge state block after the vertex states).  One
+ * homogeneous vertex batch and one homogeneous edge batch; nd_create_batched takes
+ * several. */
 typedef struct nd_network_desc {
     int64_t nv;          /* number of vertices                           */
     int64_t ne;          /* number of edges                              */
@@ -99,6 +116,8 @@ typedef struct nd_info {
     int32_t max_degree;
     int32_t n_hubs;       /* vertices on the cooperative (warp / CTA) path   */
     int32_t sum_order;    /* enum nd_sum_order in use                       */
+    int32_t n_vertex_batches; /* batches of the layout (1 for nd_create)    */
+    int32_t n_edge_batches;
 } nd_info;
 
 typedef struct nd_handle nd_handle;
@@ -113,8 +132,51 @@ const char* nd_last_error(void);
  * degree buckets and upload it.  Replaces the aggregator constructor call
  * `aggregator(im, edgebatches)` (src/construction.jl:198) together with
  * Adapt.adapt_structure(CuArray{T}, nw) (ext/NetworkDynamicsCUDAExt.jl:16-45).
- * Uses the current CUDA device. */
+ * Uses the current CUDA device.  A description outside the static AntiSymmetric kinds
+ * 1-3 (an ODE edge, another coupling, ND_V_SWING_UNIT) is built as a batched network of
+ * one vertex and one edge batch (nd_create_batched). */
 int nd_create(const nd_network_desc* desc, int dtype, nd_handle** out);
+
+/* Heterogeneous networks: several vertex and edge batches, Network(g, vertexms, edgems)
+ * with vectors of components (src/construction.jl:155-195).  The reference groups
+ * identical components into batches in order of first appearance (find_identical,
+ * src/utils.jl:197-216) and lays the flat vectors out batch by batch
+ * (src/network_structure.jl:224-258): all vertex batches first (states, outputs,
+ * parameters), then the edge batches (states after every vertex state, parameters after
+ * every vertex parameter); inside a batch, components in ascending index order.  The
+ * caller passes the batches in the reference's order and the batch of every component;
+ * the handle then uses exactly that layout for u, du and p.
+ *   batch kinds      vertex batches: enum nd_vertex_kind, coupling 0; edge batches:
+ *                    enum nd_edge_kind with its enum nd_coupling (ND_ERR_UNSUPPORTED_COMPONENT
+ *                    for a pair outside the library)
+ *   n_*_batches      1..ND_MAX_BATCHES vertex batches; 0..ND_MAX_BATCHES edge batches (0
+ *                    only without edges).  A batch may be empty.
+ * The RHS follows the reference's order of operations and SequentialAggregator's order
+ * of additions (ascending output index).  Networks of one static AntiSymmetric edge
+ * batch and one vertex batch of kinds 1-3 take the same kernels as nd_create; all others
+ * a batched two-kernel RHS (edge kernel with per-batch dispatch, then row sums and
+ * vertex functions).  nd_jvp and the ensemble calls do not take batched handles
+ * (ND_ERR_UNSUPPORTED). */
+#define ND_MAX_BATCHES 32
+typedef struct nd_batch {
+    int32_t kind;     /* enum nd_vertex_kind / enum nd_edge_kind */
+    int32_t coupling; /* edge batches: enum nd_coupling; vertex batches: 0 */
+} nd_batch;
+typedef struct nd_batched_network_desc {
+    int64_t nv;                     /* number of vertices                              */
+    int64_t ne;                     /* number of edges                                 */
+    const int64_t* src;             /* [ne] host, 0-based, edges(g) order              */
+    const int64_t* dst;             /* [ne] host                                       */
+    int32_t n_vertex_batches;
+    int32_t n_edge_batches;
+    const nd_batch* vertex_batches; /* [n_vertex_batches] host                         */
+    const nd_batch* edge_batches;   /* [n_edge_batches] host                           */
+    const int32_t* vertex_batch;    /* [nv] host: batch index of every vertex          */
+    const int32_t* edge_batch;      /* [ne] host: batch index of every edge            */
+    int32_t flags;                  /* reserved, must be 0                             */
+    int32_t reserved;
+} nd_batched_network_desc;
+int nd_create_batched(const nd_batched_network_desc* desc, int dtype, nd_handle** out);
 
 /* Free the handle and its device buffers (the Julia finalizer calls this). */
 int nd_destroy(nd_handle* h);
@@ -145,7 +207,9 @@ enum nd_kernel_kind {
     ND_KERNEL_ROW_PHASE = 1,  /* row sums over y + vertex functions (rows of degree <= 2048) */
     ND_KERNEL_HEAVY_ROWS = 2, /* rows of degree > 2048, a block per row on the side stream */
     ND_KERNEL_FUSED = 3,      /* single-kernel RHS (ND_LAYOUT_FUSED or non-canonical edges) */
-    ND_KERNEL_KINDS = 4
+    ND_KERNEL_BATCHED_EDGES = 4, /* batched networks: edge functions of every edge batch */
+    ND_KERNEL_BATCHED_ROWS = 5,  /* batched networks: row sums + vertex functions */
+    ND_KERNEL_KINDS = 6
 };
 int nd_set_kernel_timing(nd_handle* h, int on);
 int nd_kernel_times(nd_handle* h, int64_t* launches, double* ms, int n);

@@ -1,0 +1,469 @@
+// Batched (heterogeneous) networks: several vertex and edge batches, ODE edges and the
+// Symmetric / Directed / Fiducial output wrappers.
+//
+// The reference builds one batch per group of identical components
+// (src/construction.jl:155-195), lays the flat vectors out batch by batch
+// (src/network_structure.jl:224-258) and runs its core loop per batch
+// (src/coreloop.jl:111-155): vertex g, edge g / f, aggregation in output-buffer order
+// (SequentialAggregator, src/aggregators.jl:140-151), vertex f.  The GPU path needs two
+// launches for any number of batches:
+//   edges  one thread per edge position: the batch is found in a small table, the edge
+//          function of its kind runs (static g with its coupling, or the ODE edge's f,
+//          writing du of the edge states, and its StateMask outputs), and the pair
+//          (y_src, y_dst) is stored as one vector at y2[2k], the reference's output
+//          buffer order;
+//   rows   every vertex sums the y2 entries of its terms in ascending index order (the
+//          sequential aggregation order), then runs the vertex f of its batch.  Rows of
+//          degree above kLightMaxDeg take a warp each and sum by the exact scan (FP64:
+//          the same bits as the sequential sum), shorter rows a thread each, sorted by
+//          degree so the lanes of a warp do equal work.
+// Homogeneous networks of the static AntiSymmetric kinds keep the two-phase kernels of
+// nd_rhs_edge.cu; this path covers everything else in the library.
+#include <algorithm>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "nd_components.cuh"
+#include "nd_exact.cuh"
+#include "nd_internal.h"
+#include "nd_scan.cuh"
+
+namespace nd {
+
+namespace {
+
+using namespace dev;
+
+template <typename T>
+struct Vec2;
+template <>
+struct Vec2<double> {
+    using type = double2;
+};
+template <>
+struct Vec2<float> {
+    using type = float2;
+};
+
+struct BatchedKArgs {
+    void* du;
+    const void* u;
+    const void* p;
+    int64_t nv, ne, n_warp_rows;
+    const BatchTable* vb;  // device copies of the batch tables
+    const BatchTable* eb;
+    const int2* eu;
+    const uint32_t* tptr;
+    const int32_t* tidx;
+    const int32_t* slot_vpos;
+    void* y2;
+    int32_t mode;
+};
+
+// Batch of position `pos`: the last batch whose first position is <= pos (batches are few;
+// empty batches are skipped because the next one starts at the same position).
+__device__ __forceinline__ int find_batch(const BatchTable* __restrict__ t, int64_t pos) {
+    const int n = __ldg(&t->n);
+    int b = 0;
+    while (b + 1 < n && pos >= __ldg(&t->pos0[b + 1])) ++b;
+    return b;
+}
+
+template <typename T>
+__device__ __forceinline__ T static_edge_g(int kind, T vs, T vd, T w) {
+    if (kind == ND_E_DIFFUSION) return edge_g_w<T, ND_E_DIFFUSION>(vs, vd, w);
+    if (kind == ND_E_DIFFUSION_UNIT) return edge_g_w<T, ND_E_DIFFUSION_UNIT>(vs, vd, w);
+    return edge_g_w<T, ND_E_KURAMOTO>(vs, vd, w);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) batched_edge_kernel(BatchedKArgs a) {
+    using A = Arith<T>;
+    using V2 = typename Vec2<T>::type;
+    const T* __restrict__ u = static_cast<const T*>(a.u);
+    const T* __restrict__ p = static_cast<const T*>(a.p);
+    T* __restrict__ du = static_cast<T*>(a.du);
+    V2* __restrict__ y2 = static_cast<V2*>(a.y2);
+    for (int64_t k = (int64_t)blockIdx.x * kBlock + threadIdx.x; k < a.ne; k += (int64_t)gridDim.x * kBlock) {
+        const int b = find_batch(a.eb, k);
+        const int kind = __ldg(&a.eb->kind[b]);
+        const int64_t r = k - __ldg(&a.eb->pos0[b]);
+        const int2 uv = __ldg(a.eu + k);
+        const T vs = __ldg(u + uv.x), vd = __ldg(u + uv.y);  // vertex outputs: StateMask(1)
+        V2 y;
+        if (kind == ND_E_DIFFUSION_ODE || kind == ND_E_DIFFUSION_ODE_FIXED) {
+            const int64_t s = __ldg(&a.eb->s0[b]) + 2 * r;
+            const T e1 = __ldg(u + s), e2 = __ldg(u + s + 1);
+            const T rate = kind == ND_E_DIFFUSION_ODE ? A::div(T(1), __ldg(p + __ldg(&a.eb->p0[b]) + r)) : T(100);
+            T d1, d2;
+            ode_edge_f<T>(rate, vs, vd, e1, e2, d1, d2);
+            du[s] = d1;
+            du[s + 1] = d2;
+            y.x = e2;  // Fiducial(dst=1:1, src=2:2): y_src = e2, y_dst = e1
+            y.y = e1;
+        } else {
+            const T w = kind == ND_E_DIFFUSION_UNIT ? T(0) : __ldg(p + __ldg(&a.eb->p0[b]) + r);
+            const T yd = static_edge_g<T>(kind, vs, vd, w);
+            const int c = __ldg(&a.eb->coupling[b]);
+            // AntiSymmetric and the two-sided diffusionedge_fid!: y_src = -y_dst (a sign
+            // flip); Symmetric: y_src = y_dst; Directed: y_src = +0 (fill! with zero)
+            y.x = c == ND_SYMMETRIC ? yd : (c == ND_DIRECTED ? T(0) : -yd);
+            y.y = yd;
+        }
+        y2[k] = y;
+    }
+}
+
+// Sum of a row's n terms (y2 indices idx[0..n)) by one thread, in order.  FP64 folds the
+// reference's zero start into the first term (0 + t is t; -0 gives +0).
+template <typename T>
+__device__ __forceinline__ T thread_row_sum(const T* __restrict__ y2, const int32_t* __restrict__ idx, int n) {
+    using A = Arith<T>;
+    constexpr int kB = 8;
+    T acc = T(0);
+    for (int j0 = 0; j0 < n; j0 += kB) {
+        T t[kB];
+#pragma unroll
+        for (int k = 0; k < kB; ++k) t[k] = j0 + k < n ? __ldg(y2 + __ldg(idx + j0 + k)) : T(0);
+#pragma unroll
+        for (int k = 0; k < kB; ++k) {
+            if (j0 + k >= n) break;
+            if (sizeof(T) == 8 && j0 + k == 0) {
+                const double t0 = (double)t[0];
+                acc = (T)((__double_as_longlong(t0) << 1) == 0 ? 0.0 : t0);
+            } else {
+                acc = A::add(acc, t[k]);
+            }
+        }
+    }
+    return acc;
+}
+
+// Sum of a row's n terms by one warp (the result is valid in every lane).
+//   FP64 exact   the sequential sum, bit for bit, by the exact scan on the integer pipes
+//   FP64 native  the sequential sum with hardware adds (one warp-wide chain)
+//   FP64 tree    lane partial sums and a butterfly (deterministic, not the sequential bits)
+//   FP32         Kahan-compensated lane partial sums and a butterfly
+template <typename T>
+__device__ __forceinline__ T warp_row_sum(const T* __restrict__ y2, const int32_t* __restrict__ idx, int n, int lane,
+                                          int mode) {
+    if constexpr (sizeof(T) == 8) {
+        double S = 0.0;
+        for (int c = 0; c < n; c += 32) {
+            const int m = min(32, n - c);
+            const double t = lane < m ? __ldg(y2 + __ldg(idx + c + lane)) : 0.0;
+            if (mode == kModeExact) {
+                S = exact_scan_add(S, t, m, lane);
+            } else if (mode == kModeNative) {
+                for (int i = 0; i < m; ++i) S = __dadd_rn(S, __shfl_sync(kFull, t, i));
+            } else {
+                S = __dadd_rn(S, t);
+            }
+        }
+        if (mode == kModeTree) {
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) S = __dadd_rn(S, __shfl_xor_sync(kFull, S, off));
+        }
+        return (T)S;
+    } else {
+        float s = 0.f, comp = 0.f;
+        for (int j = lane; j < n; j += 32) {
+            const float yk = __fsub_rn(__ldg(y2 + __ldg(idx + j)), comp);
+            const float s2 = __fadd_rn(s, yk);
+            comp = __fsub_rn(__fsub_rn(s2, s), yk);
+            s = s2;
+        }
+        s = __fsub_rn(s, comp);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) s = __fadd_rn(s, __shfl_xor_sync(kFull, s, off));
+        return (T)s;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void batched_vertex_f(const BatchedKArgs& a, int64_t pos, T acc) {
+    const int b = find_batch(a.vb, pos);
+    const int kind = __ldg(&a.vb->kind[b]);
+    const int64_t r = pos - __ldg(&a.vb->pos0[b]);
+    const int64_t s0 = __ldg(&a.vb->s0[b]), q0 = __ldg(&a.vb->p0[b]);
+    T* du = static_cast<T*>(a.du);
+    const T* u = static_cast<const T*>(a.u);
+    const T* p = static_cast<const T*>(a.p);
+    switch (kind) {
+        case ND_V_DIFFUSION:
+            vertex_f_at<T, ND_V_DIFFUSION>(du, u, p, s0 + r, q0, acc);
+            break;
+        case ND_V_KURAMOTO:
+            vertex_f_at<T, ND_V_KURAMOTO>(du, u, p, s0 + r, q0 + r, acc);
+            break;
+        case ND_V_SWING:
+            vertex_f_at<T, ND_V_SWING>(du, u, p, s0 + 2 * r, q0 + 3 * r, acc);
+            break;
+        default:
+            vertex_f_at<T, ND_V_SWING_UNIT>(du, u, p, s0 + 2 * r, q0 + r, acc);
+            break;
+    }
+}
+
+// Rows: blocks [0, n_warp_blocks) take the long rows a warp each, the rest one row per
+// thread.
+template <typename T>
+__global__ void __launch_bounds__(kBlock) batched_row_kernel(BatchedKArgs a, int64_t n_warp_blocks) {
+    const T* __restrict__ y2 = static_cast<const T*>(a.y2);
+    if ((int64_t)blockIdx.x < n_warp_blocks) {
+        const int lane = threadIdx.x & 31;
+        const int64_t slot = (int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+        if (slot >= a.n_warp_rows) return;  // warp-uniform
+        const uint32_t t0 = __ldg(a.tptr + slot);
+        const int n = (int)(__ldg(a.tptr + slot + 1) - t0);
+        const T acc = warp_row_sum<T>(y2, a.tidx + t0, n, lane, a.mode);
+        if (lane == 0) batched_vertex_f<T>(a, __ldg(a.slot_vpos + slot), acc);
+    } else {
+        const int64_t slot = a.n_warp_rows + ((int64_t)blockIdx.x - n_warp_blocks) * kBlock + threadIdx.x;
+        if (slot >= a.nv) return;
+        const uint32_t t0 = __ldg(a.tptr + slot);
+        const int n = (int)(__ldg(a.tptr + slot + 1) - t0);
+        const T acc = thread_row_sum<T>(y2, a.tidx + t0, n);
+        batched_vertex_f<T>(a, __ldg(a.slot_vpos + slot), acc);
+    }
+}
+
+template <typename T>
+cudaError_t launch_typed(const BatchedNet& b, void* du, const void* u, const void* p, int mode, cudaStream_t s,
+                         int phases) {
+    BatchedKArgs a;
+    a.du = du;
+    a.u = u;
+    a.p = p;
+    a.nv = b.nv;
+    a.ne = b.ne;
+    a.n_warp_rows = b.n_warp_rows;
+    a.vb = b.d_vb;
+    a.eb = b.d_eb;
+    a.eu = b.eu;
+    a.tptr = b.tptr;
+    a.tidx = b.tidx;
+    a.slot_vpos = b.slot_vpos;
+    a.y2 = b.y2;
+    a.mode = mode;
+    if ((phases & kPhaseEdge) && b.ne > 0) {
+        const int64_t blocks = std::min<int64_t>((b.ne + kBlock - 1) / kBlock, int64_t(1) << 20);
+        batched_edge_kernel<T><<<(unsigned)blocks, kBlock, 0, s>>>(a);
+    }
+    if (phases & kPhaseRow) {
+        const int64_t wb = (b.n_warp_rows + kWarpsPerBlock - 1) / kWarpsPerBlock;
+        const int64_t tb = (b.nv - b.n_warp_rows + kBlock - 1) / kBlock;
+        if (wb + tb > 0) batched_row_kernel<T><<<(unsigned)(wb + tb), kBlock, 0, s>>>(a, wb);
+    }
+    return cudaGetLastError();
+}
+
+bool static_kind(int ek) { return ek >= ND_E_DIFFUSION && ek <= ND_E_KURAMOTO; }
+bool ode_kind(int ek) { return ek == ND_E_DIFFUSION_ODE || ek == ND_E_DIFFUSION_ODE_FIXED; }
+
+}  // namespace
+
+// Is (kind, coupling) an edge component of the library?
+int check_edge_component(int ek, int coupling) {
+    if (!static_kind(ek) && !ode_kind(ek))
+        return fail(ND_ERR_UNSUPPORTED_COMPONENT,
+                    "edge model is not in the GB300 component library (diffusion, unit diffusion, kuramoto / "
+                    "static line, diffusion ODE edge); no CPU fallback exists");
+    if (ode_kind(ek) && coupling != ND_FIDUCIAL)
+        return fail(ND_ERR_UNSUPPORTED_COMPONENT, "the diffusion ODE edges have Fiducial(dst=1, src=2) outputs");
+    if (static_kind(ek) && coupling != ND_ANTISYMMETRIC && coupling != ND_SYMMETRIC && coupling != ND_DIRECTED &&
+        !(coupling == ND_FIDUCIAL && ek == ND_E_DIFFUSION))
+        return fail(ND_ERR_UNSUPPORTED_COMPONENT,
+                    "edge coupling is not in the GB300 library for this edge kind (AntiSymmetric, Symmetric, "
+                    "Directed; Fiducial only for diffusionedge_fid!)");
+    return ND_OK;
+}
+
+void free_batched(BatchedNet* b) {
+    cudaFree(b->d_vb);
+    cudaFree(b->d_eb);
+    cudaFree(b->eu);
+    cudaFree(b->tptr);
+    cudaFree(b->tidx);
+    cudaFree(b->slot_vpos);
+    cudaFree(b->y2);
+    *b = BatchedNet{};
+}
+
+int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out) {
+    const int64_t nv = d->nv, ne = d->ne;
+    const int nvb = d->n_vertex_batches, neb = d->n_edge_batches;
+    if (nv <= 0) return fail(ND_ERR_ARG, "network has no vertices");
+    if (ne < 0) return fail(ND_ERR_ARG, "negative edge count");
+    if (d->flags != 0) return fail(ND_ERR_ARG, "nd_batched_network_desc.flags must be 0");
+    if (nvb < 1 || nvb > kMaxBatches) return fail(ND_ERR_ARG, "n_vertex_batches must be in 1..ND_MAX_BATCHES");
+    if (neb < 0 || neb > kMaxBatches || (ne > 0 && neb == 0))
+        return fail(ND_ERR_ARG, "n_edge_batches must be in 1..ND_MAX_BATCHES (0 only without edges)");
+    if (!d->vertex_batches || !d->vertex_batch || (neb > 0 && !d->edge_batches) ||
+        (ne > 0 && (!d->src || !d->dst || !d->edge_batch)))
+        return fail(ND_ERR_ARG, "nd_batched_network_desc: NULL array");
+    if (nv > INT32_MAX - 1) return fail(ND_ERR_UNSUPPORTED, "more than 2^31-2 vertices");
+    if (2 * ne > (int64_t)INT32_MAX) return fail(ND_ERR_UNSUPPORTED, "more than 2^30-1 edges in a batched network");
+    for (int b = 0; b < nvb; ++b) {
+        const nd_batch& vb = d->vertex_batches[b];
+        if (vb.kind < ND_V_DIFFUSION || vb.kind > ND_V_SWING_UNIT)
+            return fail(ND_ERR_UNSUPPORTED_COMPONENT,
+                        "vertex model is not in the GB300 component library (diffusion, kuramoto first order, "
+                        "swing, benchmark swing); no CPU fallback exists");
+        if (vb.coupling != 0) return fail(ND_ERR_ARG, "vertex batches take coupling 0");
+    }
+    for (int b = 0; b < neb; ++b) {
+        const int rc = check_edge_component(d->edge_batches[b].kind, d->edge_batches[b].coupling);
+        if (rc != ND_OK) return rc;
+    }
+    std::vector<int64_t> vcount(nvb, 0), ecount(std::max(neb, 1), 0);
+    for (int64_t v = 0; v < nv; ++v) {
+        const int32_t b = d->vertex_batch[v];
+        if (b < 0 || b >= nvb) return fail(ND_ERR_ARG, "vertex " + std::to_string(v) + " has no valid batch");
+        vcount[b]++;
+    }
+    for (int64_t e = 0; e < ne; ++e) {
+        const int32_t b = d->edge_batch[e];
+        if (b < 0 || b >= neb) return fail(ND_ERR_ARG, "edge " + std::to_string(e) + " has no valid batch");
+        const int64_t s = d->src[e], t = d->dst[e];
+        if (s < 0 || s >= nv || t < 0 || t >= nv)
+            return fail(ND_ERR_ARG, "edge " + std::to_string(e) + " has endpoint out of range");
+        ecount[b]++;
+    }
+    // Batch tables: vertex batches first (register_vertices!), then edge batches whose
+    // states follow every vertex state and whose parameters follow every vertex parameter
+    // (register_edges!, src/network_structure.jl:224-258).
+    BatchTable vb, eb;
+    int64_t pos = 0, st = 0, par = 0;
+    vb.n = nvb;
+    for (int b = 0; b < nvb; ++b) {
+        const int k = d->vertex_batches[b].kind;
+        vb.kind[b] = k;
+        vb.pos0[b] = pos;
+        vb.s0[b] = st;
+        vb.p0[b] = par;
+        pos += vcount[b];
+        st += vcount[b] * vertex_dim(k);
+        par += vcount[b] * vertex_pdim(k);
+    }
+    vb.pos0[nvb] = pos;
+    const int64_t vdim_total = st;
+    eb.n = neb;
+    pos = 0;
+    for (int b = 0; b < neb; ++b) {
+        const int k = d->edge_batches[b].kind;
+        eb.kind[b] = k;
+        eb.coupling[b] = d->edge_batches[b].coupling;
+        eb.pos0[b] = pos;
+        eb.s0[b] = st;
+        eb.p0[b] = par;
+        pos += ecount[b];
+        st += ecount[b] * edge_dim(k);
+        par += ecount[b] * edge_pdim(k);
+    }
+    eb.pos0[neb] = pos;
+    if (st > (int64_t)INT32_MAX) return fail(ND_ERR_UNSUPPORTED, "more than 2^31-1 states in a batched network");
+    (void)vdim_total;
+
+    // vertex positions and the u index of every vertex output (its first state)
+    std::vector<int64_t> fill(vb.pos0, vb.pos0 + nvb);
+    std::vector<int32_t> vpos(nv), vdata(nv);
+    for (int64_t v = 0; v < nv; ++v) {
+        const int b = d->vertex_batch[v];
+        const int64_t k = fill[b]++;
+        vpos[v] = (int32_t)k;
+        vdata[v] = (int32_t)(vb.s0[b] + (k - vb.pos0[b]) * vertex_dim(vb.kind[b]));
+    }
+    // edge positions
+    std::vector<int64_t> efill(eb.pos0, eb.pos0 + std::max(neb, 0));
+    std::vector<int64_t> order(ne);
+    for (int64_t e = 0; e < ne; ++e) order[efill[d->edge_batch[e]]++] = e;
+    std::vector<int2> eu(ne);
+    std::vector<uint32_t> deg(nv, 0);
+    for (int64_t k = 0; k < ne; ++k) {
+        const int64_t e = order[k];
+        eu[k] = make_int2(vdata[d->src[e]], vdata[d->dst[e]]);
+        deg[d->src[e]]++;
+        deg[d->dst[e]]++;
+    }
+    // every vertex's terms in ascending output order: for each edge position, the source's
+    // entry 2k before the destination's 2k+1
+    std::vector<uint32_t> vptr(nv + 1, 0);
+    for (int64_t v = 0; v < nv; ++v) vptr[v + 1] = vptr[v] + deg[v];
+    std::vector<int32_t> vterms((size_t)2 * ne);
+    {
+        std::vector<uint32_t> f(vptr.begin(), vptr.end() - 1);
+        for (int64_t k = 0; k < ne; ++k) {
+            const int64_t e = order[k];
+            vterms[f[d->src[e]]++] = (int32_t)(2 * k);
+            vterms[f[d->dst[e]]++] = (int32_t)(2 * k + 1);
+        }
+    }
+    // slot order: long rows by degree (descending), then short rows in runs of kLightRun
+    // vertex positions, by degree inside a run
+    std::vector<int32_t> by_pos(nv);
+    for (int64_t v = 0; v < nv; ++v) by_pos[vpos[v]] = (int32_t)v;
+    std::vector<int32_t> longr, shortr;
+    for (int64_t k = 0; k < nv; ++k) {
+        const int32_t v = by_pos[k];
+        (deg[v] > (uint32_t)kLightMaxDeg ? longr : shortr).push_back(v);
+    }
+    auto by_degree = [&](int32_t x, int32_t y) { return deg[x] > deg[y]; };
+    std::stable_sort(longr.begin(), longr.end(), by_degree);
+    for (size_t r0 = 0; r0 < shortr.size(); r0 += (size_t)kLightRun)
+        std::stable_sort(shortr.begin() + r0, shortr.begin() + std::min(shortr.size(), r0 + (size_t)kLightRun),
+                         by_degree);
+    std::vector<int32_t> slots;
+    slots.reserve(nv);
+    slots.insert(slots.end(), longr.begin(), longr.end());
+    slots.insert(slots.end(), shortr.begin(), shortr.end());
+    std::vector<uint32_t> tptr(nv + 1, 0);
+    std::vector<int32_t> tidx((size_t)2 * ne), slot_vpos(nv);
+    uint32_t maxdeg = 0;
+    for (int64_t s = 0; s < nv; ++s) {
+        const int32_t v = slots[s];
+        std::copy(vterms.begin() + vptr[v], vterms.begin() + vptr[v + 1], tidx.begin() + tptr[s]);
+        tptr[s + 1] = tptr[s] + deg[v];
+        slot_vpos[s] = vpos[v];
+        maxdeg = std::max(maxdeg, deg[v]);
+    }
+
+    BatchedNet bn;
+    bn.vb = vb;
+    bn.eb = eb;
+    bn.nv = nv;
+    bn.ne = ne;
+    bn.dim = st;
+    bn.pdim = par;
+    bn.max_degree = (int32_t)maxdeg;
+    bn.n_warp_rows = (int64_t)longr.size();
+    auto upload = [&](void** dptr, const void* hptr, size_t bytes) -> cudaError_t {
+        cudaError_t err = cudaMalloc(dptr, std::max<size_t>(bytes, 16));
+        if (err != cudaSuccess) return err;
+        if (bytes) err = cudaMemcpy(*dptr, hptr, bytes, cudaMemcpyHostToDevice);
+        return err;
+    };
+    cudaError_t err;
+    if ((err = upload((void**)&bn.d_vb, &vb, sizeof(BatchTable))) != cudaSuccess ||
+        (err = upload((void**)&bn.d_eb, &eb, sizeof(BatchTable))) != cudaSuccess ||
+        (err = upload((void**)&bn.eu, eu.data(), eu.size() * sizeof(int2))) != cudaSuccess ||
+        (err = upload((void**)&bn.tptr, tptr.data(), tptr.size() * sizeof(uint32_t))) != cudaSuccess ||
+        (err = upload((void**)&bn.tidx, tidx.data(), tidx.size() * sizeof(int32_t))) != cudaSuccess ||
+        (err = upload((void**)&bn.slot_vpos, slot_vpos.data(), slot_vpos.size() * sizeof(int32_t))) != cudaSuccess ||
+        (err = cudaMalloc(&bn.y2, std::max<size_t>((size_t)2 * ne * elem, 16))) != cudaSuccess) {
+        free_batched(&bn);
+        return cuda_fail(err, "upload of the batched network");
+    }
+    bn.enabled = true;
+    *out = bn;
+    return ND_OK;
+}
+
+cudaError_t launch_batched(int dtype, const BatchedNet& b, void* du, const void* u, const void* p, int mode,
+                           cudaStream_t s, int phases) {
+    return dtype == ND_F64 ? launch_typed<double>(b, du, u, p, mode, s, phases)
+                           : launch_typed<float>(b, du, u, p, mode, s, phases);
+}
+
+}  // namespace nd

@@ -290,30 +290,14 @@ int nd_version(void) { return ND_VERSION; }
 
 const char* nd_last_error(void) { return g_last_error.c_str(); }
 
-int nd_create(const nd_network_desc* desc, int dtype, nd_handle** out) {
-    clear_error();
-    if (!desc || !out) return fail(ND_ERR_ARG, "nd_create: NULL descriptor or output pointer");
-    *out = nullptr;
-    if (dtype != ND_F32 && dtype != ND_F64)
-        return fail(ND_ERR_DTYPE, "nd_create: dtype must be ND_F32 or ND_F64 "
-                                  "(adapt the network with CuArray{Float32} or CuArray{Float64})");
-    if (desc->vertex_kind < ND_V_DIFFUSION || desc->vertex_kind > ND_V_SWING)
-        return fail(ND_ERR_UNSUPPORTED_COMPONENT,
-                    "vertex model is not in the GB300 component library "
-                    "(diffusion, kuramoto first order, swing); no CPU fallback exists");
-    if (desc->edge_kind < ND_E_DIFFUSION || desc->edge_kind > ND_E_KURAMOTO)
-        return fail(ND_ERR_UNSUPPORTED_COMPONENT,
-                    "edge model is not in the GB300 component library "
-                    "(diffusion, unit diffusion, kuramoto / static line); no CPU fallback exists");
-    if (desc->coupling != ND_ANTISYMMETRIC)
-        return fail(ND_ERR_UNSUPPORTED_COMPONENT, "only AntiSymmetric edge coupling is in the GB300 library");
-    if (desc->flags != 0) return fail(ND_ERR_ARG, "nd_network_desc.flags must be 0");
+}  // extern "C"
 
+namespace nd {
+
+// A handle with its side stream and fork / join events (no network yet).
+static int new_handle(int dtype, nd_handle** out) {
     nd_handle* h = new nd_handle();
     h->dtype = dtype;
-    h->vertex_kind = desc->vertex_kind;
-    h->edge_kind = desc->edge_kind;
-    h->coupling = desc->coupling;
     h->sum_order = ND_ORDER_SEQUENTIAL;
     h->rhs_mode = kModeExact;
     h->edge_path = 1;
@@ -327,15 +311,123 @@ int nd_create(const nd_network_desc* desc, int dtype, nd_handle** out) {
         return cuda_fail(err, "nd_create: stream / event creation");
     }
     cudaGetDevice(&h->device);
+    *out = h;
+    return ND_OK;
+}
+
+static void delete_handle(nd_handle* h) {
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (h->side) cudaStreamDestroy(h->side);
+    delete h;
+}
+
+// The homogeneous kernels (nd_rhs_edge.cu, nd_rhs.cu) cover one vertex batch of kinds 1-3
+// with one static edge batch whose source output is -y_dst: AntiSymmetric, or the
+// two-sided diffusionedge_fid!, which computes the same values.
+static bool homogeneous_kinds(int vk, int ek, int coupling) {
+    return vk >= ND_V_DIFFUSION && vk <= ND_V_SWING && ek >= ND_E_DIFFUSION && ek <= ND_E_KURAMOTO &&
+           (coupling == ND_ANTISYMMETRIC || (coupling == ND_FIDUCIAL && ek == ND_E_DIFFUSION));
+}
+
+static int create_batched(const nd_batched_network_desc* d, int dtype, nd_handle** out) {
+    nd_handle* h = nullptr;
+    int rc = new_handle(dtype, &h);
+    if (rc != ND_OK) return rc;
+    rc = build_batched(d, dtype == ND_F64 ? 8 : 4, &h->batched);
+    if (rc != ND_OK) {
+        delete_handle(h);
+        return rc;
+    }
+    const BatchedNet& b = h->batched;
+    h->vertex_kind = b.vb.n == 1 ? b.vb.kind[0] : 0;
+    h->edge_kind = b.eb.n == 1 ? b.eb.kind[0] : 0;
+    h->coupling = b.eb.n == 1 ? b.eb.coupling[0] : 0;
+    h->dim = b.dim;
+    h->pdim = b.pdim;
+    h->topo.nv = b.nv;
+    h->topo.ne = b.ne;
+    h->topo.max_degree = b.max_degree;
+    *out = h;
+    return ND_OK;
+}
+
+}  // namespace nd
+
+extern "C" {
+
+int nd_create(const nd_network_desc* desc, int dtype, nd_handle** out) {
+    clear_error();
+    if (!desc || !out) return fail(ND_ERR_ARG, "nd_create: NULL descriptor or output pointer");
+    *out = nullptr;
+    if (dtype != ND_F32 && dtype != ND_F64)
+        return fail(ND_ERR_DTYPE, "nd_create: dtype must be ND_F32 or ND_F64 "
+                                  "(adapt the network with CuArray{Float32} or CuArray{Float64})");
+    if (desc->vertex_kind < ND_V_DIFFUSION || desc->vertex_kind > ND_V_SWING_UNIT)
+        return fail(ND_ERR_UNSUPPORTED_COMPONENT,
+                    "vertex model is not in the GB300 component library "
+                    "(diffusion, kuramoto first order, swing); no CPU fallback exists");
+    int rc = check_edge_component(desc->edge_kind, desc->coupling);
+    if (rc != ND_OK) return rc;
+    if (desc->flags != 0) return fail(ND_ERR_ARG, "nd_network_desc.flags must be 0");
+    if (!homogeneous_kinds(desc->vertex_kind, desc->edge_kind, desc->coupling)) {
+        // one vertex batch and one edge batch on the batched path
+        if (desc->nv <= 0) return fail(ND_ERR_ARG, "network has no vertices");
+        if (desc->ne < 0) return fail(ND_ERR_ARG, "negative edge count");
+        std::vector<int32_t> vb((size_t)desc->nv, 0), eb((size_t)std::max<int64_t>(desc->ne, 0), 0);
+        nd_batch vbatch{desc->vertex_kind, 0}, ebatch{desc->edge_kind, desc->coupling};
+        nd_batched_network_desc d{};
+        d.nv = desc->nv;
+        d.ne = desc->ne;
+        d.src = desc->src;
+        d.dst = desc->dst;
+        d.n_vertex_batches = 1;
+        d.n_edge_batches = 1;
+        d.vertex_batches = &vbatch;
+        d.edge_batches = &ebatch;
+        d.vertex_batch = vb.data();
+        d.edge_batch = eb.data();
+        return create_batched(&d, dtype, out);
+    }
+
+    nd_handle* h = nullptr;
+    rc = new_handle(dtype, &h);
+    if (rc != ND_OK) return rc;
+    h->vertex_kind = desc->vertex_kind;
+    h->edge_kind = desc->edge_kind;
+    h->coupling = desc->coupling;
     h->dim = desc->nv * vertex_dim(desc->vertex_kind);
     h->pdim = desc->nv * vertex_pdim(desc->vertex_kind) + desc->ne * edge_pdim(desc->edge_kind);
-    int rc = build_topology(desc->nv, desc->ne, desc->src, desc->dst, dtype == ND_F64 ? 8 : 4, &h->topo);
+    rc = build_topology(desc->nv, desc->ne, desc->src, desc->dst, dtype == ND_F64 ? 8 : 4, &h->topo);
     if (rc != ND_OK) {
-        delete h;
+        delete_handle(h);
         return rc;
     }
     *out = h;
     return ND_OK;
+}
+
+int nd_create_batched(const nd_batched_network_desc* desc, int dtype, nd_handle** out) {
+    clear_error();
+    if (!desc || !out) return fail(ND_ERR_ARG, "nd_create_batched: NULL descriptor or output pointer");
+    *out = nullptr;
+    if (dtype != ND_F32 && dtype != ND_F64)
+        return fail(ND_ERR_DTYPE, "nd_create_batched: dtype must be ND_F32 or ND_F64 "
+                                  "(adapt the network with CuArray{Float32} or CuArray{Float64})");
+    // one batch of each kind on the homogeneous kernels: the same layout, faster kernels
+    if (desc->n_vertex_batches == 1 && desc->n_edge_batches <= 1 && desc->vertex_batches && desc->flags == 0 &&
+        (desc->n_edge_batches == 0 ? desc->ne == 0 : desc->edge_batches != nullptr)) {
+        const nd_batch vb = desc->vertex_batches[0];
+        const nd_batch eb = desc->n_edge_batches ? desc->edge_batches[0] : nd_batch{ND_E_DIFFUSION_UNIT, ND_ANTISYMMETRIC};
+        bool ids_ok = desc->vertex_batch != nullptr && (desc->ne == 0 || desc->edge_batch != nullptr);
+        for (int64_t v = 0; ids_ok && v < desc->nv; ++v) ids_ok = desc->vertex_batch[v] == 0;
+        for (int64_t e = 0; ids_ok && e < desc->ne; ++e) ids_ok = desc->edge_batch[e] == 0;
+        if (ids_ok && vb.coupling == 0 && homogeneous_kinds(vb.kind, eb.kind, eb.coupling)) {
+            nd_network_desc d{desc->nv, desc->ne, desc->src, desc->dst, vb.kind, eb.kind, eb.coupling, 0};
+            return nd_create(&d, dtype, out);
+        }
+    }
+    return create_batched(desc, dtype, out);
 }
 
 int nd_destroy(nd_handle* h) {
@@ -345,13 +437,12 @@ int nd_destroy(nd_handle* h) {
     cudaGetDevice(&prev);
     if (prev != h->device) cudaSetDevice(h->device);
     if (h->side) cudaStreamSynchronize(h->side);
-    free_topology(&h->topo);
+    if (h->batched.enabled) free_batched(&h->batched);
+    else free_topology(&h->topo);
     h->tracer.release();
-    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
-    if (h->ev_join) cudaEventDestroy(h->ev_join);
-    if (h->side) cudaStreamDestroy(h->side);
-    if (prev >= 0 && prev != h->device) cudaSetDevice(prev);
-    delete h;
+    const int dev = h->device;
+    delete_handle(h);
+    if (prev >= 0 && prev != dev) cudaSetDevice(prev);
     return ND_OK;
 }
 
@@ -367,8 +458,10 @@ int nd_get_info(const nd_handle* h, nd_info* out) {
     out->vertex_kind = h->vertex_kind;
     out->edge_kind = h->edge_kind;
     out->max_degree = h->topo.max_degree;
-    out->n_hubs = h->topo.n_medium + h->topo.n_heavy;
+    out->n_hubs = h->batched.enabled ? (int32_t)h->batched.n_warp_rows : h->topo.n_medium + h->topo.n_heavy;
     out->sum_order = h->sum_order;
+    out->n_vertex_batches = h->batched.enabled ? h->batched.vb.n : 1;
+    out->n_edge_batches = h->batched.enabled ? h->batched.eb.n : 1;
     return ND_OK;
 }
 
@@ -408,6 +501,18 @@ int nd_rhs(nd_handle* h, int dtype, void* du, int64_t n_du, const void* u, int64
         return fail(ND_ERR_ARG, "p does not has expected size " + std::to_string(h->pdim));
     }
     if (!du || !u || (h->pdim > 0 && !p)) return fail(ND_ERR_ARG, "nd_rhs: NULL buffer");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (h->batched.enabled) {
+        const BatchedNet& b = h->batched;
+        cudaError_t err = cudaSuccess;
+        if (b.ne > 0)
+            err = traced(h, kKernelBatchedEdges, s,
+                         [&] { return launch_batched(h->dtype, b, du, u, p, h->rhs_mode, s, kPhaseEdge); });
+        if (err == cudaSuccess)
+            err = traced(h, kKernelBatchedRows, s,
+                         [&] { return launch_batched(h->dtype, b, du, u, p, h->rhs_mode, s, kPhaseRow); });
+        return err == cudaSuccess ? ND_OK : cuda_fail(err, "nd_rhs kernel launch");
+    }
     RhsArgs a;
     a.du = du;
     a.u = u;
@@ -437,7 +542,6 @@ int nd_rhs(nd_handle* h, int dtype, void* du, int64_t n_du, const void* u, int64
     a.ybkt = el.ybkt;
     a.heavy_only = 0;
     a.heavy_separate = 0;
-    cudaStream_t s = (cudaStream_t)stream;
     const bool edge = el.enabled && h->edge_path;
     const bool split = h->topo.n_heavy > 0;  // heavy rows: their own kernel, on the side stream
     a.heavy_separate = split ? 1 : 0;
@@ -480,7 +584,7 @@ int nd_set_kernel_timing(nd_handle* h, int on) {
 int nd_kernel_times(nd_handle* h, int64_t* launches, double* ms, int n) {
     clear_error();
     if (!h || n < 0 || (n > 0 && (!launches || !ms))) return fail(ND_ERR_ARG, "nd_kernel_times: bad arguments");
-    double total[kKernelKinds] = {0, 0, 0, 0};
+    double total[kKernelKinds] = {};
     for (const Tracer::Mark& m : h->tracer.marks) {
         float t = 0.f;
         cudaError_t err = cudaEventSynchronize(m.stop);

@@ -111,26 +111,49 @@ __device__ __forceinline__ T incidence_term(T uv, T un, const T* __restrict__ pe
 
 template <int VK>
 struct VertexDims {
-    static constexpr int dim = VK == ND_V_SWING ? 2 : 1;
-    static constexpr int pdim = VK == ND_V_DIFFUSION ? 0 : (VK == ND_V_KURAMOTO ? 1 : 3);
+    static constexpr int dim = VK == ND_V_SWING || VK == ND_V_SWING_UNIT ? 2 : 1;
+    static constexpr int pdim = VK == ND_V_DIFFUSION ? 0 : (VK == ND_V_KURAMOTO || VK == ND_V_SWING_UNIT ? 1 : 3);
 };
 
-// Vertex f with the aggregated input `acc` (the reference's aggbuf entry).
+// Vertex f of the vertex whose states start at u[s] and parameters at p[q], with the
+// aggregated input `acc` (the reference's aggbuf entry).
+template <typename T, int VK>
+__device__ __forceinline__ void vertex_f_at(T* __restrict__ du, const T* __restrict__ u, const T* __restrict__ p,
+                                            int64_t s, int64_t q, T acc) {
+    using A = Arith<T>;
+    if constexpr (VK == ND_V_DIFFUSION) {
+        du[s] = acc;  // dv[1] = acc[1]
+    } else if constexpr (VK == ND_V_KURAMOTO) {
+        du[s] = A::add(__ldg(p + q), acc);  // dθ[1] = ω + esum[1]
+    } else if constexpr (VK == ND_V_SWING) {
+        const T w = u[s + 1];
+        const T M = __ldg(p + q), D = __ldg(p + q + 1), Pm = __ldg(p + q + 2);
+        du[s] = w;  // dv[1] = v[2]
+        // dv[2] = 1 / M * (Pm - D * v[2] + acc[1])
+        du[s + 1] = A::mul(A::div(T(1), M), A::add(A::sub(Pm, A::mul(D, w)), acc));
+    } else {
+        const T w = u[s + 1];
+        du[s] = w;  // dv[1] = v[2]
+        // dv[2] = P - 1.0 * v[2]; dv[2] += esum[1]   (1.0 * v[2] is v[2] exactly)
+        du[s + 1] = A::add(A::sub(__ldg(p + q), w), acc);
+    }
+}
+
+// Vertex f of vertex v of a homogeneous batch.
 template <typename T, int VK>
 __device__ __forceinline__ void vertex_f(T* __restrict__ du, const T* __restrict__ u,
                                          const T* __restrict__ pv, int64_t v, T acc) {
+    vertex_f_at<T, VK>(du, u, pv, v * VertexDims<VK>::dim, v * VertexDims<VK>::pdim, acc);
+}
+
+// ODE edge f of diffusion_dedge!: de1 = rate (sin(vs - vd) - e1), de2 = rate (sin(vd - vs) - e2)
+// with rate = 1 / τ (ND_E_DIFFUSION_ODE; Julia evaluates 1 / τ * x as (1 / τ) * x) or the
+// constant 100.0 (ND_E_DIFFUSION_ODE_FIXED).
+template <typename T>
+__device__ __forceinline__ void ode_edge_f(T rate, T vs, T vd, T e1, T e2, T& de1, T& de2) {
     using A = Arith<T>;
-    if constexpr (VK == ND_V_DIFFUSION) {
-        du[v] = acc;  // dv[1] = acc[1]
-    } else if constexpr (VK == ND_V_KURAMOTO) {
-        du[v] = A::add(__ldg(pv + v), acc);  // dθ[1] = ω + esum[1]
-    } else {
-        const T w = u[2 * v + 1];
-        const T M = __ldg(pv + 3 * v), D = __ldg(pv + 3 * v + 1), Pm = __ldg(pv + 3 * v + 2);
-        du[2 * v] = w;  // dv[1] = v[2]
-        // dv[2] = 1 / M * (Pm - D * v[2] + acc[1])
-        du[2 * v + 1] = A::mul(A::div(T(1), M), A::add(A::sub(Pm, A::mul(D, w)), acc));
-    }
+    de1 = A::mul(rate, A::sub(A::sin_phase(A::sub(vs, vd)), e1));
+    de2 = A::mul(rate, A::sub(A::sin_phase(A::sub(vd, vs)), e2));
 }
 
 }  // namespace nd

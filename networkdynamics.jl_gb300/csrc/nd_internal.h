@@ -32,9 +32,12 @@ struct __align__(8) Incidence {
 constexpr int32_t kSrcSideBit = int32_t(0x80000000u);
 
 // Dimensions of the library components.
-inline int vertex_dim(int vk) { return vk == ND_V_SWING ? 2 : 1; }
-inline int vertex_pdim(int vk) { return vk == ND_V_DIFFUSION ? 0 : (vk == ND_V_KURAMOTO ? 1 : 3); }
-inline int edge_pdim(int ek) { return ek == ND_E_DIFFUSION_UNIT ? 0 : 1; }
+inline int vertex_dim(int vk) { return vk == ND_V_SWING || vk == ND_V_SWING_UNIT ? 2 : 1; }
+inline int vertex_pdim(int vk) {
+    return vk == ND_V_DIFFUSION ? 0 : (vk == ND_V_KURAMOTO || vk == ND_V_SWING_UNIT ? 1 : 3);
+}
+inline int edge_dim(int ek) { return ek == ND_E_DIFFUSION_ODE || ek == ND_E_DIFFUSION_ODE_FIXED ? 2 : 0; }
+inline int edge_pdim(int ek) { return ek == ND_E_DIFFUSION_UNIT || ek == ND_E_DIFFUSION_ODE_FIXED ? 0 : 1; }
 
 // Degree buckets.  Rows with degree <= kMediumMaxDeg are processed in windows: a block
 // evaluates all edge terms of up to kWindow rows / kWindowIncidences incidences in
@@ -140,14 +143,64 @@ enum : int { kPhaseEdge = 1, kPhaseRow = 2, kPhaseBoth = 3 };
 cudaError_t launch_rhs_edge(int dtype, const RhsArgs& a, cudaStream_t stream, int phases = kPhaseBoth);
 
 // Kernel kinds that nd_rhs launches, for launch counting and optional per-kernel timing.
-enum KernelKind : int { kKernelEdgePhase = 0, kKernelRowPhase = 1, kKernelHeavyRows = 2, kKernelFused = 3, kKernelKinds = 4 };
+enum KernelKind : int {
+    kKernelEdgePhase = 0,
+    kKernelRowPhase = 1,
+    kKernelHeavyRows = 2,
+    kKernelFused = 3,
+    kKernelBatchedEdges = 4,
+    kKernelBatchedRows = 5,
+    kKernelKinds = 6
+};
+
+// ---- batched (heterogeneous) networks -------------------------------------------------------
+// Batch table of one component class (vertices or edges), passed to the kernels by value.
+// Components are numbered by "position": their rank in the reference's batch-major order;
+// batch b holds positions [pos0[b], pos0[b+1]), its states start at s0[b] with stride
+// dim(kind), its parameters at p0[b] with stride pdim(kind) (the BatchStride of
+// src/utils.jl:1-35).
+constexpr int kMaxBatches = ND_MAX_BATCHES;
+struct BatchTable {
+    int32_t n = 0;
+    int32_t kind[kMaxBatches] = {};
+    int32_t coupling[kMaxBatches] = {};
+    int64_t pos0[kMaxBatches + 1] = {};
+    int64_t s0[kMaxBatches] = {};
+    int64_t p0[kMaxBatches] = {};
+};
+
+// Device data of a batched network.  Edge values go to y2, two per edge position k:
+// y2[2k] = y_src, y2[2k+1] = y_dst -- the reference's output buffer for edges, which lays
+// out src then dst per edge (src/network_structure.jl:240-250).  Every row lists the y2
+// indices of its terms in ascending order, which is SequentialAggregator's order of
+// additions (src/aggregators.jl:140-151).
+struct BatchedNet {
+    bool enabled = false;
+    BatchTable vb, eb;                                 // host copies
+    BatchTable* d_vb = nullptr;                        // device copies, read by the kernels
+    BatchTable* d_eb = nullptr;
+    int64_t nv = 0, ne = 0, dim = 0, pdim = 0;
+    int32_t max_degree = 0;
+    int64_t n_warp_rows = 0;     // slots [0, n_warp_rows): degree > kLightMaxDeg, a warp per row
+    int2* eu = nullptr;          // [ne] by edge position: u indices of the src / dst vertex outputs
+    uint32_t* tptr = nullptr;    // [nv+1] by slot: range of the slot's terms in tidx
+    int32_t* tidx = nullptr;     // [2ne] y2 indices of every row's terms, ascending
+    int32_t* slot_vpos = nullptr;  // [nv] vertex position of each slot
+    void* y2 = nullptr;          // [2ne] scratch, element type of the handle
+};
+
+int check_edge_component(int edge_kind, int coupling);  // ND_OK or ND_ERR_UNSUPPORTED_COMPONENT
+int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out);
+void free_batched(BatchedNet* b);
+cudaError_t launch_batched(int dtype, const BatchedNet& b, void* du, const void* u, const void* p, int mode,
+                           cudaStream_t s, int phases);
 
 // Launch counter and CUDA-event timer for the kernels of one handle.  Timing is off by
 // default; when on, each launch is bracketed by two events on its stream, and
 // nd_kernel_times sums the bracketed durations.
 struct Tracer {
     bool timing = false;
-    int64_t launches[kKernelKinds] = {0, 0, 0, 0};
+    int64_t launches[kKernelKinds] = {};
     struct Mark {
         int kind;
         cudaEvent_t start, stop;
@@ -176,5 +229,6 @@ struct nd_handle {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int64_t dim, pdim;
     nd::Topology topo;
+    nd::BatchedNet batched;  // enabled: the handle is a batched network (topo unused)
     nd::Tracer tracer;
 };

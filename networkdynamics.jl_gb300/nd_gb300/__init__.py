@@ -6,8 +6,10 @@ top of it.
 """
 from . import _capi as capi
 from ._capi import ArgumentError, NDError, NotConvergedError, UnsupportedComponentError
-from .components import (EdgeModel, VertexModel, diffusion_edge, diffusion_edge_unit, diffusion_vertex,
-                         kuramoto_edge, kuramoto_first, kuramoto_second, static_line, swing_vertex)
+from .components import (AntiSymmetric, Directed, EdgeModel, Symmetric, VertexModel, diffusion_dedge, diffusion_edge,
+                         diffusion_edge_fid, diffusion_edge_unit, diffusion_odeedge, diffusion_vertex, kuramoto_edge,
+                         kuramoto_first, kuramoto_second, kuramoto_vertex_1d, kuramoto_vertex_2d, static_kuramoto_edge,
+                         static_line, swing_vertex)
 from .graphs import Graph, barabasi_albert, complete_graph, cycle_graph, random_geometric, simple_graph, watts_strogatz
 from .network import (ExecutionStyle, GB300Aggregator, GB300Execution, Network, adapt, get_aggr_constructor,
                       iscudacompatible, jvp)
@@ -16,8 +18,10 @@ from .mpnn import MPNN
 
 __all__ = [
     "capi", "ArgumentError", "NDError", "NotConvergedError", "UnsupportedComponentError",
-    "EdgeModel", "VertexModel", "diffusion_edge", "diffusion_edge_unit", "diffusion_vertex", "kuramoto_edge",
-    "kuramoto_first", "kuramoto_second", "static_line", "swing_vertex",
+    "AntiSymmetric", "Directed", "EdgeModel", "Symmetric", "VertexModel", "diffusion_dedge", "diffusion_edge",
+    "diffusion_edge_fid", "diffusion_edge_unit", "diffusion_odeedge", "diffusion_vertex", "kuramoto_edge",
+    "kuramoto_first", "kuramoto_second", "kuramoto_vertex_1d", "kuramoto_vertex_2d", "static_kuramoto_edge",
+    "static_line", "swing_vertex",
     "Graph", "barabasi_albert", "complete_graph", "cycle_graph", "random_geometric", "simple_graph",
     "watts_strogatz",
     "ExecutionStyle", "GB300Aggregator", "GB300Execution", "Network", "adapt", "get_aggr_constructor",

@@ -26,18 +26,28 @@ ND_F64 = 2
 ND_V_DIFFUSION = 1
 ND_V_KURAMOTO = 2
 ND_V_SWING = 3
+ND_V_SWING_UNIT = 4
 
 ND_E_DIFFUSION = 1
 ND_E_DIFFUSION_UNIT = 2
 ND_E_KURAMOTO = 3
+ND_E_DIFFUSION_ODE = 4
+ND_E_DIFFUSION_ODE_FIXED = 5
 
 ND_ANTISYMMETRIC = 1
+ND_SYMMETRIC = 2
+ND_DIRECTED = 3
+ND_FIDUCIAL = 4
+COUPLINGS = {"AntiSymmetric": ND_ANTISYMMETRIC, "Symmetric": ND_SYMMETRIC, "Directed": ND_DIRECTED,
+             "Fiducial": ND_FIDUCIAL}
+
+ND_MAX_BATCHES = 32
 
 ND_ORDER_SEQUENTIAL = 0
 ND_ORDER_TREE = 1
 ND_ORDER_SEQUENTIAL_HW = 2
 
-KERNEL_KINDS = ("edge_phase", "row_phase", "heavy_rows", "fused")
+KERNEL_KINDS = ("edge_phase", "row_phase", "heavy_rows", "fused", "batched_edges", "batched_rows")
 
 
 class NDError(RuntimeError):
@@ -71,7 +81,20 @@ class nd_info(C.Structure):
     _fields_ = [("dim", C.c_int64), ("pdim", C.c_int64), ("nv", C.c_int64), ("ne", C.c_int64),
                 ("n_incidences", C.c_int64), ("dtype", C.c_int32), ("vertex_kind", C.c_int32),
                 ("edge_kind", C.c_int32), ("max_degree", C.c_int32), ("n_hubs", C.c_int32),
-                ("sum_order", C.c_int32)]
+                ("sum_order", C.c_int32), ("n_vertex_batches", C.c_int32), ("n_edge_batches", C.c_int32)]
+
+
+class nd_batch(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("coupling", C.c_int32)]
+
+
+class nd_batched_network_desc(C.Structure):
+    _fields_ = [("nv", C.c_int64), ("ne", C.c_int64),
+                ("src", C.POINTER(C.c_int64)), ("dst", C.POINTER(C.c_int64)),
+                ("n_vertex_batches", C.c_int32), ("n_edge_batches", C.c_int32),
+                ("vertex_batches", C.POINTER(nd_batch)), ("edge_batches", C.POINTER(nd_batch)),
+                ("vertex_batch", C.POINTER(C.c_int32)), ("edge_batch", C.POINTER(C.c_int32)),
+                ("flags", C.c_int32), ("reserved", C.c_int32)]
 
 
 # Every symbol include/nd_gb300.h declares, with (restype, argtypes).
@@ -79,6 +102,7 @@ SIGNATURES = {
     "nd_version": (C.c_int, []),
     "nd_last_error": (C.c_char_p, []),
     "nd_create": (C.c_int, [C.POINTER(nd_network_desc), C.c_int, C.POINTER(C.c_void_p)]),
+    "nd_create_batched": (C.c_int, [C.POINTER(nd_batched_network_desc), C.c_int, C.POINTER(C.c_void_p)]),
     "nd_destroy": (C.c_int, [C.c_void_p]),
     "nd_get_info": (C.c_int, [C.c_void_p, C.POINTER(nd_info)]),
     "nd_set_sum_order": (C.c_int, [C.c_void_p, C.c_int]),

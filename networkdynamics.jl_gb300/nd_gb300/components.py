@@ -94,3 +94,61 @@ def static_line() -> EdgeModel:
     m = kuramoto_edge()
     m.name = "static_line"
     return m
+
+
+def diffusion_edge_fid() -> EdgeModel:
+    """diffusionedge_fid!: the two-sided g e_d = p (v_s - v_d), e_s = -e_d
+    (test/ComponentLibrary.jl:22-28)."""
+    return EdgeModel("diff_edge_fid", pdim=1, psym=("p",), pdef=(1.0,), kind=capi.ND_E_DIFFUSION,
+                     coupling="Fiducial")
+
+
+def diffusion_odeedge() -> EdgeModel:
+    """diffusion_dedge!: ODE edge with states (e_dst, e_src),
+    de1 = 1/τ (sin(v_s - v_d) - e1), de2 = 1/τ (sin(v_d - v_s) - e2), outputs
+    Fiducial(dst=1:1, src=2:2)   (test/ComponentLibrary.jl:30-40)."""
+    return EdgeModel("diff_edge_ode", pdim=1, psym=("τ",), pdef=(100.0,), kind=capi.ND_E_DIFFUSION_ODE,
+                     coupling="Fiducial", dim=2)
+
+
+def diffusion_dedge() -> EdgeModel:
+    """The benchmarks' ODE edge: de = 100.0 (sin(..) - e), no parameters
+    (benchmark/benchmark_models.jl:11-16)."""
+    return EdgeModel("diffusion_dedge", pdim=0, kind=capi.ND_E_DIFFUSION_ODE_FIXED, coupling="Fiducial", dim=2)
+
+
+def kuramoto_vertex_2d() -> VertexModel:
+    """The benchmarks' second-order Kuramoto vertex: dθ = ω, dω = P - 1.0 ω + Σ e
+    (benchmark/benchmark_models.jl:37-42)."""
+    return VertexModel("kuramoto_vertex_2d", dim=2, pdim=1, sym=("θ", "ω"), psym=("P",), pdef=(None,),
+                       kind=capi.ND_V_SWING_UNIT)
+
+
+kuramoto_vertex_1d = kuramoto_first           # benchmark/benchmark_models.jl:32-35
+static_kuramoto_edge = kuramoto_edge          # benchmark/benchmark_models.jl:27-30
+
+
+# --- output wrappers (src/component_functions.jl:101-203) -----------------------------------
+
+def _rewrap(m: EdgeModel, coupling: str) -> EdgeModel:
+    if m.kind is None or m.dim != 0 or m.coupling == "Fiducial":
+        raise capi.UnsupportedComponentError(
+            capi.ND_ERR_UNSUPPORTED_COMPONENT,
+            f"{coupling} wraps the single-sided g of a static library edge, not {m.name!r}")
+    return EdgeModel(f"{coupling}({m.name})", pdim=m.pdim, psym=m.psym, pdef=m.pdef, kind=m.kind,
+                     coupling=coupling)
+
+
+def AntiSymmetric(m: EdgeModel) -> EdgeModel:
+    """y_dst = g(...), y_src = -y_dst (src/component_functions.jl:117-126)."""
+    return _rewrap(m, "AntiSymmetric")
+
+
+def Symmetric(m: EdgeModel) -> EdgeModel:
+    """y_dst = g(...), y_src = y_dst (src/component_functions.jl:142-151)."""
+    return _rewrap(m, "Symmetric")
+
+
+def Directed(m: EdgeModel) -> EdgeModel:
+    """y_dst = g(...), no output for the source (y_src = 0) (src/component_functions.jl:167-175)."""
+    return _rewrap(m, "Directed")

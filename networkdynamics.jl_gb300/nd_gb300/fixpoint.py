@@ -23,8 +23,9 @@ def find_fixpoint(nw, p, x0=None, tol=1e-10, max_newton=50, max_cg=0):
     NetworkInitError) when Newton does not reach tol.  x0: initial state (its phases are
     used; ω is 0 at any steady state)."""
     import torch
-    if nw.vertexm.kind != capi.ND_V_SWING:
-        raise capi.ArgumentError(capi.ND_ERR_ARG, "find_fixpoint on the GPU supports swing (kuramoto_second) vertices")
+    if nw.vertexm is None or nw.edgem is None or nw.vertexm.kind != capi.ND_V_SWING:
+        raise capi.ArgumentError(capi.ND_ERR_ARG,
+                                 "find_fixpoint on the GPU supports homogeneous swing (kuramoto_second) networks")
     ens = Ensemble([nw.graph], kuramoto_second(), nw.edgem, torch.float64)
     pt = torch.as_tensor(np.asarray(p.cpu() if isinstance(p, torch.Tensor) else p, dtype=np.float64)).cuda()
     if pt.numel() != ens.pdim:

@@ -73,25 +73,43 @@ def _dtype_code(dtype) -> int:
                              f"Use adapt on Network with either float32 or float64, got {dtype}")
 
 
-def _single_kind(models, what):
-    kinds = {m.kind for m in models}
-    if None in kinds:
-        bad = next(m for m in models if m.kind is None)
+def _check_library(models, what):
+    bad = next((m for m in models if m.kind is None), None)
+    if bad is not None:
         raise capi.UnsupportedComponentError(
             capi.ND_ERR_UNSUPPORTED_COMPONENT,
             f"{what} model {bad.name!r} is not in the GB300 component library; "
             "GB300Execution has no CPU fallback")
-    if len(kinds) != 1:
-        raise capi.UnsupportedComponentError(
-            capi.ND_ERR_UNSUPPORTED_COMPONENT,
-            f"GB300Execution needs one homogeneous {what} batch, got {len(kinds)} different {what} models")
-    return models[0]
+
+
+def _batches(models, key):
+    """Batches of identical components in order of first appearance, as find_identical
+    groups them (src/utils.jl:197-216, src/construction.jl:155-168): the model of every
+    batch and the batch index of every component."""
+    keys, reps = [], []
+    ids = np.empty(len(models), dtype=np.int32)
+    for i, m in enumerate(models):
+        k = key(m)
+        try:
+            b = keys.index(k)
+        except ValueError:
+            keys.append(k)
+            reps.append(m)
+            b = len(keys) - 1
+        ids[i] = b
+    if len(reps) > capi.ND_MAX_BATCHES:
+        raise capi.UnsupportedComponentError(capi.ND_ERR_UNSUPPORTED_COMPONENT,
+                                             f"more than {capi.ND_MAX_BATCHES} different components")
+    return reps, ids
 
 
 class Network:
-    """A network of library components on a graph, in the reference's flat layout:
-    u = [vertex states in vertex order], p = [vertex parameters in vertex order,
-    edge parameters in edges(g) order] (src/network_structure.jl:224-258)."""
+    """A network of library components on a graph, in the reference's flat layout
+    (src/network_structure.jl:224-258): u = [vertex states batch by batch, edge states
+    batch by batch], p = [vertex parameters batch by batch, edge parameters batch by
+    batch]; components are batched by identity in order of first appearance, ascending
+    index inside a batch.  With one vertex and one edge model that is vertex order and
+    edges(g) order."""
 
     def __init__(self, g: Graph, vertexm: Union[VertexModel, Sequence[VertexModel]],
                  edgem: Union[EdgeModel, Sequence[EdgeModel]], execution: ExecutionStyle = None,
@@ -110,20 +128,45 @@ class Network:
         if not ems:
             raise capi.ArgumentError(capi.ND_ERR_ARG,
                                      "a graph without edges needs the edge model passed as a single EdgeModel")
+        _check_library(vms, "vertex")
+        _check_library(ems, "edge")
+        for m in ems:
+            if m.coupling not in capi.COUPLINGS:
+                raise capi.UnsupportedComponentError(capi.ND_ERR_UNSUPPORTED_COMPONENT,
+                                                     f"unknown edge output wrapper {m.coupling!r}")
         self.graph = g
-        self.vertexm = _single_kind(vms, "vertex")
-        self.edgem = _single_kind(ems, "edge")
-        if self.edgem.coupling != "AntiSymmetric":
-            raise capi.UnsupportedComponentError(capi.ND_ERR_UNSUPPORTED_COMPONENT,
-                                                 "only AntiSymmetric edges are in the GB300 library")
+        if isinstance(vertexm, VertexModel):
+            self.vertex_batches, self.vertex_batch = [vertexm], np.zeros(g.nv, dtype=np.int32)
+        else:
+            self.vertex_batches, self.vertex_batch = _batches(vms, lambda m: m.kind)
+        if isinstance(edgem, EdgeModel):
+            self.edge_batches, self.edge_batch = [edgem], np.zeros(g.ne, dtype=np.int32)
+        else:
+            self.edge_batches, self.edge_batch = _batches(ems, lambda m: (m.kind, m.coupling))
+        # the single model of a one-batch network (None when there are several)
+        self.vertexm = self.vertex_batches[0] if len(self.vertex_batches) == 1 else None
+        self.edgem = self.edge_batches[0] if len(self.edge_batches) == 1 else None
         self.execution = execution
         self.aggregator = aggregator
-        self.dim = g.nv * self.vertexm.dim
-        self.pdim = g.nv * self.vertexm.pdim + g.ne * self.edgem.pdim
+        self._layout()
         self._handle = None
         self._dtype = None
         if dtype is not None:
             self._create(dtype)
+
+    def _layout(self):
+        """First state / parameter index of every component (register_vertices! /
+        register_edges!, src/network_structure.jl:224-258)."""
+        def place(batch, models, attr, start):
+            order = np.argsort(batch, kind="stable")
+            size = np.array([getattr(m, attr) for m in models], dtype=np.int64)[batch[order]]
+            first = np.empty(len(batch), dtype=np.int64)
+            first[order] = start + np.cumsum(size) - size
+            return first, start + int(size.sum())
+        self.v_data, nstate = place(self.vertex_batch, self.vertex_batches, "dim", 0)
+        self.e_data, self.dim = place(self.edge_batch, self.edge_batches, "dim", nstate)
+        self.v_para, npar = place(self.vertex_batch, self.vertex_batches, "pdim", 0)
+        self.e_para, self.pdim = place(self.edge_batch, self.edge_batches, "pdim", npar)
 
     # --- layout helpers -------------------------------------------------------------------
     @property
@@ -134,30 +177,38 @@ class Network:
     def ne(self) -> int:
         return self.graph.ne
 
+    @property
+    def homogeneous(self) -> bool:
+        return len(self.vertex_batches) == 1 and len(self.edge_batches) == 1
+
     def vertex_state_index(self, v: int, k: int = 0) -> int:
-        return v * self.vertexm.dim + k
+        return int(self.v_data[v]) + k
+
+    def edge_state_index(self, e: int, k: int = 0) -> int:
+        return int(self.e_data[e]) + k
 
     def vertex_param_index(self, v: int, k: int = 0) -> int:
-        return v * self.vertexm.pdim + k
+        return int(self.v_para[v]) + k
 
     def edge_param_index(self, e: int, k: int = 0) -> int:
-        return self.nv * self.vertexm.pdim + e * self.edgem.pdim + k
+        return int(self.e_para[e]) + k
 
     def pflat(self, vertex: dict | None = None, edge: dict | None = None) -> np.ndarray:
-        """Flat parameter vector from per-symbol arrays (defaults where omitted)."""
+        """Flat parameter vector from per-symbol values (defaults where omitted).  A value
+        is a scalar or an array over all vertices (edges), read at the components that
+        have the symbol."""
         p = np.zeros(self.pdim, dtype=np.float64)
-        vp = self.vertexm.pdim
-        for k, name in enumerate(self.vertexm.psym):
-            val = (vertex or {}).get(name, self.vertexm.pdef[k] if k < len(self.vertexm.pdef) else None)
-            if val is None:
-                raise capi.ArgumentError(capi.ND_ERR_ARG, f"vertex parameter {name} has no default")
-            p[k:self.nv * vp:vp] = val
-        ep, off = self.edgem.pdim, self.nv * vp
-        for k, name in enumerate(self.edgem.psym):
-            val = (edge or {}).get(name, self.edgem.pdef[k] if k < len(self.edgem.pdef) else None)
-            if val is None:
-                raise capi.ArgumentError(capi.ND_ERR_ARG, f"edge parameter {name} has no default")
-            p[off + k:off + self.ne * ep:ep] = val
+        for models, batch, first, given, what in (
+                (self.vertex_batches, self.vertex_batch, self.v_para, vertex or {}, "vertex"),
+                (self.edge_batches, self.edge_batch, self.e_para, edge or {}, "edge")):
+            for b, m in enumerate(models):
+                idx = np.flatnonzero(batch == b)
+                for k, name in enumerate(m.psym):
+                    val = given.get(name, m.pdef[k] if k < len(m.pdef) else None)
+                    if val is None:
+                        raise capi.ArgumentError(capi.ND_ERR_ARG, f"{what} parameter {name} has no default")
+                    val = np.asarray(val, dtype=np.float64)
+                    p[first[idx] + k] = val if val.ndim == 0 else val[idx]
         return p
 
     # --- device handle -------------------------------------------------------------------
@@ -168,10 +219,23 @@ class Network:
         src = np.ascontiguousarray(g.src, dtype=np.int64)
         dst = np.ascontiguousarray(g.dst, dtype=np.int64)
         P = C.POINTER(C.c_int64)
-        desc = capi.nd_network_desc(g.nv, g.ne, src.ctypes.data_as(P), dst.ctypes.data_as(P),
-                                    self.vertexm.kind, self.edgem.kind, capi.ND_ANTISYMMETRIC, 0)
         h = C.c_void_p()
-        capi.check(lib.nd_create(C.byref(desc), code, C.byref(h)))
+        if self.homogeneous:
+            vm, em = self.vertex_batches[0], self.edge_batches[0]
+            desc = capi.nd_network_desc(g.nv, g.ne, src.ctypes.data_as(P), dst.ctypes.data_as(P), vm.kind, em.kind,
+                                        capi.COUPLINGS[em.coupling], 0)
+            capi.check(lib.nd_create(C.byref(desc), code, C.byref(h)))
+        else:
+            vb = (capi.nd_batch * len(self.vertex_batches))(*[(m.kind, 0) for m in self.vertex_batches])
+            eb = (capi.nd_batch * len(self.edge_batches))(
+                *[(m.kind, capi.COUPLINGS[m.coupling]) for m in self.edge_batches])
+            vbi = np.ascontiguousarray(self.vertex_batch, dtype=np.int32)
+            ebi = np.ascontiguousarray(self.edge_batch, dtype=np.int32)
+            P32 = C.POINTER(C.c_int32)
+            desc = capi.nd_batched_network_desc(g.nv, g.ne, src.ctypes.data_as(P), dst.ctypes.data_as(P),
+                                                len(self.vertex_batches), len(self.edge_batches), vb, eb,
+                                                vbi.ctypes.data_as(P32), ebi.ctypes.data_as(P32), 0, 0)
+            capi.check(lib.nd_create_batched(C.byref(desc), code, C.byref(h)))
         self._handle = h
         self._dtype = code
         self._lib = lib

@@ -14,7 +14,7 @@
  *                          controller, driving the sequential RHS
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline load this library,
- * as the checker.  Compile with -ffp-contract=off: the reference performs no fused
+ * to check the GPU results against.  Compile with -ffp-contract=off: the reference performs no fused
  * multiply-adds in these functions, so neither may the restatement.
  */
 #include <math.h>
@@ -25,13 +25,16 @@
 #include <omp.h>
 #endif
 
-/* Component kinds: same numbering as the C ABI of the GB300 library. */
-enum { V_DIFFUSION = 1, V_KURAMOTO = 2, V_SWING = 3 };
-enum { E_DIFFUSION = 1, E_DIFFUSION_UNIT = 2, E_KURAMOTO = 3 };
+/* Component kinds and output wrappers: same numbering as the C ABI of the GB300 library. */
+enum { V_DIFFUSION = 1, V_KURAMOTO = 2, V_SWING = 3, V_SWING_UNIT = 4 };
+enum { E_DIFFUSION = 1, E_DIFFUSION_UNIT = 2, E_KURAMOTO = 3, E_DIFFUSION_ODE = 4, E_DIFFUSION_ODE_FIXED = 5 };
+enum { C_ANTISYMMETRIC = 1, C_SYMMETRIC = 2, C_DIRECTED = 3, C_FIDUCIAL = 4 };
 
-static int vdim(int vk) { return vk == V_SWING ? 2 : 1; }
-static int vpdim(int vk) { return vk == V_DIFFUSION ? 0 : (vk == V_KURAMOTO ? 1 : 3); }
-static int epdim(int ek) { return ek == E_DIFFUSION_UNIT ? 0 : 1; }
+static int vdim(int vk) { return vk == V_SWING || vk == V_SWING_UNIT ? 2 : 1; }
+static int vpdim(int vk) { return vk == V_DIFFUSION ? 0 : (vk == V_KURAMOTO || vk == V_SWING_UNIT ? 1 : 3); }
+static int is_ode_edge(int ek) { return ek == E_DIFFUSION_ODE || ek == E_DIFFUSION_ODE_FIXED; }
+static int edim(int ek) { return is_ode_edge(ek) ? 2 : 0; }
+static int epdim(int ek) { return ek == E_DIFFUSION_UNIT || ek == E_DIFFUSION_ODE_FIXED ? 0 : 1; }
 
 /*
  * Index layout of src/network_structure.jl:224-289, built as src/construction.jl:155-195
@@ -44,10 +47,12 @@ typedef struct {
     int64_t nv, ne;
     const int64_t* src;
     const int64_t* dst;
-    const int32_t* vkind; /* [nv] */
-    const int32_t* ekind; /* [ne] */
+    int32_t* vkind; /* [nv] kind of every vertex */
+    int32_t* ekind; /* [ne] kind of every edge */
+    int32_t* ecoup; /* [ne] output wrapper of every edge */
     /* layout, 0-based offsets */
     int64_t* v_data; /* first state index of vertex */
+    int64_t* e_data; /* first state index of edge (ODE edges) */
     int64_t* v_out;  /* output index */
     int64_t* v_para; /* first parameter index */
     int64_t* v_aggr; /* aggregation index */
@@ -64,44 +69,50 @@ typedef struct {
     int64_t* inv_idx;
 } layout_t;
 
-/* Batch order: kinds in order of first appearance, indices ascending inside a batch. */
-static void batch_order(int64_t n, const int32_t* kind, int64_t* order) {
-    int32_t seen[16];
-    int nseen = 0;
-    for (int64_t i = 0; i < n; ++i) {
-        int found = 0;
-        for (int j = 0; j < nseen; ++j)
-            if (seen[j] == kind[i]) found = 1;
-        if (!found && nseen < 16) seen[nseen++] = kind[i];
-    }
+/* Batch order: batches in index order, components ascending inside a batch. */
+static void batch_order(int64_t n, const int32_t* batch, int nb, int64_t* order) {
     int64_t pos = 0;
-    for (int j = 0; j < nseen; ++j)
+    for (int b = 0; b < nb; ++b)
         for (int64_t i = 0; i < n; ++i)
-            if (kind[i] == seen[j]) order[pos++] = i;
+            if (batch[i] == b) order[pos++] = i;
 }
 
 void nd_oracle_layout_free(layout_t* L);
 
-layout_t* nd_oracle_layout_new(int64_t nv, int64_t ne, const int64_t* src, const int64_t* dst,
-                               const int32_t* vkind, const int32_t* ekind) {
+/* Layout of a network whose batches are given explicitly: vertex v belongs to vertex batch
+ * vbatch[v] of kind vb_kind[.], edge e to edge batch ebatch[e] of kind eb_kind[.] and
+ * wrapper eb_coup[.].  The batches are laid out in index order, which is the reference's
+ * order of first appearance when the caller numbers them that way. */
+layout_t* nd_oracle_layout_new_batched(int64_t nv, int64_t ne, const int64_t* src, const int64_t* dst,
+                                       int nvb, const int32_t* vb_kind, const int32_t* vbatch, int neb,
+                                       const int32_t* eb_kind, const int32_t* eb_coup, const int32_t* ebatch) {
     layout_t* L = (layout_t*)calloc(1, sizeof(layout_t));
     L->nv = nv;
     L->ne = ne;
     L->src = src;
     L->dst = dst;
-    L->vkind = vkind;
-    L->ekind = ekind;
+    L->vkind = (int32_t*)malloc(sizeof(int32_t) * (nv + 1));
+    L->ekind = (int32_t*)malloc(sizeof(int32_t) * (ne + 1));
+    L->ecoup = (int32_t*)malloc(sizeof(int32_t) * (ne + 1));
+    for (int64_t v = 0; v < nv; ++v) L->vkind[v] = vb_kind[vbatch[v]];
+    for (int64_t e = 0; e < ne; ++e) {
+        L->ekind[e] = eb_kind[ebatch[e]];
+        L->ecoup[e] = eb_coup[ebatch[e]];
+    }
     L->v_data = (int64_t*)malloc(sizeof(int64_t) * (nv + 1));
     L->v_out = (int64_t*)malloc(sizeof(int64_t) * (nv + 1));
     L->v_para = (int64_t*)malloc(sizeof(int64_t) * (nv + 1));
     L->v_aggr = (int64_t*)malloc(sizeof(int64_t) * (nv + 1));
+    L->e_data = (int64_t*)malloc(sizeof(int64_t) * (ne + 1));
     L->e_out_src = (int64_t*)malloc(sizeof(int64_t) * (ne + 1));
     L->e_out_dst = (int64_t*)malloc(sizeof(int64_t) * (ne + 1));
     L->e_para = (int64_t*)malloc(sizeof(int64_t) * (ne + 1));
     L->vbatch_order = (int64_t*)malloc(sizeof(int64_t) * (nv + 1));
     L->ebatch_order = (int64_t*)malloc(sizeof(int64_t) * (ne + 1));
-    batch_order(nv, vkind, L->vbatch_order);
-    batch_order(ne, ekind, L->ebatch_order);
+    batch_order(nv, vbatch, nvb, L->vbatch_order);
+    batch_order(ne, ebatch, neb, L->ebatch_order);
+    const int32_t* vkind = L->vkind;
+    const int32_t* ekind = L->ekind;
     int64_t dyn = 0, out = 0, par = 0, agg = 0;
     for (int64_t k = 0; k < nv; ++k) { /* register_vertices! */
         int64_t v = L->vbatch_order[k];
@@ -114,8 +125,10 @@ layout_t* nd_oracle_layout_new(int64_t nv, int64_t ne, const int64_t* src, const
         L->v_aggr[v] = agg;
         agg += 1;
     }
-    for (int64_t k = 0; k < ne; ++k) { /* register_edges!: static edges have no states */
+    for (int64_t k = 0; k < ne; ++k) { /* register_edges!: states after every vertex state */
         int64_t e = L->ebatch_order[k];
+        L->e_data[e] = dyn;
+        dyn += edim(ekind[e]);
         L->e_out_src[e] = out;
         out += 1;
         L->e_out_dst[e] = out;
@@ -171,8 +184,41 @@ layout_t* nd_oracle_layout_new(int64_t nv, int64_t ne, const int64_t* src, const
     return L;
 }
 
+/* Layout from per-component kinds: one batch per kind in order of first appearance
+ * (find_identical over identical components), every edge AntiSymmetric. */
+layout_t* nd_oracle_layout_new(int64_t nv, int64_t ne, const int64_t* src, const int64_t* dst,
+                               const int32_t* vkind, const int32_t* ekind) {
+    int32_t vk[16], ek[16], ec[16];
+    int nvb = 0, neb = 0;
+    int32_t* vb = (int32_t*)malloc(sizeof(int32_t) * (nv + 1));
+    int32_t* eb = (int32_t*)malloc(sizeof(int32_t) * (ne + 1));
+    for (int64_t v = 0; v < nv; ++v) {
+        int b = 0;
+        while (b < nvb && vk[b] != vkind[v]) ++b;
+        if (b == nvb && nvb < 16) vk[nvb++] = vkind[v];
+        vb[v] = b;
+    }
+    for (int64_t e = 0; e < ne; ++e) {
+        int b = 0;
+        while (b < neb && ek[b] != ekind[e]) ++b;
+        if (b == neb && neb < 16) {
+            ek[neb] = ekind[e];
+            ec[neb++] = C_ANTISYMMETRIC;
+        }
+        eb[e] = b;
+    }
+    layout_t* L = nd_oracle_layout_new_batched(nv, ne, src, dst, nvb, vk, vb, neb, ek, ec, eb);
+    free(vb);
+    free(eb);
+    return L;
+}
+
 void nd_oracle_layout_free(layout_t* L) {
     if (!L) return;
+    free(L->vkind);
+    free(L->ekind);
+    free(L->ecoup);
+    free(L->e_data);
     free(L->v_data);
     free(L->v_out);
     free(L->v_para);
@@ -193,19 +239,29 @@ int64_t nd_oracle_pdim(const layout_t* L) { return L->lastidx_p; }
 int64_t nd_oracle_v_data(const layout_t* L, int64_t v) { return L->v_data[v]; }
 int64_t nd_oracle_v_para(const layout_t* L, int64_t v) { return L->v_para[v]; }
 int64_t nd_oracle_e_para(const layout_t* L, int64_t e) { return L->e_para[e]; }
+int64_t nd_oracle_e_data(const layout_t* L, int64_t e) { return L->e_data[e]; }
 
 /*
  * The RHS, once per precision.  Steps and line references follow src/coreloop.jl.
  * Workspace o (lastidx_out) and aggbuf (lastidx_aggr) are caller-provided.
  *
- * Component functions (test/ComponentLibrary.jl):
+ * Component functions (test/ComponentLibrary.jl, benchmark/benchmark_models.jl):
  *   diffusionedge!   e = p * (v_s - v_d)                 :8-13
  *   diffusion_edge!  e = v_s - v_d                       test/diffusion_test.jl:57-60
  *   kuramoto_edge!   e = K * sin(θ_s - θ_d)              :51-57
- *   AntiSymmetric    y_src = -y_dst                      src/component_functions.jl:117-127
+ *   diffusion_dedge! de1 = 1/τ * (sin(v_s - v_d) - e1), de2 = 1/τ * (sin(v_d - v_s) - e2)
+ *                    with outputs Fiducial(dst=1:1, src=2:2)   :30-40; the benchmark
+ *                    variant has 100.0 in place of 1/τ (benchmark_models.jl:11-16)
+ *   AntiSymmetric    y_src = -y_dst                      src/component_functions.jl:117-126
+ *   Symmetric        y_src = y_dst                       :142-151
+ *   Directed         y_src = 0                           :167-175
+ *   diffusionedge_fid! (two-sided)  e_d = p * (v_s - v_d), e_s = -e_d   :22-28
  *   diffusionvertex! dv = acc                            :42-46
  *   kuramoto_vertex! dθ = ω + esum                       :69-72
  *   kuramoto_inertia! dv1 = v2; dv2 = 1/M*(Pm - D*v2 + acc)  :59-67
+ *   kuramoto_inertia! (benchmarks) dv1 = v2; dv2 = P - 1.0*v2; dv2 += esum
+ *                    benchmark_models.jl:37-42 (the literal 1.0 is a Float64, so for
+ *                    Float32 data P - 1.0*v2 is computed in double and rounded on store)
  */
 #define DEFINE_ORACLE_RHS(T, SFX, SIN)                                                              \
     static inline T edge_g_##SFX(int ek, T vs, T vd, const T* pe) {                                \
@@ -218,18 +274,49 @@ int64_t nd_oracle_e_para(const layout_t* L, int64_t e) { return L->e_para[e]; }
             du[0] = acc;                                                                            \
         } else if (vk == V_KURAMOTO) {                                                              \
             du[0] = pv[0] + acc;                                                                    \
-        } else {                                                                                    \
+        } else if (vk == V_SWING) {                                                                 \
             T M = pv[0], D = pv[1], Pm = pv[2];                                                     \
             du[0] = u[1];                                                                           \
             du[1] = (T)1 / M * (Pm - D * u[1] + acc);                                               \
+        } else {                                                                                    \
+            du[0] = u[1];                                                                           \
+            du[1] = (T)((double)pv[0] - 1.0 * (double)u[1]);                                       \
+            du[1] = du[1] + acc;                                                                    \
         }                                                                                           \
     }                                                                                               \
-    static void edges_g_##SFX(const layout_t* L, T* o, const T* p, int64_t k) {                    \
+    /* edge g: ODE edges map their states (PureStateMap, :41), static edges evaluate g */         \
+    /* on the vertex outputs (PureFeedForward, :76-78) and apply their wrapper */                   \
+    static void edges_g_##SFX(const layout_t* L, T* o, const T* u, const T* p, int64_t k) {        \
         int64_t e = L->ebatch_order[k];                                                             \
+        int ek = L->ekind[e];                                                                       \
+        if (is_ode_edge(ek)) {                                                                      \
+            o[L->e_out_dst[e]] = u[L->e_data[e]];                                                   \
+            o[L->e_out_src[e]] = u[L->e_data[e] + 1];                                               \
+            return;                                                                                 \
+        }                                                                                           \
         T vs = o[L->v_out[L->src[e]]], vd = o[L->v_out[L->dst[e]]];                                 \
-        T y = edge_g_##SFX(L->ekind[e], vs, vd, p + L->e_para[e]);                                  \
+        T y = edge_g_##SFX(ek, vs, vd, p + L->e_para[e]);                                           \
         o[L->e_out_dst[e]] = y;                                                                     \
-        o[L->e_out_src[e]] = -y;                                                                    \
+        int c = L->ecoup[e];                                                                        \
+        o[L->e_out_src[e]] = c == C_SYMMETRIC ? y : (c == C_DIRECTED ? (T)0 : -y);                  \
+    }                                                                                               \
+    /* edge f of the ODE edges (:71) */                                                             \
+    static void edges_f_##SFX(const layout_t* L, T* du, const T* u, const T* o, const T* p,         \
+                              int64_t k) {                                                          \
+        int64_t e = L->ebatch_order[k];                                                             \
+        int ek = L->ekind[e];                                                                       \
+        if (!is_ode_edge(ek)) return;                                                               \
+        T vs = o[L->v_out[L->src[e]]], vd = o[L->v_out[L->dst[e]]];                                 \
+        const T* x = u + L->e_data[e];                                                              \
+        T* dx = du + L->e_data[e];                                                                  \
+        if (ek == E_DIFFUSION_ODE) {                                                                \
+            T tau = p[L->e_para[e]];                                                                \
+            dx[0] = (T)1 / tau * (SIN(vs - vd) - x[0]);                                             \
+            dx[1] = (T)1 / tau * (SIN(vd - vs) - x[1]);                                             \
+        } else {                                                                                    \
+            dx[0] = (T)100.0 * (SIN(vs - vd) - x[0]);                                               \
+            dx[1] = (T)100.0 * (SIN(vd - vs) - x[1]);                                               \
+        }                                                                                           \
     }                                                                                               \
     void nd_oracle_rhs_##SFX(const layout_t* L, T* du, const T* u, const T* p, T* o, T* aggbuf) {   \
         int64_t i;                                                                                  \
@@ -240,8 +327,8 @@ int64_t nd_oracle_e_para(const layout_t* L, int64_t e) { return L->e_para[e]; }
             int64_t v = L->vbatch_order[k];                                                         \
             o[L->v_out[v]] = u[L->v_data[v]];                                                       \
         }                                                                                           \
-        /* static edges are PureFeedForward: g with f&g pass, :76-78; lazy gather :67 */            \
-        for (int64_t k = 0; k < L->ne; ++k) edges_g_##SFX(L, o, p, k);                              \
+        for (int64_t k = 0; k < L->ne; ++k) edges_g_##SFX(L, o, u, p, k);                           \
+        for (int64_t k = 0; k < L->ne; ++k) edges_f_##SFX(L, du, u, o, p, k);                       \
         /* SequentialAggregator: walk the tightened output range in index order :90 */              \
         for (int64_t j = 0; j < L->agg_len; ++j) {                                                  \
             int64_t m = L->agg_map[j];                                                              \
@@ -263,7 +350,9 @@ int64_t nd_oracle_e_para(const layout_t* L, int64_t e) { return L->e_para[e]; }
             o[L->v_out[v]] = u[L->v_data[v]];                                                       \
         }                                                                                           \
         _Pragma("omp parallel for schedule(static)") for (i = 0; i < L->ne; ++i)                   \
-            edges_g_##SFX(L, o, p, i);                                                              \
+            edges_g_##SFX(L, o, u, p, i);                                                           \
+        _Pragma("omp parallel for schedule(static)") for (i = 0; i < L->ne; ++i)                   \
+            edges_f_##SFX(L, du, u, o, p, i);                                                       \
         _Pragma("omp parallel for schedule(static)") for (i = 0; i < L->lastidx_aggr; ++i) {       \
             T acc = aggbuf[i];                                                                      \
             for (int64_t q = L->inv_ptr[i]; q < L->inv_ptr[i + 1]; ++q) acc = acc + o[L->inv_idx[q]]; \

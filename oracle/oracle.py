@@ -27,12 +27,14 @@ SRC = HERE / "nd_oracle.c"
 BUILD_DIR = HERE / "_build"
 LIB = BUILD_DIR / "liboracle.so"
 
-V_DIFFUSION, V_KURAMOTO, V_SWING = 1, 2, 3
-E_DIFFUSION, E_DIFFUSION_UNIT, E_KURAMOTO = 1, 2, 3
+V_DIFFUSION, V_KURAMOTO, V_SWING, V_SWING_UNIT = 1, 2, 3, 4
+E_DIFFUSION, E_DIFFUSION_UNIT, E_KURAMOTO, E_DIFFUSION_ODE, E_DIFFUSION_ODE_FIXED = 1, 2, 3, 4, 5
+C_ANTISYMMETRIC, C_SYMMETRIC, C_DIRECTED, C_FIDUCIAL = 1, 2, 3, 4
 
-VDIM = {V_DIFFUSION: 1, V_KURAMOTO: 1, V_SWING: 2}
-VPDIM = {V_DIFFUSION: 0, V_KURAMOTO: 1, V_SWING: 3}
-EPDIM = {E_DIFFUSION: 1, E_DIFFUSION_UNIT: 0, E_KURAMOTO: 1}
+VDIM = {V_DIFFUSION: 1, V_KURAMOTO: 1, V_SWING: 2, V_SWING_UNIT: 2}
+VPDIM = {V_DIFFUSION: 0, V_KURAMOTO: 1, V_SWING: 3, V_SWING_UNIT: 1}
+EDIM = {E_DIFFUSION: 0, E_DIFFUSION_UNIT: 0, E_KURAMOTO: 0, E_DIFFUSION_ODE: 2, E_DIFFUSION_ODE_FIXED: 2}
+EPDIM = {E_DIFFUSION: 1, E_DIFFUSION_UNIT: 0, E_KURAMOTO: 1, E_DIFFUSION_ODE: 1, E_DIFFUSION_ODE_FIXED: 0}
 
 
 def build_oracle(force: bool = False) -> Path:
@@ -68,11 +70,13 @@ def load():
         P32 = C.POINTER(C.c_int32)
         lib.nd_oracle_layout_new.restype = vp
         lib.nd_oracle_layout_new.argtypes = [i64, i64, P64, P64, P32, P32]
+        lib.nd_oracle_layout_new_batched.restype = vp
+        lib.nd_oracle_layout_new_batched.argtypes = [i64, i64, P64, P64, C.c_int, P32, P32, C.c_int, P32, P32, P32]
         lib.nd_oracle_layout_free.argtypes = [vp]
         for fn in ("nd_oracle_dim", "nd_oracle_pdim"):
             getattr(lib, fn).restype = i64
             getattr(lib, fn).argtypes = [vp]
-        for fn in ("nd_oracle_v_data", "nd_oracle_v_para", "nd_oracle_e_para"):
+        for fn in ("nd_oracle_v_data", "nd_oracle_v_para", "nd_oracle_e_para", "nd_oracle_e_data"):
             getattr(lib, fn).restype = i64
             getattr(lib, fn).argtypes = [vp, i64]
         for fn in ("nd_oracle_rhs_f64", "nd_oracle_rhs_f32", "nd_oracle_rhs_poly_f64", "nd_oracle_rhs_poly_f32"):
@@ -125,6 +129,36 @@ class OracleNetwork:
     @classmethod
     def from_graph(cls, g, vkind, ekind):
         return cls(g.nv, g.src, g.dst, vkind, ekind)
+
+    @classmethod
+    def from_batches(cls, nv, src, dst, vertex_batches, vertex_batch, edge_batches, edge_batch):
+        """Network with explicit batches (the reference's order of first appearance):
+        ``vertex_batches`` lists the vertex kind of every batch, ``edge_batches`` the
+        (edge kind, coupling) of every batch; ``vertex_batch`` / ``edge_batch`` give each
+        component's batch."""
+        self = cls.__new__(cls)
+        self.lib = load()
+        self.nv = int(nv)
+        self.src = np.ascontiguousarray(src, dtype=np.int64)
+        self.dst = np.ascontiguousarray(dst, dtype=np.int64)
+        self.ne = int(self.src.shape[0])
+        vbk = np.ascontiguousarray(vertex_batches, dtype=np.int32)
+        ebk = np.ascontiguousarray([k for k, _ in edge_batches] or [0], dtype=np.int32)
+        ebc = np.ascontiguousarray([c for _, c in edge_batches] or [0], dtype=np.int32)
+        vb = np.ascontiguousarray(vertex_batch, dtype=np.int32)
+        eb = np.ascontiguousarray(edge_batch if self.ne else np.zeros(1), dtype=np.int32)
+        self.vkind = vbk[vb]
+        self.ekind = ebk[eb[:self.ne]] if self.ne else np.zeros(0, dtype=np.int32)
+        P64 = C.POINTER(C.c_int64)
+        P32 = C.POINTER(C.c_int32)
+        self.L = self.lib.nd_oracle_layout_new_batched(
+            self.nv, self.ne, self.src.ctypes.data_as(P64), self.dst.ctypes.data_as(P64), len(vbk),
+            vbk.ctypes.data_as(P32), vb.ctypes.data_as(P32), len(edge_batches), ebk.ctypes.data_as(P32),
+            ebc.ctypes.data_as(P32), eb.ctypes.data_as(P32))
+        self.dim = int(self.lib.nd_oracle_dim(self.L))
+        self.pdim = int(self.lib.nd_oracle_pdim(self.L))
+        self.n_out = self.nv + 2 * self.ne
+        return self
 
     def __del__(self):
         if getattr(self, "L", None):
@@ -225,6 +259,90 @@ def rhs_numpy(nv, src, dst, vk, ek, u, p, dtype=np.float64):
         w = u[1::2]
         du[0::2] = w
         du[1::2] = dtype(1) / M * (Pm - D * w + agg)
+    return du
+
+
+def layout_batched(nv, src, dst, vertex_batches, vertex_batch, edge_batches, edge_batch):
+    """Flat layout of a batched network (src/network_structure.jl:224-258), restated in
+    numpy: vertex batches then edge batches, components ascending inside a batch.
+    Returns the per-component first state / parameter indices and the edge order."""
+    vb = np.asarray(vertex_batch)
+    eb = np.asarray(edge_batch) if len(src) else np.zeros(0, dtype=np.int64)
+    vorder = np.concatenate([np.flatnonzero(vb == b) for b in range(len(vertex_batches))])
+    eorder = (np.concatenate([np.flatnonzero(eb == b) for b in range(len(edge_batches))])
+              if len(edge_batches) else np.zeros(0, dtype=np.int64))
+    v_data = np.zeros(nv, dtype=np.int64)
+    v_para = np.zeros(nv, dtype=np.int64)
+    e_data = np.zeros(len(src), dtype=np.int64)
+    e_para = np.zeros(len(src), dtype=np.int64)
+    st = par = 0
+    for v in vorder:
+        k = vertex_batches[vb[v]]
+        v_data[v], v_para[v] = st, par
+        st += VDIM[k]
+        par += VPDIM[k]
+    for e in eorder:
+        k = edge_batches[eb[e]][0]
+        e_data[e], e_para[e] = st, par
+        st += EDIM[k]
+        par += EPDIM[k]
+    return dict(v_data=v_data, v_para=v_para, e_data=e_data, e_para=e_para, eorder=eorder, dim=st, pdim=par)
+
+
+def rhs_numpy_batched(nv, src, dst, vertex_batches, vertex_batch, edge_batches, edge_batch, u, p,
+                      dtype=np.float64):
+    """Independent numpy restatement of the sequential RHS of a batched network (several
+    vertex / edge batches, ODE edges, Symmetric / Directed / Fiducial outputs)."""
+    src = np.asarray(src, dtype=np.int64)
+    dst = np.asarray(dst, dtype=np.int64)
+    L = layout_batched(nv, src, dst, vertex_batches, vertex_batch, edge_batches, edge_batch)
+    u = np.asarray(u, dtype=dtype)
+    p = np.asarray(p if p is not None else np.zeros(0), dtype=dtype)
+    sin = (lambda x: np.sin(x)) if dtype == np.float64 else (lambda x: np.sin(x).astype(dtype))
+    du = np.zeros(L["dim"], dtype=dtype)
+    ov = u[L["v_data"]]                                # vertex g: StateMask(1)
+    eo = L["eorder"]
+    eb = np.asarray(edge_batch, dtype=np.int64)
+    ne = len(src)
+    ysrc = np.zeros(ne, dtype=dtype)
+    ydst = np.zeros(ne, dtype=dtype)
+    for b, (k, c) in enumerate(edge_batches):
+        es = np.flatnonzero(eb == b)
+        vs, vd = ov[src[es]], ov[dst[es]]
+        if k in (E_DIFFUSION_ODE, E_DIFFUSION_ODE_FIXED):
+            x0, x1 = u[L["e_data"][es]], u[L["e_data"][es] + 1]
+            rate = dtype(1) / p[L["e_para"][es]] if k == E_DIFFUSION_ODE else dtype(100.0)
+            du[L["e_data"][es]] = rate * (sin(vs - vd) - x0)
+            du[L["e_data"][es] + 1] = rate * (sin(vd - vs) - x1)
+            ydst[es], ysrc[es] = x0, x1                # Fiducial(dst=1:1, src=2:2)
+            continue
+        w = p[L["e_para"][es]] if EPDIM[k] else None
+        y = (w * (vs - vd) if k == E_DIFFUSION else (vs - vd) if k == E_DIFFUSION_UNIT else w * sin(vs - vd))
+        ydst[es] = y
+        ysrc[es] = y if c == C_SYMMETRIC else (np.zeros_like(y) if c == C_DIRECTED else -y)
+    # output buffer: per edge in batch order, src slot then dst slot; SequentialAggregator
+    vals = np.empty(2 * ne, dtype=dtype)
+    vals[0::2], vals[1::2] = ysrc[eo], ydst[eo]
+    tg = np.empty(2 * ne, dtype=np.int64)
+    tg[0::2], tg[1::2] = src[eo], dst[eo]
+    agg = np.zeros(nv, dtype=dtype)
+    np.add.at(agg, tg, vals)
+    vbatch = np.asarray(vertex_batch)
+    for b, k in enumerate(vertex_batches):
+        vs_ = np.flatnonzero(vbatch == b)
+        s, q, a = L["v_data"][vs_], L["v_para"][vs_], agg[vs_]
+        if k == V_DIFFUSION:
+            du[s] = a
+        elif k == V_KURAMOTO:
+            du[s] = p[q] + a
+        elif k == V_SWING:
+            w = u[s + 1]
+            du[s] = w
+            du[s + 1] = dtype(1) / p[q] * (p[q + 2] - p[q + 1] * w + a)
+        else:
+            w = u[s + 1]
+            du[s] = w
+            du[s + 1] = (p[q].astype(np.float64) - 1.0 * w.astype(np.float64)).astype(dtype) + a
     return du
 
 

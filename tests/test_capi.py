@@ -66,8 +66,11 @@ def test_create_rejects_bad_dtype_and_coupling():
     d, _keep = _desc(g, capi.ND_V_DIFFUSION, capi.ND_E_DIFFUSION)
     h = C.c_void_p()
     assert lib.nd_create(C.byref(d), 3, C.byref(h)) == capi.ND_ERR_DTYPE
-    d2, _keep2 = _desc(g, capi.ND_V_DIFFUSION, capi.ND_E_DIFFUSION, coupling=2)
-    assert lib.nd_create(C.byref(d2), capi.ND_F64, C.byref(h)) == capi.ND_ERR_UNSUPPORTED_COMPONENT
+    for ek, coupling in ((capi.ND_E_DIFFUSION, 9), (capi.ND_E_KURAMOTO, capi.ND_FIDUCIAL),
+                         (capi.ND_E_DIFFUSION_ODE, capi.ND_ANTISYMMETRIC), (6, capi.ND_FIDUCIAL)):
+        d2, _keep2 = _desc(g, capi.ND_V_DIFFUSION, ek, coupling=coupling)
+        assert lib.nd_create(C.byref(d2), capi.ND_F64, C.byref(h)) == capi.ND_ERR_UNSUPPORTED_COMPONENT
+        assert not h.value
     assert lib.nd_create(None, capi.ND_F64, C.byref(h)) == capi.ND_ERR_ARG
 
 

@@ -33,9 +33,28 @@ def test_unsupported_component_raises_no_fallback():
     user_vertex = nd.VertexModel("my_vertex", dim=1, pdim=0, f=lambda *a: None)
     with pytest.raises(nd.UnsupportedComponentError):
         nd.Network(g, user_vertex, nd.diffusion_edge())
-    mixed = [nd.kuramoto_first(), nd.kuramoto_second(), nd.kuramoto_first(), nd.kuramoto_second()]
     with pytest.raises(nd.UnsupportedComponentError):
-        nd.Network(g, mixed, nd.kuramoto_edge())
+        nd.Symmetric(nd.diffusion_odeedge())  # the wrappers take a static single-sided g
+
+
+def test_heterogeneous_network_layout():
+    """Batches in order of first appearance, laid out batch by batch; edge states after
+    every vertex state (src/construction.jl:155-195, src/network_structure.jl:224-258)."""
+    g = nd.complete_graph(4)
+    vf = [nd.kuramoto_second(), nd.diffusion_vertex(), nd.kuramoto_second(), nd.diffusion_vertex()]
+    ef = [nd.diffusion_odeedge(), nd.kuramoto_edge(), nd.kuramoto_edge(), nd.diffusion_edge_fid(),
+          nd.diffusion_odeedge(), nd.diffusion_edge_fid()]
+    nw = nd.Network(g, vf, ef)
+    assert not nw.homogeneous and nw.vertexm is None and nw.edgem is None
+    assert (nw.dim, nw.pdim) == (10, 12)
+    assert nw.vertex_batch.tolist() == [0, 1, 0, 1] and nw.edge_batch.tolist() == [0, 1, 1, 2, 0, 2]
+    assert [nw.vertex_state_index(v) for v in range(4)] == [0, 4, 2, 5]
+    assert [nw.edge_state_index(e) for e in (0, 4)] == [6, 8]
+    assert [nw.edge_param_index(e) for e in range(6)] == [6, 8, 9, 10, 7, 11]
+    p = nw.pflat(vertex={"Pm": np.arange(4.0)}, edge={"K": 3.0})
+    np.testing.assert_array_equal(p, [1, .1, 0, 1, .1, 2, 100, 100, 3, 3, 1, 1])
+    same = nd.Network(g, [nd.kuramoto_first()] * 4, [nd.Directed(nd.kuramoto_edge())] * 6)
+    assert same.homogeneous and same.edgem.coupling == "Directed"
 
 
 def test_aggregator_only_plus():
