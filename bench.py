@@ -47,6 +47,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-f32", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cases", action="store_true",
+                    help="instead of the headline workload: the reference's benchmark cases at their largest size, "
+                         "one JSON line each")
     return ap.parse_args()
 
 
@@ -446,8 +449,96 @@ def run_gb300(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+# The reference's benchmark cases (benchmark/benchmark_cases.jl:20-66) at their largest N.
+# Graphs.jl's watts_strogatz(N, 3, 0.8) links div(3, 2) = 1 ring neighbour per side before
+# rewiring, which is k = 2 here.  The powergrid cases need mass-matrix (DAE) vertices and
+# the pi-line edge, which the GPU library does not have.
+def _case_networks(N, name):
+    import nd_gb300 as nd
+    if name == "diffusion_static_edge":
+        return nd.watts_strogatz(N, N // 2, 0.0, seed=1), nd.diffusion_vertex(), nd.diffusion_edge_unit()
+    if name == "diffusion_ode_edge":
+        return nd.watts_strogatz(N, N // 2, 0.0, seed=1), nd.diffusion_vertex(), nd.diffusion_dedge()
+    g = nd.watts_strogatz(N, 2, 0.8, seed=1)
+    if name == "kuramoto_homogeneous":
+        return g, nd.kuramoto_vertex_2d(), nd.static_kuramoto_edge()
+    kinds = np.random.default_rng(1).permutation(np.repeat([0, 1], N // 2))
+    return g, [nd.kuramoto_vertex_1d() if k == 0 else nd.kuramoto_vertex_2d() for k in kinds], \
+        nd.static_kuramoto_edge()
+
+
+CASES = (("diffusion_static_edge", 3000), ("diffusion_ode_edge", 3000), ("kuramoto_homogeneous", 100_000),
+         ("kuramoto_heterogeneous", 100_000))
+
+
+def run_cases(args):
+    """GPU RHS time of every reference benchmark case (FP64 and FP32, CUDA events over
+    back-to-back calls on resident buffers, as the reference's @benchmark of nw(du, u, p, NaN)),
+    with the CPU oracle (sequential on one core, threaded on all cores) on the same inputs."""
+    import torch
+
+    import nd_gb300 as nd
+    from nd_gb300 import _capi as capi
+    from oracle import oracle as O
+    dev = torch.device("cuda:0")
+    torch.cuda.set_device(dev)
+    hbm = peaks()[0]
+    for name, N in CASES:
+        g, vm, em = _case_networks(N, name)
+        net = nd.Network(g, vm, em)
+        rng = np.random.default_rng(2)
+        u = rng.normal(size=net.dim)
+        p = rng.uniform(0.5, 1.5, size=net.pdim)
+        line = {"case": name, "N": N, "ne": g.ne, "dim": net.dim, "pdim": net.pdim,
+                "vertex_batches": len(net.vertex_batches), "edge_batches": len(net.edge_batches)}
+        for tag, dt, s in (("f64", torch.float64, 8), ("f32", torch.float32, 4)):
+            nw = nd.adapt(net, dt)
+            ut = torch.from_numpy(u).to(dev, dt)
+            pt = torch.from_numpy(p).to(dev, dt) if net.pdim else None
+            du = torch.empty_like(ut)
+            stream = torch.cuda.current_stream()
+            for _ in range(max(3, args.warmup)):
+                nw(du, ut, pt, 0.0, stream=stream)
+            nw.kernel_times()
+            steps = max(10, min(args.steps, 500))
+            torch.cuda.synchronize()
+            el = time_device(nw, du, ut, pt, steps, stream)
+            launches = {k: n // steps for k, (n, _) in nw.kernel_times().items() if n}
+            # per-kernel device time from a second, event-bracketed pass
+            nw.set_kernel_timing(True)
+            time_device(nw, du, ut, pt, 50, stream)
+            kernel_us = {k: 1e3 * ms / n for k, (n, ms) in nw.kernel_times().items() if n}
+            nw.set_kernel_timing(False)
+            algo = s * (2 * net.dim + net.pdim) + 4 * (g.nv + 1) + 2 * g.ne * 8
+            line[tag] = {"rhs_us": 1e6 * el / steps, "edges_per_s": g.ne * steps / el,
+                         "algorithmic_gbs": algo * steps / el / 1e9,
+                         "hbm_frac_of_measured": algo * steps / el / 1e9 / hbm,
+                         "kernels_per_rhs": launches, "kernel_us": kernel_us,
+                         "path": "batched" if "batched_rows" in launches else "homogeneous"}
+        vb = [m.kind for m in net.vertex_batches]
+        eb = [(m.kind, capi.COUPLINGS[m.coupling]) for m in net.edge_batches]
+        on = O.OracleNetwork.from_batches(g.nv, g.src, g.dst, vb, net.vertex_batch, eb, net.edge_batch)
+        for tag, fn, threads in (("cpu_sequential", on.rhs, 1), ("cpu_threaded", on.rhs_poly, os.cpu_count() or 1)):
+            O.load().nd_oracle_set_num_threads(threads)
+            fn(u, p)
+            n, t0 = 0, time.perf_counter()
+            while True:
+                fn(u, p)
+                n += 1
+                sec = time.perf_counter() - t0
+                if sec > 3.0 or n >= 200:
+                    break
+            line[tag] = {"rhs_us": 1e6 * sec / n, "cores": threads, "kind": "port", "evaluations": n}
+        O.load().nd_oracle_set_num_threads(os.cpu_count() or 1)
+        line["speedup_f64_vs_cpu_threaded"] = line["cpu_threaded"]["rhs_us"] / line["f64"]["rhs_us"]
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.cases:
+        run_cases(args)
+        return
     rank, world, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, rank, world)

@@ -13,10 +13,10 @@
 //          (y_src, y_dst) is stored as one vector at y2[2k], the reference's output
 //          buffer order;
 //   rows   every vertex sums the y2 entries of its terms in ascending index order (the
-//          sequential aggregation order), then runs the vertex f of its batch.  Rows of
-//          degree above kLightMaxDeg take a warp each and sum by the exact scan (FP64:
-//          the same bits as the sequential sum), shorter rows a thread each, sorted by
-//          degree so the lanes of a warp do equal work.
+//          sequential aggregation order), then runs the vertex f of its batch.  Long rows
+//          take a warp each (FP64: the windowed exact scan, the same bits as the sequential
+//          sum), shorter rows a thread each, sorted by degree so the lanes of a warp do
+//          equal work.
 // Homogeneous networks of the static AntiSymmetric kinds keep the two-phase kernels of
 // nd_rhs_edge.cu; this path covers everything else in the library.
 #include <algorithm>
@@ -115,55 +115,96 @@ __global__ void __launch_bounds__(kBlock) batched_edge_kernel(BatchedKArgs a) {
     }
 }
 
-// Sum of a row's n terms (y2 indices idx[0..n)) by one thread, in order.  FP64 folds the
-// reference's zero start into the first term (0 + t is t; -0 gives +0).
+// Rows with at least this many terms take a warp each; shorter rows a thread each.  FP64
+// keeps the sequential sum, whose running sum changes binade often on rows of mixed-sign
+// terms; there a thread per row (32 rows in step per warp) beats the warp scan up to the
+// length at which the homogeneous path also moves rows to the exact scan.  FP32 rows are
+// compensated sums with no order to keep, which a warp splits across its lanes.
+constexpr int kWarpRowMinDegF64 = kMediumMaxDeg + 1;
+constexpr int kWarpRowMinDegF32 = 2 * kLightMaxDeg + 1;
+// Terms per warp tile in shared memory (FP64 warp rows): 16 per lane.
+constexpr int kWarpTile = 512;
+
+// Sum of a row's n terms (y2 indices idx[0..n)) by one thread, in order, loads issued
+// kB terms ahead of the adds.  The adds of a batch stop at the longest remaining row in
+// the warp (a warp-uniform bound), so no add is issued for batch slots no lane has.
+//   FP64  the sequential sum with the reference's zero start folded into the first term
+//         (0 + t is t; -0 gives +0);
+//   FP32  the same order, Kahan-compensated on rows longer than kLightMaxDeg.
 template <typename T>
 __device__ __forceinline__ T thread_row_sum(const T* __restrict__ y2, const int32_t* __restrict__ idx, int n) {
     using A = Arith<T>;
-    constexpr int kB = 8;
-    T acc = T(0);
+    constexpr int kB = 12;
+    const bool kahan = sizeof(T) == 4 && n > kLightMaxDeg;
+    T acc = T(0), comp = T(0);
     for (int j0 = 0; j0 < n; j0 += kB) {
         T t[kB];
 #pragma unroll
         for (int k = 0; k < kB; ++k) t[k] = j0 + k < n ? __ldg(y2 + __ldg(idx + j0 + k)) : T(0);
+        const int lim = __reduce_max_sync(__activemask(), (unsigned)min(kB, n - j0));
 #pragma unroll
         for (int k = 0; k < kB; ++k) {
-            if (j0 + k >= n) break;
+            if (k >= lim) break;
+            if (j0 + k >= n) continue;
             if (sizeof(T) == 8 && j0 + k == 0) {
                 const double t0 = (double)t[0];
                 acc = (T)((__double_as_longlong(t0) << 1) == 0 ? 0.0 : t0);
+            } else if (kahan) {
+                const T yk = A::sub(t[k], comp);
+                const T s2 = A::add(acc, yk);
+                comp = A::sub(A::sub(s2, acc), yk);
+                acc = s2;
             } else {
                 acc = A::add(acc, t[k]);
             }
         }
     }
-    return acc;
+    return sizeof(T) == 4 ? A::sub(acc, comp) : acc;
 }
 
 // Sum of a row's n terms by one warp (the result is valid in every lane).
-//   FP64 exact   the sequential sum, bit for bit, by the exact scan on the integer pipes
-//   FP64 native  the sequential sum with hardware adds (one warp-wide chain)
+//   FP64 exact   the sequential sum, bit for bit: the terms are gathered tile by tile into
+//                shared memory and added by the windowed exact scan (256 terms per warp
+//                step while the running sum keeps its binade)
+//   FP64 native  the sequential sum with hardware adds (lane 0 walks the tile)
 //   FP64 tree    lane partial sums and a butterfly (deterministic, not the sequential bits)
 //   FP32         Kahan-compensated lane partial sums and a butterfly
 template <typename T>
 __device__ __forceinline__ T warp_row_sum(const T* __restrict__ y2, const int32_t* __restrict__ idx, int n, int lane,
-                                          int mode) {
+                                          int mode, double* __restrict__ tile) {
     if constexpr (sizeof(T) == 8) {
-        double S = 0.0;
-        for (int c = 0; c < n; c += 32) {
-            const int m = min(32, n - c);
-            const double t = lane < m ? __ldg(y2 + __ldg(idx + c + lane)) : 0.0;
-            if (mode == kModeExact) {
-                S = exact_scan_add(S, t, m, lane);
-            } else if (mode == kModeNative) {
-                for (int i = 0; i < m; ++i) S = __dadd_rn(S, __shfl_sync(kFull, t, i));
-            } else {
-                S = __dadd_rn(S, t);
+        constexpr int kPer = kWarpTile / 32;
+        double S = 0.0, part = 0.0;
+        for (int c = 0; c < n; c += kWarpTile) {
+            const int m = min(kWarpTile, n - c);
+            double r[kPer];
+#pragma unroll
+            for (int k = 0; k < kPer; ++k) {
+                const int j = lane + 32 * k;
+                r[k] = j < m ? __ldg(y2 + __ldg(idx + c + j)) : 0.0;
             }
+#pragma unroll
+            for (int k = 0; k < kPer; ++k) {
+                const int j = lane + 32 * k;
+                if (j < m) tile[j] = r[k];
+            }
+            __syncwarp();
+            if (mode == kModeExact) {
+                S = exact_scan_wide(S, tile, m, lane);
+            } else if (mode == kModeNative) {
+                if (lane == 0)
+                    for (int i = 0; i < m; ++i) S = __dadd_rn(S, tile[i]);
+                S = __shfl_sync(kFull, S, 0);
+            } else {
+#pragma unroll
+                for (int k = 0; k < kPer; ++k) part = __dadd_rn(part, r[k]);
+            }
+            __syncwarp();
         }
         if (mode == kModeTree) {
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1) S = __dadd_rn(S, __shfl_xor_sync(kFull, S, off));
+            for (int off = 16; off > 0; off >>= 1) part = __dadd_rn(part, __shfl_xor_sync(kFull, part, off));
+            S = part;
         }
         return (T)S;
     } else {
@@ -207,20 +248,29 @@ __device__ __forceinline__ void batched_vertex_f(const BatchedKArgs& a, int64_t 
 }
 
 // Rows: blocks [0, n_warp_blocks) take the long rows a warp each, the rest one row per
-// thread.
+// thread.  Blocks are small (kRowBlock threads) so that networks with few rows -- dense
+// graphs, whose long per-thread chains are the whole cost -- still spread over every SM.
+constexpr int kRowBlock = 64;
+constexpr int kRowWarps = kRowBlock / 32;
 template <typename T>
-__global__ void __launch_bounds__(kBlock) batched_row_kernel(BatchedKArgs a, int64_t n_warp_blocks) {
+__global__ void __launch_bounds__(kRowBlock) batched_row_kernel(BatchedKArgs a, int64_t n_warp_blocks) {
     const T* __restrict__ y2 = static_cast<const T*>(a.y2);
     if ((int64_t)blockIdx.x < n_warp_blocks) {
-        const int lane = threadIdx.x & 31;
-        const int64_t slot = (int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        const int64_t slot = (int64_t)blockIdx.x * kRowWarps + warp;
         if (slot >= a.n_warp_rows) return;  // warp-uniform
         const uint32_t t0 = __ldg(a.tptr + slot);
         const int n = (int)(__ldg(a.tptr + slot + 1) - t0);
-        const T acc = warp_row_sum<T>(y2, a.tidx + t0, n, lane, a.mode);
+        T acc;
+        if constexpr (sizeof(T) == 8) {
+            __shared__ double tiles[kRowWarps][kWarpTile];
+            acc = warp_row_sum<T>(y2, a.tidx + t0, n, lane, a.mode, tiles[warp]);
+        } else {
+            acc = warp_row_sum<T>(y2, a.tidx + t0, n, lane, a.mode, nullptr);
+        }
         if (lane == 0) batched_vertex_f<T>(a, __ldg(a.slot_vpos + slot), acc);
     } else {
-        const int64_t slot = a.n_warp_rows + ((int64_t)blockIdx.x - n_warp_blocks) * kBlock + threadIdx.x;
+        const int64_t slot = a.n_warp_rows + ((int64_t)blockIdx.x - n_warp_blocks) * kRowBlock + threadIdx.x;
         if (slot >= a.nv) return;
         const uint32_t t0 = __ldg(a.tptr + slot);
         const int n = (int)(__ldg(a.tptr + slot + 1) - t0);
@@ -252,9 +302,9 @@ cudaError_t launch_typed(const BatchedNet& b, void* du, const void* u, const voi
         batched_edge_kernel<T><<<(unsigned)blocks, kBlock, 0, s>>>(a);
     }
     if (phases & kPhaseRow) {
-        const int64_t wb = (b.n_warp_rows + kWarpsPerBlock - 1) / kWarpsPerBlock;
-        const int64_t tb = (b.nv - b.n_warp_rows + kBlock - 1) / kBlock;
-        if (wb + tb > 0) batched_row_kernel<T><<<(unsigned)(wb + tb), kBlock, 0, s>>>(a, wb);
+        const int64_t wb = (b.n_warp_rows + kRowWarps - 1) / kRowWarps;
+        const int64_t tb = (b.nv - b.n_warp_rows + kRowBlock - 1) / kRowBlock;
+        if (wb + tb > 0) batched_row_kernel<T><<<(unsigned)(wb + tb), kRowBlock, 0, s>>>(a, wb);
     }
     return cudaGetLastError();
 }
@@ -405,9 +455,10 @@ int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out) {
     std::vector<int32_t> by_pos(nv);
     for (int64_t v = 0; v < nv; ++v) by_pos[vpos[v]] = (int32_t)v;
     std::vector<int32_t> longr, shortr;
+    const int warp_min = elem == 8 ? kWarpRowMinDegF64 : kWarpRowMinDegF32;
     for (int64_t k = 0; k < nv; ++k) {
         const int32_t v = by_pos[k];
-        (deg[v] > (uint32_t)kLightMaxDeg ? longr : shortr).push_back(v);
+        (deg[v] >= (uint32_t)warp_min ? longr : shortr).push_back(v);
     }
     auto by_degree = [&](int32_t x, int32_t y) { return deg[x] > deg[y]; };
     std::stable_sort(longr.begin(), longr.end(), by_degree);

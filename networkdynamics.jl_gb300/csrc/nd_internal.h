@@ -181,7 +181,7 @@ struct BatchedNet {
     BatchTable* d_eb = nullptr;
     int64_t nv = 0, ne = 0, dim = 0, pdim = 0;
     int32_t max_degree = 0;
-    int64_t n_warp_rows = 0;     // slots [0, n_warp_rows): degree > kLightMaxDeg, a warp per row
+    int64_t n_warp_rows = 0;     // slots [0, n_warp_rows): the long rows, a warp per row
     int2* eu = nullptr;          // [ne] by edge position: u indices of the src / dst vertex outputs
     uint32_t* tptr = nullptr;    // [nv+1] by slot: range of the slot's terms in tidx
     int32_t* tidx = nullptr;     // [2ne] y2 indices of every row's terms, ascending

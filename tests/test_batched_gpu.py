@@ -126,28 +126,42 @@ def test_random_batched_parity(cuda, nv, m, seed):
     u = rng.normal(size=nw.dim)
     p = rng.uniform(0.5, 1.5, size=nw.pdim)
     ref = on.rhs(u, p)
-    nw64 = adapt(nw, np.float64)
-    assert nw64.info().n_hubs > 0
+    nw64, nw32 = adapt(nw, np.float64), adapt(nw, np.float32)
+    # FP32 rows of 65+ terms take a warp each; FP64 rows only beyond 2048 terms
+    assert (nw32.info().n_hubs > 0) == (nv >= 5000) and nw64.info().n_hubs == 0
     check_sine_f64(gpu_rhs(nw64, u, p, cuda, np.float64), ref, g, nw, u, p)
-    got32 = gpu_rhs(adapt(nw, np.float32), u, p, cuda, np.float32).astype(np.float64)
+    got32 = gpu_rhs(nw32, u, p, cuda, np.float32).astype(np.float64)
     check_f32_isapprox(got32, ref)
     np.testing.assert_allclose(got32, ref, rtol=2e-4, atol=2e-4 * (1 + np.abs(ref).max()))
 
 
+def star_with_ring(n):
+    """Vertex 0 linked to all others (a row of n - 1 terms), the others on a ring."""
+    src = np.concatenate([np.zeros(n - 1, dtype=np.int64), np.arange(1, n - 1)])
+    dst = np.concatenate([np.arange(1, n), np.arange(2, n)])
+    return nd.Graph(n, src, dst)
+
+
+@pytest.mark.parametrize("graph", ["ba20k", "dense_ws1500", "star6000"])
 @pytest.mark.parametrize("order", ["sequential", "sequential_hw"])
-def test_batched_without_sine_bitwise(cuda, order):
-    g = nd.barabasi_albert(20_000, 3, seed=7)
+def test_batched_without_sine_bitwise(cuda, order, graph):
+    """Power-law hubs, a dense graph (rows of ~1400 terms), and a hub of 5999 terms that
+    takes the warp-row path and spans several shared-memory tiles of its exact scan."""
+    g = {"ba20k": lambda: nd.barabasi_albert(20_000, 3, seed=7),
+         "dense_ws1500": lambda: nd.watts_strogatz(1500, 1400, 0.1, seed=7),
+         "star6000": lambda: star_with_ring(6000)}[graph]()
     rng = np.random.default_rng(7)
     nw, on = build(g, VKINDS, NO_SINE, vassign=rng.integers(0, 4, g.nv), eassign=rng.integers(0, len(NO_SINE), g.ne))
     u = rng.normal(size=nw.dim)
     p = rng.uniform(0.5, 1.5, size=nw.pdim)
     nw64 = adapt(nw, np.float64)
+    assert nw64.info().n_hubs == (1 if graph == "star6000" else 0)
     nw64.set_sum_order(order)
     np.testing.assert_array_equal(gpu_rhs(nw64, u, p, cuda, np.float64), on.rhs(u, p))
 
 
 def test_batched_tree_order_close(cuda):
-    g = nd.barabasi_albert(20_000, 3, seed=8)
+    g = star_with_ring(6000)
     rng = np.random.default_rng(8)
     nw, on = build(g, VKINDS, NO_SINE, vassign=rng.integers(0, 4, g.nv), eassign=rng.integers(0, len(NO_SINE), g.ne))
     u = rng.normal(size=nw.dim)
@@ -221,6 +235,19 @@ def test_tsit5_with_ode_edges_matches_oracle(cuda):
     assert st.status == 0 and rst.status == 0
     assert abs(st.naccept - rst.naccept) <= 1 and abs(st.nreject - rst.nreject) <= 1
     np.testing.assert_allclose(u.cpu().numpy(), ref, rtol=1e-7, atol=1e-7)
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_device_sine_is_odd(cuda, dtype):
+    """The ODE edge evaluates sin(vs - vd) once and uses its negation for sin(vd - vs): the
+    same bits only if the device sine is exactly odd (vd - vs is exactly -(vs - vd) in
+    IEEE arithmetic).  Checked on the device over 2^22 arguments of every magnitude."""
+    import torch
+    dt = getattr(torch, dtype)
+    g = torch.Generator(device=cuda).manual_seed(0)
+    mag = torch.pow(10.0, torch.empty(1 << 22, device=cuda, dtype=torch.float64).uniform_(-12, 6, generator=g))
+    x = (mag * torch.empty_like(mag).uniform_(1, 2, generator=g)).to(dt)
+    assert torch.equal(torch.sin(-x), -torch.sin(x))
 
 
 def test_batched_errors(cuda):
