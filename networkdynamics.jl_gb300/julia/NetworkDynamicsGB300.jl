@@ -16,10 +16,17 @@ Plug points used (paths relative to the NetworkDynamics.jl source tree):
 
 Only the hand-written component library runs on this path; any other component function
 raises an `ArgumentError` when the aggregator is built.  There is no CPU fallback.
+
+Heterogeneous networks (several vertex / edge batches), ODE edges and the Symmetric /
+Directed / Fiducial outputs go through `nd_create_batched`: the shim hands over the
+reference's own batches (the edge batches the aggregator constructor receives, and the
+vertex batches `_find_identical_components` forms, both in order of first appearance),
+so the device handle uses exactly the layout of `u` and `p` the `Network` defines.
 """
 module NetworkDynamicsGB300
 
-using NetworkDynamics: NetworkDynamics, Network, ExecutionStyle, AntiSymmetric, executionstyle
+using NetworkDynamics: NetworkDynamics, Network, ExecutionStyle, AntiSymmetric, Symmetric, Directed, Fiducial,
+                       executionstyle
 using CUDA: CUDA, CuArray, CuPtr
 using Adapt: Adapt
 
@@ -35,16 +42,28 @@ const ND_ERR_DTYPE = Cint(-3)
 const ND_F32 = Cint(1)
 const ND_F64 = Cint(2)
 const ND_ANTISYMMETRIC = Cint(1)
+const ND_SYMMETRIC = Cint(2)
+const ND_DIRECTED = Cint(3)
+const ND_FIDUCIAL = Cint(4)
 
-struct nd_network_desc
+struct nd_batch
+    kind::Int32
+    coupling::Int32
+end
+
+struct nd_batched_network_desc
     nv::Int64
     ne::Int64
     src::Ptr{Int64}
     dst::Ptr{Int64}
-    vertex_kind::Int32
-    edge_kind::Int32
-    coupling::Int32
+    n_vertex_batches::Int32
+    n_edge_batches::Int32
+    vertex_batches::Ptr{nd_batch}
+    edge_batches::Ptr{nd_batch}
+    vertex_batch::Ptr{Int32}
+    edge_batch::Ptr{Int32}
     flags::Int32
+    reserved::Int32
 end
 
 """
@@ -55,7 +74,9 @@ Unbuffered execution style whose RHS is one call into libnd_b200.so.
 struct GB300Execution <: ExecutionStyle{false} end
 
 # Known component functions -> library kinds (nd_vertex_kind / nd_edge_kind).  Models
-# built from the component library register their functions here.
+# built from the component library register their functions here: vertex f, the
+# single-sided g inside an AntiSymmetric / Symmetric / Directed wrapper, the f of an ODE
+# edge, or a two-sided g (diffusionedge_fid!, registered with register_gb300_edge!(g, 1)).
 const VERTEX_KINDS = IdDict{Any,Cint}()
 const EDGE_KINDS = IdDict{Any,Cint}()
 register_gb300_vertex!(f, kind::Integer) = (VERTEX_KINDS[f] = Cint(kind); f)
@@ -64,11 +85,13 @@ register_gb300_edge!(g, kind::Integer) = (EDGE_KINDS[g] = Cint(kind); g)
 mutable struct GB300Aggregator{F}
     f::F
     nv::Int
-    src::Vector{Int64}       # 0-based, edges(g) order
+    src::Vector{Int64}                # 0-based, edges(g) order
     dst::Vector{Int64}
-    vertex_kind::Cint
-    edge_kind::Cint
-    handle::Ptr{Cvoid}       # C_NULL until adapted to the device
+    vertex_batches::Vector{nd_batch}  # in the reference's batch order
+    edge_batches::Vector{nd_batch}
+    vertex_batch::Vector{Int32}       # batch of every vertex / edge (0-based)
+    edge_batch::Vector{Int32}
+    handle::Ptr{Cvoid}                # C_NULL until adapted to the device
     dtype::Cint
 end
 
@@ -83,21 +106,40 @@ function GB300Aggregator(f)
     (im, batches) -> GB300Aggregator(im, batches, f)
 end
 
+unsupported(what) = throw(ArgumentError("$what is not in the GB300 component library; \
+                                         GB300Execution has no CPU fallback"))
+
+function edge_batch_kind(batch)
+    g = batch.compg
+    if g isa Fiducial        # ODE edges: StateMask outputs, the kind is the edge's f
+        return nd_batch(get(() -> unsupported("edge function $(batch.compf)"), EDGE_KINDS, batch.compf), ND_FIDUCIAL)
+    end
+    for (W, c) in ((AntiSymmetric, ND_ANTISYMMETRIC), (Symmetric, ND_SYMMETRIC), (Directed, ND_DIRECTED))
+        g isa W && return nd_batch(get(() -> unsupported("edge function $(g.g)"), EDGE_KINDS, g.g), c)
+    end
+    nd_batch(get(() -> unsupported("edge function $g"), EDGE_KINDS, g), ND_FIDUCIAL)  # two-sided g
+end
+
 function GB300Aggregator(im, batches, f)
-    nw_vm = unique(map(m -> m.f, im.vertexm))
-    length(nw_vm) == 1 || throw(ArgumentError("GB300Execution needs one homogeneous vertex batch"))
-    vk = get(VERTEX_KINDS, only(nw_vm), Cint(0))
-    vk == 0 && throw(ArgumentError("vertex function $(only(nw_vm)) is not in the GB300 component library; \
-                                    GB300Execution has no CPU fallback"))
-    length(batches) == 1 || throw(ArgumentError("GB300Execution needs one homogeneous edge batch"))
-    g = only(batches).compg
-    g isa AntiSymmetric || throw(ArgumentError("only AntiSymmetric edges are in the GB300 library"))
-    ek = get(EDGE_KINDS, g.g, Cint(0))
-    ek == 0 && throw(ArgumentError("edge function $(g.g) is not in the GB300 component library; \
-                                    GB300Execution has no CPU fallback"))
+    # vertex batches exactly as the Network formed them (src/construction.jl:155-160)
+    vidxs = NetworkDynamics._find_identical_components(im.vertexm)
+    vbatches = map(vidxs) do idxs
+        vf = im.vertexm[first(idxs)].f
+        nd_batch(get(() -> unsupported("vertex function $vf"), VERTEX_KINDS, vf), 0)
+    end
+    vbatch = zeros(Int32, length(im.v_data))
+    for (b, idxs) in enumerate(vidxs), i in idxs
+        vbatch[i] = b - 1
+    end
+    ebatches = nd_batch[edge_batch_kind(batch) for batch in batches]
+    ebatch = zeros(Int32, length(im.edgevec))
+    for (b, batch) in enumerate(batches), i in batch.indices
+        ebatch[i] = b - 1
+    end
     src = Int64[e.src - 1 for e in im.edgevec]
     dst = Int64[e.dst - 1 for e in im.edgevec]
-    GB300Aggregator{typeof(f)}(f, length(im.v_data), src, dst, vk, ek, C_NULL, Cint(0))
+    GB300Aggregator{typeof(f)}(f, length(im.v_data), src, dst, collect(vbatches), ebatches, vbatch, ebatch,
+                               C_NULL, Cint(0))
 end
 
 NetworkDynamics.get_aggr_constructor(a::GB300Aggregator) = GB300Aggregator(a.f)
@@ -118,12 +160,16 @@ end
 # the device handle for element type T (the reference's cache typing at adapt time).
 function Adapt.adapt_structure(::Type{<:CuArray{T}}, a::GB300Aggregator) where {T<:Union{Float32,Float64}}
     dtype = T === Float64 ? ND_F64 : ND_F32
-    desc = nd_network_desc(a.nv, length(a.src), pointer(a.src), pointer(a.dst), a.vertex_kind, a.edge_kind,
-                           ND_ANTISYMMETRIC, 0)
-    out = GB300Aggregator{typeof(a.f)}(a.f, a.nv, a.src, a.dst, a.vertex_kind, a.edge_kind, C_NULL, dtype)
+    out = GB300Aggregator{typeof(a.f)}(a.f, a.nv, a.src, a.dst, a.vertex_batches, a.edge_batches, a.vertex_batch,
+                                       a.edge_batch, C_NULL, dtype)
     h = Ref{Ptr{Cvoid}}(C_NULL)
-    GC.@preserve a check(ccall((:nd_create, libnd), Cint, (Ref{nd_network_desc}, Cint, Ref{Ptr{Cvoid}}),
-                               desc, dtype, h))
+    GC.@preserve a begin
+        desc = nd_batched_network_desc(a.nv, length(a.src), pointer(a.src), pointer(a.dst),
+                                       length(a.vertex_batches), length(a.edge_batches), pointer(a.vertex_batches),
+                                       pointer(a.edge_batches), pointer(a.vertex_batch), pointer(a.edge_batch), 0, 0)
+        check(ccall((:nd_create_batched, libnd), Cint, (Ref{nd_batched_network_desc}, Cint, Ref{Ptr{Cvoid}}),
+                    desc, dtype, h))
+    end
     out.handle = h[]
     finalizer(x -> x.handle == C_NULL || ccall((:nd_destroy, libnd), Cint, (Ptr{Cvoid},), x.handle), out)
     out
