@@ -233,6 +233,19 @@ int nd_rhs(nd_handle* h, int dtype, void* du, int64_t n_du, const void* u, int64
  * of the handle.  Stream-ordered. */
 int nd_jvp(nd_handle* h, int dtype, void* jv, const void* u, const void* p, const void* v, double t, void* stream);
 
+/* Sparse Jacobian ∂f/∂u of the RHS in CSR form, rows and columns in the flat state order.
+ * nd_jacobian_pattern replaces get_jac_prototype(nw) (ext/NetworkDynamicsSparsityExt.jl:
+ * 57-127, SparseConnectivityTracer): the structural pattern of the library components
+ * (columns sorted and unique per row; an entry may be numerically zero, e.g. for a self
+ * loop).  It writes nnz, and, when the pointers are not NULL, rowptr[dim + 1] and
+ * colidx[nnz] (host arrays, 0-based).  nd_jacobian replaces the solver's colored
+ * ForwardDiff Jacobian on that prototype: the analytic values at (u, p, t) into
+ * values[nnz] (device, element type of the handle), in the pattern's order.  Both take
+ * homogeneous and batched handles; the pattern is built on first use (host work and a
+ * copy of the structure) and kept by the handle.  nd_jacobian is stream-ordered. */
+int nd_jacobian_pattern(nd_handle* h, int64_t* nnz, int32_t* rowptr, int32_t* colidx);
+int nd_jacobian(nd_handle* h, int dtype, void* values, const void* u, const void* p, double t, void* stream);
+
 /* Result of a solve. */
 typedef struct nd_solve_stats {
     int64_t naccept; /* accepted steps                               */

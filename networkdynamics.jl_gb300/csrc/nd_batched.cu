@@ -61,15 +61,6 @@ struct BatchedKArgs {
     int32_t mode;
 };
 
-// Batch of position `pos`: the last batch whose first position is <= pos (batches are few;
-// empty batches are skipped because the next one starts at the same position).
-__device__ __forceinline__ int find_batch(const BatchTable* __restrict__ t, int64_t pos) {
-    const int n = __ldg(&t->n);
-    int b = 0;
-    while (b + 1 < n && pos >= __ldg(&t->pos0[b + 1])) ++b;
-    return b;
-}
-
 template <typename T>
 __device__ __forceinline__ T static_edge_g(int kind, T vs, T vd, T w) {
     if (kind == ND_E_DIFFUSION) return edge_g_w<T, ND_E_DIFFUSION>(vs, vd, w);
@@ -502,7 +493,7 @@ int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out) {
         (err = upload((void**)&bn.tptr, tptr.data(), tptr.size() * sizeof(uint32_t))) != cudaSuccess ||
         (err = upload((void**)&bn.tidx, tidx.data(), tidx.size() * sizeof(int32_t))) != cudaSuccess ||
         (err = upload((void**)&bn.slot_vpos, slot_vpos.data(), slot_vpos.size() * sizeof(int32_t))) != cudaSuccess ||
-        (err = cudaMalloc(&bn.y2, std::max<size_t>((size_t)2 * ne * elem, 16))) != cudaSuccess) {
+        (elem > 0 && (err = cudaMalloc(&bn.y2, std::max<size_t>((size_t)2 * ne * elem, 16))) != cudaSuccess)) {
         free_batched(&bn);
         return cuda_fail(err, "upload of the batched network");
     }

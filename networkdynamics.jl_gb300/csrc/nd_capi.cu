@@ -439,6 +439,7 @@ int nd_destroy(nd_handle* h) {
     if (h->side) cudaStreamSynchronize(h->side);
     if (h->batched.enabled) free_batched(&h->batched);
     else free_topology(&h->topo);
+    free_jacobian(&h->jac);
     h->tracer.release();
     const int dev = h->device;
     delete_handle(h);

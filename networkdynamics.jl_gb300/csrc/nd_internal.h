@@ -189,7 +189,20 @@ struct BatchedNet {
     void* y2 = nullptr;          // [2ne] scratch, element type of the handle
 };
 
+#ifdef __CUDACC__
+// Batch of position `pos`: the last batch whose first position is <= pos (batches are few;
+// empty batches are skipped because the next one starts at the same position).
+__device__ __forceinline__ int find_batch(const BatchTable* __restrict__ t, int64_t pos) {
+    const int n = __ldg(&t->n);
+    int b = 0;
+    while (b + 1 < n && pos >= __ldg(&t->pos0[b + 1])) ++b;
+    return b;
+}
+#endif
+
 int check_edge_component(int edge_kind, int coupling);  // ND_OK or ND_ERR_UNSUPPORTED_COMPONENT
+// elem: scratch element size (4 / 8); 0 builds the structure without the y2 scratch (a
+// view of a network for the Jacobian).
 int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out);
 void free_batched(BatchedNet* b);
 cudaError_t launch_batched(int dtype, const BatchedNet& b, void* du, const void* u, const void* p, int mode,
@@ -218,6 +231,20 @@ cudaError_t launch_scan_selftest(const double* terms, const int64_t* seg, const 
 
 }  // namespace nd
 
+namespace nd {
+// Sparse Jacobian of a handle (nd_jacobian.cu): the CSR pattern of ∂f/∂u, built on first
+// use, and for homogeneous handles the batched view of their network it is built from.
+struct JacPlan {
+    bool ready = false;
+    BatchedNet view;  // homogeneous handles only (batched handles use their own)
+    int64_t nnz = 0;
+    std::vector<int32_t> rowptr_h, colidx_h;
+    int32_t* rowptr = nullptr;  // device copies
+    int32_t* colidx = nullptr;
+};
+void free_jacobian(JacPlan* j);
+}  // namespace nd
+
 struct nd_handle {
     int dtype;
     int vertex_kind, edge_kind, coupling;
@@ -230,5 +257,6 @@ struct nd_handle {
     int64_t dim, pdim;
     nd::Topology topo;
     nd::BatchedNet batched;  // enabled: the handle is a batched network (topo unused)
+    nd::JacPlan jac;
     nd::Tracer tracer;
 };

@@ -12,7 +12,7 @@ from .components import (AntiSymmetric, Directed, EdgeModel, Symmetric, VertexMo
                          static_line, swing_vertex)
 from .graphs import Graph, barabasi_albert, complete_graph, cycle_graph, random_geometric, simple_graph, watts_strogatz
 from .network import (ExecutionStyle, GB300Aggregator, GB300Execution, Network, adapt, get_aggr_constructor,
-                      iscudacompatible, jvp)
+                      iscudacompatible, jacobian, jacobian_pattern, jvp)
 from .fixpoint import find_fixpoint
 from .mpnn import MPNN
 
@@ -25,5 +25,5 @@ __all__ = [
     "Graph", "barabasi_albert", "complete_graph", "cycle_graph", "random_geometric", "simple_graph",
     "watts_strogatz",
     "ExecutionStyle", "GB300Aggregator", "GB300Execution", "Network", "adapt", "get_aggr_constructor",
-    "iscudacompatible", "jvp", "MPNN", "find_fixpoint",
+    "iscudacompatible", "jacobian", "jacobian_pattern", "jvp", "MPNN", "find_fixpoint",
 ]

@@ -316,6 +316,34 @@ def jvp(nw: Network, jv, u, p, v, t=0.0, stream=None):
                               C.c_void_p(s.cuda_stream)))
 
 
+def jacobian_pattern(nw: Network):
+    """CSR sparsity pattern of ∂f/∂u, the counterpart of get_jac_prototype(nw)
+    (ext/NetworkDynamicsSparsityExt.jl:57-127): (rowptr [dim+1], colidx [nnz]) as int32
+    numpy arrays, columns sorted per row."""
+    lib = nw._lib
+    nnz = C.c_int64()
+    capi.check(lib.nd_jacobian_pattern(nw.handle, C.byref(nnz), None, None))
+    rowptr = np.empty(nw.dim + 1, dtype=np.int32)
+    colidx = np.empty(max(nnz.value, 1), dtype=np.int32)
+    capi.check(lib.nd_jacobian_pattern(nw.handle, C.byref(nnz), rowptr.ctypes.data, colidx.ctypes.data))
+    return rowptr, colidx[:nnz.value]
+
+
+def jacobian(nw: Network, u, p, t=0.0, stream=None):
+    """∂f/∂u at (u, p, t) with the analytic derivatives of the library components, as a
+    torch sparse CSR tensor on u's device (values in the network's precision)."""
+    import torch
+    rowptr, colidx = jacobian_pattern(nw)
+    values = torch.empty(len(colidx), dtype=u.dtype, device=u.device)
+    s = stream if stream is not None else torch.cuda.current_stream()
+    pp = p.data_ptr() if p is not None and p.numel() else None
+    capi.check(nw._lib.nd_jacobian(nw.handle, _dtype_code(u.dtype), values.data_ptr(), u.data_ptr(), pp, float(t),
+                                   C.c_void_p(s.cuda_stream)))
+    return torch.sparse_csr_tensor(torch.from_numpy(rowptr.astype(np.int64)).to(u.device),
+                                   torch.from_numpy(colidx.astype(np.int64)).to(u.device), values,
+                                   size=(nw.dim, nw.dim))
+
+
 def adapt(nw: Network, dtype) -> Network:
     """Counterpart of ``adapt(CuArray{T}, nw)``: a new Network whose handle lives on the
     current CUDA device with caches for element type `dtype` (float32 / float64)."""

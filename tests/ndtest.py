@@ -73,3 +73,18 @@ def exact_rows(g, vk, ek, u, p, vertices):
             w = u[2 * v + 1]
             out[v] = (w, 1.0 / M * (Pm - D * w + acc))
     return out
+
+
+def fd_jacobian(on, u, p):
+    """Dense central-difference Jacobian of the oracle RHS (FP64).  An entry whose state does
+    not enter a row's arithmetic is exactly 0: both perturbed evaluations give the same
+    bits."""
+    u = np.asarray(u, dtype=np.float64)
+    J = np.zeros((on.dim, on.dim))
+    for i in range(on.dim):
+        h = 1e-6 * max(1.0, abs(u[i]))
+        up, um = u.copy(), u.copy()
+        up[i] += h
+        um[i] -= h
+        J[:, i] = (on.rhs(up, p) - on.rhs(um, p)) / (up[i] - um[i])
+    return J
