@@ -241,6 +241,8 @@ struct JacPlan {
     std::vector<int32_t> rowptr_h, colidx_h;
     int32_t* rowptr = nullptr;  // device copies
     int32_t* colidx = nullptr;
+    int32_t* long_slots = nullptr;  // slots of the rows that take a warp each
+    int64_t n_long = 0;
 };
 void free_jacobian(JacPlan* j);
 }  // namespace nd

@@ -14,9 +14,10 @@
 // Columns are sorted and unique per row; a structural entry can be numerically zero (a
 // self loop, whose two derivatives cancel), as in a traced pattern.
 //
-// Values: one thread per vertex row adds its terms' derivatives into its row (found by
-// binary search in the sorted columns), in the order of its terms, so the result is
-// deterministic; one thread per ODE edge writes that edge's two rows.  Homogeneous handles
+// Values: one thread per vertex row of up to 32 terms adds its terms' derivatives into its
+// row (found by binary search in the sorted columns), in the order of its terms; longer
+// rows take a warp each; one thread per ODE edge writes that edge's two rows.  For simple
+// graphs the result is deterministic.  Homogeneous handles
 // get a batched view of their network (no scratch) built from their device topology.
 #include <algorithm>
 #include <string>
@@ -70,6 +71,19 @@ __device__ __forceinline__ void jadd(T* __restrict__ vals, const int32_t* __rest
     if (__ldg(cols + lo) == c) vals[lo] += v;
 }
 
+template <typename T>
+__device__ __forceinline__ void jadd_atomic(T* __restrict__ vals, const int32_t* __restrict__ cols, int n, int32_t c,
+                                            T v) {
+    if (n <= 0) return;
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(cols + mid) < c) lo = mid + 1;
+        else hi = mid;
+    }
+    if (__ldg(cols + lo) == c) atomicAdd(vals + lo, v);
+}
+
 // ∂g/∂vs and ∂g/∂vd of a static edge.
 template <typename T>
 __device__ __forceinline__ void static_edge_dg(int kind, T vs, T vd, T w, T& gs, T& gd) {
@@ -87,11 +101,15 @@ __device__ __forceinline__ void static_edge_dg(int kind, T vs, T vd, T w, T& gs,
     }
 }
 
+// Rows with more terms than this take a warp each (jac_long_row_kernel).
+constexpr uint32_t kJacLongRow = 32;
+
 template <typename T>
 __global__ void __launch_bounds__(kJacBlock) jac_vertex_kernel(JacArgs<T> a) {
     using A = Arith<T>;
     const int64_t slot = (int64_t)blockIdx.x * kJacBlock + threadIdx.x;
     if (slot >= a.nv) return;
+    if (__ldg(a.tptr + slot + 1) - __ldg(a.tptr + slot) > kJacLongRow) return;
     const int64_t pos = __ldg(a.slot_vpos + slot);
     const int b = find_batch(a.vb, pos);
     const int vk = __ldg(&a.vb->kind[b]);
@@ -144,6 +162,75 @@ __global__ void __launch_bounds__(kJacBlock) jac_vertex_kernel(JacArgs<T> a) {
         jadd<T>(vals, cols, n, o.x, A::mul(f, gs));
         jadd<T>(vals, cols, n, o.y, A::mul(f, gd));
     }
+}
+
+// The same for the rows of more than kJacLongRow terms, a warp each: the lanes take the
+// terms in turn.  The derivatives with respect to the vertex's own output (one per term)
+// are summed per lane and then across the warp; the neighbour columns are distinct in a
+// simple graph, and are added atomically for the repeated ones of a multigraph.
+template <typename T>
+__global__ void __launch_bounds__(kJacBlock) jac_long_row_kernel(JacArgs<T> a, const int32_t* __restrict__ slots,
+                                                                 int64_t n_long) {
+    using A = Arith<T>;
+    const int lane = threadIdx.x & 31;
+    const int64_t w = ((int64_t)blockIdx.x * kJacBlock + threadIdx.x) >> 5;
+    if (w >= n_long) return;  // warp-uniform
+    const int64_t slot = __ldg(slots + w);
+    const int64_t pos = __ldg(a.slot_vpos + slot);
+    const int b = find_batch(a.vb, pos);
+    const int vk = __ldg(&a.vb->kind[b]);
+    const int64_t r = pos - __ldg(&a.vb->pos0[b]);
+    const int dim = vk == ND_V_SWING || vk == ND_V_SWING_UNIT ? 2 : 1;
+    const int pd = vk == ND_V_DIFFUSION ? 0 : (vk == ND_V_SWING ? 3 : 1);
+    const int64_t s = __ldg(&a.vb->s0[b]) + dim * r, q = __ldg(&a.vb->p0[b]) + pd * r;
+    T scale = T(1);
+    if (dim == 2) {
+        T dw = T(-1);
+        if (vk == ND_V_SWING) {
+            scale = A::div(T(1), __ldg(a.p + q));
+            dw = -A::mul(scale, __ldg(a.p + q + 1));
+        }
+        if (lane == 0) {
+            const int32_t r0 = __ldg(a.rowptr + s), r1 = __ldg(a.rowptr + s + 1), r2 = __ldg(a.rowptr + s + 2);
+            jadd<T>(a.values + r0, a.colidx + r0, r1 - r0, (int32_t)(s + 1), T(1));
+            jadd<T>(a.values + r1, a.colidx + r1, r2 - r1, (int32_t)(s + 1), dw);
+        }
+    }
+    const int64_t row = s + dim - 1;
+    const int32_t r0 = __ldg(a.rowptr + row);
+    const int n = __ldg(a.rowptr + row + 1) - r0;
+    T* vals = a.values + r0;
+    const int32_t* cols = a.colidx + r0;
+    const int32_t own = (int32_t)s;
+    T own_sum = T(0);
+    const uint32_t t0 = __ldg(a.tptr + slot), t1 = __ldg(a.tptr + slot + 1);
+    for (uint32_t j = t0 + lane; j < t1; j += 32) {
+        const int32_t t = __ldg(a.tidx + j);
+        const int64_t k = t >> 1;
+        const bool dst_side = t & 1;
+        const int eb = find_batch(a.eb, k);
+        const int ek = __ldg(&a.eb->kind[eb]);
+        const int64_t re = k - __ldg(&a.eb->pos0[eb]);
+        if (ek == ND_E_DIFFUSION_ODE || ek == ND_E_DIFFUSION_ODE_FIXED) {
+            jadd_atomic<T>(vals, cols, n, (int32_t)(__ldg(&a.eb->s0[eb]) + 2 * re + (dst_side ? 0 : 1)), scale);
+            continue;
+        }
+        const int c = __ldg(&a.eb->coupling[eb]);
+        if (!dst_side && c == ND_DIRECTED) continue;
+        const int2 o = __ldg(a.eu + k);
+        const T wgt = ek == ND_E_DIFFUSION_UNIT ? T(0) : __ldg(a.p + __ldg(&a.eb->p0[eb]) + re);
+        T gs, gd;
+        static_edge_dg<T>(ek, __ldg(a.u + o.x), __ldg(a.u + o.y), wgt, gs, gd);
+        const T f = dst_side || c == ND_SYMMETRIC ? scale : -scale;
+        const T ds = A::mul(f, gs), dd = A::mul(f, gd);
+        if (o.x == own) own_sum = A::add(own_sum, ds);
+        else jadd_atomic<T>(vals, cols, n, o.x, ds);
+        if (o.y == own) own_sum = A::add(own_sum, dd);
+        else jadd_atomic<T>(vals, cols, n, o.y, dd);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) own_sum = A::add(own_sum, __shfl_xor_sync(0xffffffffu, own_sum, off));
+    if (lane == 0) jadd<T>(vals, cols, n, own, own_sum);
 }
 
 template <typename T>
@@ -276,6 +363,10 @@ int build_plan(nd_handle* h) {
         if (nnz > (int64_t)INT32_MAX) return fail(ND_ERR_UNSUPPORTED, "nd_jacobian: more than 2^31-1 nonzeros");
         J.rowptr_h[i + 1] = (int32_t)nnz;
     }
+    std::vector<int32_t> long_slots;
+    for (int64_t slot = 0; slot < nv; ++slot)
+        if (tptr[slot + 1] - tptr[slot] > kJacLongRow) long_slots.push_back((int32_t)slot);
+    J.n_long = (int64_t)long_slots.size();
     J.colidx_h.resize(nnz);
     for (int64_t i = 0; i < dim; ++i) std::copy(rows[i].begin(), rows[i].end(), J.colidx_h.begin() + J.rowptr_h[i]);
     J.nnz = nnz;
@@ -284,7 +375,10 @@ int build_plan(nd_handle* h) {
         (err = cudaMemcpy(J.rowptr, J.rowptr_h.data(), (dim + 1) * sizeof(int32_t), cudaMemcpyHostToDevice)) !=
             cudaSuccess ||
         (nnz > 0 &&
-         (err = cudaMemcpy(J.colidx, J.colidx_h.data(), nnz * sizeof(int32_t), cudaMemcpyHostToDevice)) != cudaSuccess))
+         (err = cudaMemcpy(J.colidx, J.colidx_h.data(), nnz * sizeof(int32_t), cudaMemcpyHostToDevice)) != cudaSuccess) ||
+        (err = cudaMalloc(&J.long_slots, std::max<int64_t>(J.n_long, 1) * sizeof(int32_t))) != cudaSuccess ||
+        (J.n_long > 0 && (err = cudaMemcpy(J.long_slots, long_slots.data(), J.n_long * sizeof(int32_t),
+                                           cudaMemcpyHostToDevice)) != cudaSuccess))
         return cuda_fail(err, "nd_jacobian: pattern upload");
     J.ready = true;
     return ND_OK;
@@ -311,6 +405,9 @@ cudaError_t launch_values(nd_handle* h, void* values, const void* u, const void*
     cudaError_t err = cudaMemsetAsync(values, 0, std::max<int64_t>(J.nnz, 1) * sizeof(T), s);
     if (err != cudaSuccess) return err;
     jac_vertex_kernel<T><<<(unsigned)((b.nv + kJacBlock - 1) / kJacBlock), kJacBlock, 0, s>>>(a);
+    if (J.n_long > 0)
+        jac_long_row_kernel<T><<<(unsigned)((J.n_long * 32 + kJacBlock - 1) / kJacBlock), kJacBlock, 0, s>>>(
+            a, J.long_slots, J.n_long);
     if (b.ne > 0) jac_ode_edge_kernel<T><<<(unsigned)((b.ne + kJacBlock - 1) / kJacBlock), kJacBlock, 0, s>>>(a);
     return cudaGetLastError();
 }
@@ -321,6 +418,7 @@ void free_jacobian(JacPlan* j) {
     if (j->view.enabled) free_batched(&j->view);
     cudaFree(j->rowptr);
     cudaFree(j->colidx);
+    cudaFree(j->long_slots);
     *j = JacPlan{};
 }
 

@@ -3,6 +3,7 @@
     python -m nd_gb300.benchmarks warmstart [--train 20000 --test 2000 --nv 2000]
     python -m nd_gb300.benchmarks ensemble  [--instances 4096]
     python -m nd_gb300.benchmarks swing     [--nv 100000]
+    python -m nd_gb300.benchmarks jacobian  [--nv 1000000]
 
 Each prints one JSON object.  All inputs are seeded synthetic instances of the stated
 shapes; no dataset is read.
@@ -234,9 +235,56 @@ def swing(nv=100000, m=2, t_end=20.0, steps=200, seed=0):
     return out
 
 
+def jacobian(nv=1_000_000, m=2, seed=0, steps=100):
+    """Swing network on BA(nv, m): build time of the Jacobian pattern (host, once per
+    network), device time of the analytic values, and of one JVP for comparison."""
+    import torch
+
+    import nd_gb300 as nd
+    from nd_gb300 import warmstart as W
+    g = nd.barabasi_albert(nv, m, seed=seed + 1)
+    P, K = W.swing_instances(g, 1, seed + 2)
+    p = torch.from_numpy(W.swing_flat_params(g, P, K)).cuda()
+    net = nd.Network(g, nd.kuramoto_second(), nd.static_line())
+    nw = nd.adapt(net, torch.float64)
+    rng = np.random.default_rng(seed + 3)
+    u = torch.from_numpy(rng.normal(size=net.dim)).cuda()
+    t0 = time.perf_counter()
+    rowptr, colidx = nd.jacobian_pattern(nw)
+    t_pattern = time.perf_counter() - t0
+    values = torch.empty(len(colidx), dtype=torch.float64, device="cuda")
+    lib = nw._lib
+    import ctypes as C
+    from nd_gb300 import _capi as capi
+    stream = torch.cuda.current_stream()
+
+    def values_call():
+        capi.check(lib.nd_jacobian(nw.handle, capi.ND_F64, values.data_ptr(), u.data_ptr(), p.data_ptr(), 0.0,
+                                   C.c_void_p(stream.cuda_stream)))
+
+    jv = torch.empty_like(u)
+    out = {"workload": f"swing on Barabasi-Albert N={nv}, m={m}", "dim": net.dim, "nnz": int(len(colidx)),
+           "pattern_build_s": t_pattern}
+    for name, fn in (("values", values_call), ("jvp", lambda: nd.jvp(nw, jv, u, p, u))):
+        for _ in range(3):
+            fn()
+        _sync()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(steps):
+            fn()
+        b.record()
+        b.synchronize()
+        out[f"{name}_us"] = 1e3 * a.elapsed_time(b) / steps
+    # bytes of one values call: memset + write of the values, the pattern and structure reads
+    out["values_bytes"] = int(8 * 2 * len(colidx) + 4 * len(colidx) + 4 * (net.dim + 1) + 16 * g.ne)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("which", choices=["warmstart", "ensemble", "swing"])
+    ap.add_argument("which", choices=["warmstart", "ensemble", "swing", "jacobian"])
     ap.add_argument("--train", type=int, default=20000)
     ap.add_argument("--test", type=int, default=2000)
     ap.add_argument("--nv", type=int, default=None)
@@ -249,6 +297,8 @@ def main():
         r = warmstart(a.train, a.test, a.nv or 2000, epochs=a.epochs)
     elif a.which == "ensemble":
         r = ensemble(a.instances, baseline_sample=a.sample, t_end=a.t_end)
+    elif a.which == "jacobian":
+        r = jacobian(a.nv or 1_000_000)
     else:
         r = swing(a.nv or 100000)
     print(json.dumps(r), flush=True)
