@@ -449,10 +449,10 @@ def run_gb300(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
-# The reference's benchmark cases (benchmark/benchmark_cases.jl:20-66) at their largest N.
+# The reference's benchmark cases (benchmark/benchmark_cases.jl:20-102) at their largest N.
 # Graphs.jl's watts_strogatz(N, 3, 0.8) links div(3, 2) = 1 ring neighbour per side before
-# rewiring, which is k = 2 here.  The powergrid cases need mass-matrix (DAE) vertices and
-# the pi-line edge, which the GPU library does not have.
+# rewiring, which is k = 2 here.  powergrid_inhomogeneous_pq gives every PQ bus its own
+# component (its own batch), beyond the batch table of the GPU path.
 def _case_networks(N, name):
     import nd_gb300 as nd
     if name == "diffusion_static_edge":
@@ -462,13 +462,16 @@ def _case_networks(N, name):
     g = nd.watts_strogatz(N, 2, 0.8, seed=1)
     if name == "kuramoto_homogeneous":
         return g, nd.kuramoto_vertex_2d(), nd.static_kuramoto_edge()
+    if name == "powergrid":
+        kinds = np.random.default_rng(1).permutation(np.repeat([0, 1], N // 2))
+        return g, [nd.pqnode() if k == 0 else nd.generator() for k in kinds], nd.piline()
     kinds = np.random.default_rng(1).permutation(np.repeat([0, 1], N // 2))
     return g, [nd.kuramoto_vertex_1d() if k == 0 else nd.kuramoto_vertex_2d() for k in kinds], \
         nd.static_kuramoto_edge()
 
 
 CASES = (("diffusion_static_edge", 3000), ("diffusion_ode_edge", 3000), ("kuramoto_homogeneous", 100_000),
-         ("kuramoto_heterogeneous", 100_000))
+         ("kuramoto_heterogeneous", 100_000), ("powergrid", 100_000))
 
 
 def run_cases(args):
@@ -489,6 +492,12 @@ def run_cases(args):
         rng = np.random.default_rng(2)
         u = rng.normal(size=net.dim)
         p = rng.uniform(0.5, 1.5, size=net.pdim)
+        if name == "powergrid":  # line and machine data in the ranges of per-unit grid models
+            p = net.pflat(vertex={"P": rng.uniform(-1, 1, g.nv), "Q": rng.uniform(-1, 1, g.nv), "H": 5.0,
+                                  "D": 0.1, "Ω": 2 * np.pi * 50, "E_f": 1.0, "T_d_dash": 7.0, "T_q_dash": 0.5,
+                                  "X_d_dash": 0.3, "X_q_dash": 0.6, "X_d": 1.8, "X_q": 1.7},
+                          edge={"L": 1e-3, "R": 0.05, "C1": 1e-5, "C2": 1e-5})
+            u = 1.0 + 0.1 * rng.normal(size=net.dim)
         line = {"case": name, "N": N, "ne": g.ne, "dim": net.dim, "pdim": net.pdim,
                 "vertex_batches": len(net.vertex_batches), "edge_batches": len(net.edge_batches)}
         for tag, dt, s in (("f64", torch.float64, 8), ("f32", torch.float32, 4)):

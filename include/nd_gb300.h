@@ -51,8 +51,13 @@ enum nd_vertex_kind {
     ND_V_DIFFUSION = 1, /* diffusionvertex!  dv = Σe                 test/ComponentLibrary.jl:42-46   dim 1, pdim 0          */
     ND_V_KURAMOTO = 2,  /* kuramoto_vertex!  dθ = ω + Σe             test/ComponentLibrary.jl:69-72   dim 1, pdim 1 (ω)      */
     ND_V_SWING = 3,     /* kuramoto_inertia! dθ = ω, dω = (Pm-Dω+Σe)/M test/ComponentLibrary.jl:59-67 dim 2, pdim 3 (M,D,Pm) */
-    ND_V_SWING_UNIT = 4 /* kuramoto_inertia! of the benchmarks: dθ = ω, dω = (P - 1.0ω) + Σe
+    ND_V_SWING_UNIT = 4, /* kuramoto_inertia! of the benchmarks: dθ = ω, dω = (P - 1.0ω) + Σe
                            benchmark/benchmark_models.jl:37-42                                 dim 2, pdim 1 (P)      */
+    /* Power-grid vertices: complex voltage output (StateMask(1:2)), complex current input. */
+    ND_V_PQ = 5,        /* pq!  algebraic PQ bus (mass matrix 0): du = S / conj(i), S = P + iQ
+                           benchmark/benchmark_models.jl:65-74                                 dim 2, pdim 2 (P,Q)    */
+    ND_V_GENERATOR = 6  /* gen!  generator with states (u_r, u_i, θ, ω)
+                           benchmark/benchmark_models.jl:76-111                                dim 4, pdim 11         */
 };
 enum nd_edge_kind {
     ND_E_DIFFUSION = 1,      /* diffusionedge!   e = w·(vs-vd)   test/ComponentLibrary.jl:8-13   pdim 1 (w) */
@@ -63,9 +68,14 @@ enum nd_edge_kind {
      * y_dst = e1, y_src = e2. */
     ND_E_DIFFUSION_ODE = 4,      /* diffusion_dedge!  de1 = 1/τ·(sin(vs-vd) - e1), de2 = 1/τ·(sin(vd-vs) - e2)
                                     test/ComponentLibrary.jl:30-40                  dim 2, pdim 1 (τ)  */
-    ND_E_DIFFUSION_ODE_FIXED = 5 /* the same with the rate fixed: de = 100.0·(sin(..) - e)
+    ND_E_DIFFUSION_ODE_FIXED = 5, /* the same with the rate fixed: de = 100.0·(sin(..) - e)
                                     benchmark/benchmark_models.jl:11-16             dim 2, pdim 0      */
+    ND_E_PILINE = 6               /* piline!  two-sided π-line currents (complex outputs), coupling
+                                    ND_FIDUCIAL   benchmark/benchmark_models.jl:46-63  pdim 4 (L,R,C1,C2) */
 };
+/* All vertex models of a network share one output dimension, and all edge models one
+ * (src/construction.jl:98-106): 1 for kinds 1-5 / 1-3, 2 (a complex value) for
+ * ND_V_PQ, ND_V_GENERATOR and ND_E_PILINE.  A mix is ND_ERR_ARG. */
 /* Output wrapper of the edge (src/component_functions.jl:101-203):
  *   ND_ANTISYMMETRIC  y_dst = g(...), y_src = -y_dst          (:117-126)
  *   ND_SYMMETRIC      y_dst = g(...), y_src = y_dst           (:142-151)

@@ -270,6 +270,66 @@ __global__ void __launch_bounds__(kRowBlock) batched_row_kernel(BatchedKArgs a, 
     }
 }
 
+// ---- output dimension 2: the power-grid networks (complex voltages and currents) ----------
+// The same two launches with complex values: y2 holds (y_src, y_dst) as two complex numbers
+// per edge position, a term index t names the complex number y2[t], and a row's real and
+// imaginary parts are summed side by side in the sequential order, one thread per row.
+template <typename T>
+__global__ void __launch_bounds__(kBlock) batched_edge_kernel2(BatchedKArgs a) {
+    using V2 = typename Vec2<T>::type;
+    const T* __restrict__ u = static_cast<const T*>(a.u);
+    const T* __restrict__ p = static_cast<const T*>(a.p);
+    V2* __restrict__ y2 = static_cast<V2*>(a.y2);
+    for (int64_t k = (int64_t)blockIdx.x * kBlock + threadIdx.x; k < a.ne; k += (int64_t)gridDim.x * kBlock) {
+        const int b = find_batch(a.eb, k);  // every edge batch is a pi-line batch
+        const int64_t q = __ldg(&a.eb->p0[b]) + 4 * (k - __ldg(&a.eb->pos0[b]));
+        const int2 uv = __ldg(a.eu + k);
+        const Cx<T> vs = {__ldg(u + uv.x), __ldg(u + uv.x + 1)}, vd = {__ldg(u + uv.y), __ldg(u + uv.y + 1)};
+        Cx<T> ys, yd;
+        piline_g<T>(vs, vd, __ldg(p + q), __ldg(p + q + 1), __ldg(p + q + 2), __ldg(p + q + 3), ys, yd);
+        V2 a0, a1;
+        a0.x = ys.r;
+        a0.y = ys.i;
+        a1.x = yd.r;
+        a1.y = yd.i;
+        y2[2 * k] = a0;
+        y2[2 * k + 1] = a1;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRowBlock) batched_row_kernel2(BatchedKArgs a) {
+    using A = Arith<T>;
+    using V2 = typename Vec2<T>::type;
+    const V2* __restrict__ y2 = static_cast<const V2*>(a.y2);
+    const int64_t slot = (int64_t)blockIdx.x * kRowBlock + threadIdx.x;
+    if (slot >= a.nv) return;
+    const uint32_t t0 = __ldg(a.tptr + slot);
+    const int n = (int)(__ldg(a.tptr + slot + 1) - t0);
+    T re = T(0), im = T(0);
+    for (int j = 0; j < n; ++j) {
+        const V2 t = y2[__ldg(a.tidx + t0 + j)];
+        if (j == 0) {  // the reference's zero start folded into the first term (0 + t is t)
+            re = A::add(T(0), t.x);
+            im = A::add(T(0), t.y);
+        } else {
+            re = A::add(re, t.x);
+            im = A::add(im, t.y);
+        }
+    }
+    const int64_t pos = __ldg(a.slot_vpos + slot);
+    const int b = find_batch(a.vb, pos);
+    const int64_t r = pos - __ldg(&a.vb->pos0[b]);
+    const int64_t s0 = __ldg(&a.vb->s0[b]), q0 = __ldg(&a.vb->p0[b]);
+    T* du = static_cast<T*>(a.du);
+    const T* u = static_cast<const T*>(a.u);
+    const T* p = static_cast<const T*>(a.p);
+    if (__ldg(&a.vb->kind[b]) == ND_V_PQ)
+        vertex_f2_at<T, ND_V_PQ>(du, u, p, s0 + 2 * r, q0 + 2 * r, {re, im});
+    else
+        vertex_f2_at<T, ND_V_GENERATOR>(du, u, p, s0 + 4 * r, q0 + 11 * r, {re, im});
+}
+
 template <typename T>
 cudaError_t launch_typed(const BatchedNet& b, void* du, const void* u, const void* p, int mode, cudaStream_t s,
                          int phases) {
@@ -288,6 +348,15 @@ cudaError_t launch_typed(const BatchedNet& b, void* du, const void* u, const voi
     a.slot_vpos = b.slot_vpos;
     a.y2 = b.y2;
     a.mode = mode;
+    if (b.depth == 2) {
+        if ((phases & kPhaseEdge) && b.ne > 0) {
+            const int64_t blocks = std::min<int64_t>((b.ne + kBlock - 1) / kBlock, int64_t(1) << 20);
+            batched_edge_kernel2<T><<<(unsigned)blocks, kBlock, 0, s>>>(a);
+        }
+        if (phases & kPhaseRow)
+            batched_row_kernel2<T><<<(unsigned)((b.nv + kRowBlock - 1) / kRowBlock), kRowBlock, 0, s>>>(a);
+        return cudaGetLastError();
+    }
     if ((phases & kPhaseEdge) && b.ne > 0) {
         const int64_t blocks = std::min<int64_t>((b.ne + kBlock - 1) / kBlock, int64_t(1) << 20);
         batched_edge_kernel<T><<<(unsigned)blocks, kBlock, 0, s>>>(a);
@@ -307,10 +376,12 @@ bool ode_kind(int ek) { return ek == ND_E_DIFFUSION_ODE || ek == ND_E_DIFFUSION_
 
 // Is (kind, coupling) an edge component of the library?
 int check_edge_component(int ek, int coupling) {
-    if (!static_kind(ek) && !ode_kind(ek))
+    if (!static_kind(ek) && !ode_kind(ek) && ek != ND_E_PILINE)
         return fail(ND_ERR_UNSUPPORTED_COMPONENT,
                     "edge model is not in the GB300 component library (diffusion, unit diffusion, kuramoto / "
-                    "static line, diffusion ODE edge); no CPU fallback exists");
+                    "static line, diffusion ODE edge, pi-line); no CPU fallback exists");
+    if (ek == ND_E_PILINE && coupling != ND_FIDUCIAL)
+        return fail(ND_ERR_UNSUPPORTED_COMPONENT, "the pi-line edge has a two-sided output function (ND_FIDUCIAL)");
     if (ode_kind(ek) && coupling != ND_FIDUCIAL)
         return fail(ND_ERR_UNSUPPORTED_COMPONENT, "the diffusion ODE edges have Fiducial(dst=1, src=2) outputs");
     if (static_kind(ek) && coupling != ND_ANTISYMMETRIC && coupling != ND_SYMMETRIC && coupling != ND_DIRECTED &&
@@ -348,16 +419,24 @@ int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out) {
     if (2 * ne > (int64_t)INT32_MAX) return fail(ND_ERR_UNSUPPORTED, "more than 2^30-1 edges in a batched network");
     for (int b = 0; b < nvb; ++b) {
         const nd_batch& vb = d->vertex_batches[b];
-        if (vb.kind < ND_V_DIFFUSION || vb.kind > ND_V_SWING_UNIT)
+        if (vb.kind < ND_V_DIFFUSION || vb.kind > ND_V_GENERATOR)
             return fail(ND_ERR_UNSUPPORTED_COMPONENT,
                         "vertex model is not in the GB300 component library (diffusion, kuramoto first order, "
-                        "swing, benchmark swing); no CPU fallback exists");
+                        "swing, benchmark swing, PQ bus, generator); no CPU fallback exists");
         if (vb.coupling != 0) return fail(ND_ERR_ARG, "vertex batches take coupling 0");
     }
     for (int b = 0; b < neb; ++b) {
         const int rc = check_edge_component(d->edge_batches[b].kind, d->edge_batches[b].coupling);
         if (rc != ND_OK) return rc;
     }
+    // one output dimension for all vertex models and all edge models (src/construction.jl:98-106)
+    const int depth = vertex_outdim(d->vertex_batches[0].kind);
+    for (int b = 0; b < nvb; ++b)
+        if (vertex_outdim(d->vertex_batches[b].kind) != depth)
+            return fail(ND_ERR_ARG, "All vertex models must have the same output dimension!");
+    for (int b = 0; b < neb; ++b)
+        if (edge_outdim(d->edge_batches[b].kind) != depth)
+            return fail(ND_ERR_ARG, "All edge models must have the same output dimension as the vertex models!");
     std::vector<int64_t> vcount(nvb, 0), ecount(std::max(neb, 1), 0);
     for (int64_t v = 0; v < nv; ++v) {
         const int32_t b = d->vertex_batch[v];
@@ -479,6 +558,7 @@ int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out) {
     bn.dim = st;
     bn.pdim = par;
     bn.max_degree = (int32_t)maxdeg;
+    bn.depth = depth;
     bn.n_warp_rows = (int64_t)longr.size();
     auto upload = [&](void** dptr, const void* hptr, size_t bytes) -> cudaError_t {
         cudaError_t err = cudaMalloc(dptr, std::max<size_t>(bytes, 16));
@@ -493,7 +573,7 @@ int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out) {
         (err = upload((void**)&bn.tptr, tptr.data(), tptr.size() * sizeof(uint32_t))) != cudaSuccess ||
         (err = upload((void**)&bn.tidx, tidx.data(), tidx.size() * sizeof(int32_t))) != cudaSuccess ||
         (err = upload((void**)&bn.slot_vpos, slot_vpos.data(), slot_vpos.size() * sizeof(int32_t))) != cudaSuccess ||
-        (elem > 0 && (err = cudaMalloc(&bn.y2, std::max<size_t>((size_t)2 * ne * elem, 16))) != cudaSuccess)) {
+        (elem > 0 && (err = cudaMalloc(&bn.y2, std::max<size_t>((size_t)2 * depth * ne * elem, 16))) != cudaSuccess)) {
         free_batched(&bn);
         return cuda_fail(err, "upload of the batched network");
     }

@@ -363,7 +363,7 @@ int nd_create(const nd_network_desc* desc, int dtype, nd_handle** out) {
     if (dtype != ND_F32 && dtype != ND_F64)
         return fail(ND_ERR_DTYPE, "nd_create: dtype must be ND_F32 or ND_F64 "
                                   "(adapt the network with CuArray{Float32} or CuArray{Float64})");
-    if (desc->vertex_kind < ND_V_DIFFUSION || desc->vertex_kind > ND_V_SWING_UNIT)
+    if (desc->vertex_kind < ND_V_DIFFUSION || desc->vertex_kind > ND_V_GENERATOR)
         return fail(ND_ERR_UNSUPPORTED_COMPONENT,
                     "vertex model is not in the GB300 component library "
                     "(diffusion, kuramoto first order, swing); no CPU fallback exists");

@@ -159,4 +159,105 @@ __device__ __forceinline__ void ode_edge_f(T rate, T vs, T vd, T e1, T e2, T& de
     de2 = A::mul(rate, A::sub(-s, e2));
 }
 
+// ---- power-grid components: complex values (outputs of dimension 2) ------------------------
+// Complex arithmetic as Julia defines it: the product (ac - bd, ad + bc) and division by
+// the robust method of Baudin & Smith ("A Robust Complex Division in Scilab", 2012, with
+// their improved r = 0 / br = 0 branches), which Julia's Base uses.  The method's range
+// scaling only acts near the overflow / underflow thresholds and is left out.
+template <typename T>
+struct Cx {
+    T r, i;
+};
+
+template <typename T>
+__device__ __forceinline__ Cx<T> cmul(Cx<T> a, Cx<T> b) {
+    using A = Arith<T>;
+    return {A::sub(A::mul(a.r, b.r), A::mul(a.i, b.i)), A::add(A::mul(a.r, b.i), A::mul(a.i, b.r))};
+}
+
+template <typename T>
+__device__ __forceinline__ T cdiv_part(T a, T b, T c, T d, T r, T t) {
+    using A = Arith<T>;
+    if (r != T(0)) {
+        const T br = A::mul(b, r);
+        return br != T(0) ? A::mul(A::add(a, br), t) : A::add(A::mul(a, t), A::mul(A::mul(b, t), r));
+    }
+    return A::mul(A::add(a, A::mul(d, A::div(b, c))), t);
+}
+
+template <typename T>
+__device__ __forceinline__ Cx<T> cdiv(Cx<T> x, Cx<T> y) {
+    using A = Arith<T>;
+    T a = x.r, b = x.i, c = y.r, d = y.i;
+    const bool swap = !(fabs(d) <= fabs(c));
+    if (swap) {
+        T t0 = a;
+        a = b;
+        b = t0;
+        t0 = c;
+        c = d;
+        d = t0;
+    }
+    const T r = A::div(d, c);
+    const T t = A::div(T(1), A::add(c, A::mul(d, r)));
+    const T p = cdiv_part<T>(a, b, c, d, r, t);
+    const T q = cdiv_part<T>(b, -a, c, d, r, t);
+    return {p, swap ? -q : q};
+}
+
+// 2π·50 as Julia evaluates 2π*50 in Float64
+constexpr double kPiLineOmega = 314.1592653589793;
+
+// piline! (benchmark/benchmark_models.jl:46-63): currents out of a π-line with series
+// impedance R + iωL and shunt capacitances C1, C2, from the complex source / destination
+// voltages.  Outputs y_src = -isrc, y_dst = -idst.
+template <typename T>
+__device__ __forceinline__ void piline_g(Cx<T> vs, Cx<T> vd, T L, T R, T C1, T C2, Cx<T>& ysrc, Cx<T>& ydst) {
+    using A = Arith<T>;
+    const T w = T(kPiLineOmega);
+    const Cx<T> imain = cdiv<T>({A::sub(vs.r, vd.r), A::sub(vs.i, vd.i)}, {R, A::mul(w, L)});  // R + im*ω*L
+    const Cx<T> ic1 = {A::mul(A::mul(-vs.i, w), C1), A::mul(A::mul(vs.r, w), C1)};        // Vsrc*im*ω*C1
+    const Cx<T> ic2 = {A::mul(A::mul(-vd.i, w), C2), A::mul(A::mul(vd.r, w), C2)};
+    // isrc = -(imain + iC1), idst = imain - iC2; the outputs are their negatives
+    ysrc = {A::add(imain.r, ic1.r), A::add(imain.i, ic1.i)};
+    ydst = {-A::sub(imain.r, ic2.r), -A::sub(imain.i, ic2.i)};
+}
+
+// Vertex f of the power-grid vertices with the aggregated complex current `in`.
+//   pq!   (benchmark_models.jl:65-73)  algebraic bus: du = S / conj(i), S = P + iQ
+//   gen!  (benchmark_models.jl:76-109) 4-state generator (u_r, u_i, θ, ω)
+template <typename T, int VK>
+__device__ __forceinline__ void vertex_f2_at(T* __restrict__ du, const T* __restrict__ u, const T* __restrict__ p,
+                                             int64_t s, int64_t q, Cx<T> in) {
+    using A = Arith<T>;
+    if constexpr (VK == ND_V_PQ) {
+        const Cx<T> uc = cdiv<T>({__ldg(p + q), __ldg(p + q + 1)}, {in.r, -in.i});
+        du[s] = uc.r;
+        du[s + 1] = uc.i;
+    } else {
+        const T H = __ldg(p + q), P = __ldg(p + q + 1), D = __ldg(p + q + 2), Om = __ldg(p + q + 3);
+        const T E_f = __ldg(p + q + 4), T_d_dash = __ldg(p + q + 5), T_q_dash = __ldg(p + q + 6);
+        const T X_q_dash = __ldg(p + q + 7), X_d_dash = __ldg(p + q + 8), X_d = __ldg(p + q + 9);
+        const T X_q = __ldg(p + q + 10);
+        const T Om_H = A::div(Om, A::mul(T(2), H));
+        const Cx<T> uc = {u[s], u[s + 1]};
+        const T th = u[s + 2], w = u[s + 3];
+        const T ct = A::cos_phase(th), st = A::sin_phase(th);
+        const Cx<T> em = {ct, -st};                        // exp(-im*θ) = (cos θ, -sin θ)
+        const Cx<T> i_c = cmul<T>({-in.i, in.r}, em);     // (im*i)*exp(-im*θ)
+        const Cx<T> e_c = cmul<T>({-uc.i, uc.r}, em);     // (im*u)*exp(-im*θ)
+        const T pw = cmul<T>(uc, {in.r, -in.i}).r;        // real(u*conj(i))
+        const T de_d = A::mul(A::div(T(1), T_q_dash), A::add(-e_c.r, A::mul(A::sub(X_q, X_q_dash), i_c.i)));
+        const T de_q = A::mul(A::div(T(1), T_d_dash),
+                              A::add(A::sub(-e_c.i, A::mul(A::sub(X_d, X_d_dash), i_c.r)), E_f));
+        const Cx<T> t1 = cmul<T>({de_q, -de_d}, {ct, st}); // (-im*de_c)*exp(im*θ)
+        du[s] = A::add(t1.r, A::mul(-uc.i, w));            // + (u*im)*ω
+        du[s + 1] = A::add(t1.i, A::mul(uc.r, w));
+        du[s + 2] = w;
+        du[s + 3] = A::mul(A::sub(A::sub(A::sub(P, A::mul(D, w)), pw),
+                                  A::mul(A::mul(A::sub(X_q_dash, X_d_dash), i_c.r), i_c.i)),
+                           Om_H);
+    }
+}
+
 }  // namespace nd

@@ -32,12 +32,25 @@ struct __align__(8) Incidence {
 constexpr int32_t kSrcSideBit = int32_t(0x80000000u);
 
 // Dimensions of the library components.
-inline int vertex_dim(int vk) { return vk == ND_V_SWING || vk == ND_V_SWING_UNIT ? 2 : 1; }
+inline int vertex_dim(int vk) {
+    return vk == ND_V_GENERATOR ? 4 : (vk == ND_V_SWING || vk == ND_V_SWING_UNIT || vk == ND_V_PQ ? 2 : 1);
+}
 inline int vertex_pdim(int vk) {
-    return vk == ND_V_DIFFUSION ? 0 : (vk == ND_V_KURAMOTO || vk == ND_V_SWING_UNIT ? 1 : 3);
+    switch (vk) {
+        case ND_V_DIFFUSION: return 0;
+        case ND_V_KURAMOTO: case ND_V_SWING_UNIT: return 1;
+        case ND_V_SWING: return 3;
+        case ND_V_PQ: return 2;
+        default: return 11;  // ND_V_GENERATOR
+    }
 }
 inline int edge_dim(int ek) { return ek == ND_E_DIFFUSION_ODE || ek == ND_E_DIFFUSION_ODE_FIXED ? 2 : 0; }
-inline int edge_pdim(int ek) { return ek == ND_E_DIFFUSION_UNIT || ek == ND_E_DIFFUSION_ODE_FIXED ? 0 : 1; }
+inline int edge_pdim(int ek) {
+    return ek == ND_E_DIFFUSION_UNIT || ek == ND_E_DIFFUSION_ODE_FIXED ? 0 : (ek == ND_E_PILINE ? 4 : 1);
+}
+// output dimension (vdepth / edepth)
+inline int vertex_outdim(int vk) { return vk == ND_V_PQ || vk == ND_V_GENERATOR ? 2 : 1; }
+inline int edge_outdim(int ek) { return ek == ND_E_PILINE ? 2 : 1; }
 
 // Degree buckets.  Rows with degree <= kMediumMaxDeg are processed in windows: a block
 // evaluates all edge terms of up to kWindow rows / kWindowIncidences incidences in
@@ -181,12 +194,13 @@ struct BatchedNet {
     BatchTable* d_eb = nullptr;
     int64_t nv = 0, ne = 0, dim = 0, pdim = 0;
     int32_t max_degree = 0;
+    int32_t depth = 1;           // output dimension of vertices and edge sides (2: complex)
     int64_t n_warp_rows = 0;     // slots [0, n_warp_rows): the long rows, a warp per row
     int2* eu = nullptr;          // [ne] by edge position: u indices of the src / dst vertex outputs
     uint32_t* tptr = nullptr;    // [nv+1] by slot: range of the slot's terms in tidx
     int32_t* tidx = nullptr;     // [2ne] y2 indices of every row's terms, ascending
     int32_t* slot_vpos = nullptr;  // [nv] vertex position of each slot
-    void* y2 = nullptr;          // [2ne] scratch, element type of the handle
+    void* y2 = nullptr;          // [2ne·depth] scratch, element type of the handle
 };
 
 #ifdef __CUDACC__

@@ -306,6 +306,9 @@ int build_plan(nd_handle* h) {
         if (rc != ND_OK) return rc;
     }
     const BatchedNet& b = h->batched.enabled ? h->batched : J.view;
+    if (b.depth != 1)
+        return fail(ND_ERR_UNSUPPORTED, "nd_jacobian: networks with complex (two-dimensional) outputs, the "
+                                        "power-grid components, have no analytic Jacobian here");
     const int64_t nv = b.nv, ne = b.ne, dim = b.dim;
     std::vector<uint32_t> tptr(nv + 1);
     std::vector<int32_t> tidx((size_t)2 * ne), slot_vpos(nv);

@@ -27,12 +27,15 @@ ND_V_DIFFUSION = 1
 ND_V_KURAMOTO = 2
 ND_V_SWING = 3
 ND_V_SWING_UNIT = 4
+ND_V_PQ = 5
+ND_V_GENERATOR = 6
 
 ND_E_DIFFUSION = 1
 ND_E_DIFFUSION_UNIT = 2
 ND_E_KURAMOTO = 3
 ND_E_DIFFUSION_ODE = 4
 ND_E_DIFFUSION_ODE_FIXED = 5
+ND_E_PILINE = 6
 
 ND_ANTISYMMETRIC = 1
 ND_SYMMETRIC = 2

@@ -26,10 +26,8 @@ class VertexModel:
     kind: Optional[int] = None          # ND_V_* of the CUDA implementation, None = user function
     f: Optional[Callable] = None
     g: object = 1                       # StateMask(1): the first state is the output
-
-    @property
-    def outdim(self) -> int:
-        return 1
+    outdim: int = 1                     # StateMask(1:outdim)
+    mass_matrix: Optional[float] = None  # 0: algebraic states (the PQ bus); None: identity
 
 
 @dataclass
@@ -43,10 +41,7 @@ class EdgeModel:
     dim: int = 0                        # static edges: no states
     f: Optional[Callable] = None
     g: Optional[Callable] = None
-
-    @property
-    def outdim(self) -> int:
-        return 1
+    outdim: int = 1                     # per side
 
 
 # --- vertices (test/ComponentLibrary.jl) -------------------------------------------------
@@ -152,3 +147,30 @@ def Symmetric(m: EdgeModel) -> EdgeModel:
 def Directed(m: EdgeModel) -> EdgeModel:
     """y_dst = g(...), no output for the source (y_src = 0) (src/component_functions.jl:167-175)."""
     return _rewrap(m, "Directed")
+
+
+# --- power-grid components (benchmark/benchmark_models.jl:46-111) ----------------------------
+
+def piline() -> EdgeModel:
+    """piline!: π-line with series impedance R + iωL (ω = 2π·50) and shunt capacitances C1,
+    C2; two-sided complex current outputs (benchmark/benchmark_models.jl:46-63)."""
+    return EdgeModel("piline", pdim=4, psym=("L", "R", "C1", "C2"), pdef=(None, None, None, None),
+                     kind=capi.ND_E_PILINE, coupling="Fiducial", outdim=2)
+
+
+def pqnode() -> VertexModel:
+    """pq!: algebraic PQ bus, du = S / conj(i) with S = P + iQ, mass matrix 0
+    (benchmark/benchmark_models.jl:65-74)."""
+    return VertexModel("pqnode", dim=2, pdim=2, sym=("u_r", "u_i"), psym=("P", "Q"), pdef=(None, None),
+                       kind=capi.ND_V_PQ, outdim=2, mass_matrix=0.0)
+
+
+def generator() -> VertexModel:
+    """gen!: generator with states (u_r, u_i, θ, ω) and 11 parameters
+    (benchmark/benchmark_models.jl:76-111).  The parameter names are the reference's psym;
+    gen! itself unpacks the 8th and 9th parameters as X_q_dash, X_d_dash, and so does the
+    GPU implementation."""
+    return VertexModel("generator", dim=4, pdim=11, sym=("u_r", "u_i", "θ", "ω"),
+                       psym=("H", "P", "D", "Ω", "E_f", "T_d_dash", "T_q_dash", "X_d_dash", "X_q_dash", "X_d",
+                             "X_q"),
+                       pdef=(None,) * 11, kind=capi.ND_V_GENERATOR, outdim=2)

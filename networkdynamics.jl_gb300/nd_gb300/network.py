@@ -130,6 +130,11 @@ class Network:
                                      "a graph without edges needs the edge model passed as a single EdgeModel")
         _check_library(vms, "vertex")
         _check_library(ems, "edge")
+        # src/construction.jl:98-106
+        if len({m.outdim for m in vms}) != 1:
+            raise capi.ArgumentError(capi.ND_ERR_ARG, "All vertex models must have the same output dimension!")
+        if len({m.outdim for m in ems}) != 1:
+            raise capi.ArgumentError(capi.ND_ERR_ARG, "All edge models must have the same output dimension!")
         for m in ems:
             if m.coupling not in capi.COUPLINGS:
                 raise capi.UnsupportedComponentError(capi.ND_ERR_UNSUPPORTED_COMPONENT,

@@ -26,15 +26,31 @@
 #endif
 
 /* Component kinds and output wrappers: same numbering as the C ABI of the GB300 library. */
-enum { V_DIFFUSION = 1, V_KURAMOTO = 2, V_SWING = 3, V_SWING_UNIT = 4 };
-enum { E_DIFFUSION = 1, E_DIFFUSION_UNIT = 2, E_KURAMOTO = 3, E_DIFFUSION_ODE = 4, E_DIFFUSION_ODE_FIXED = 5 };
+enum { V_DIFFUSION = 1, V_KURAMOTO = 2, V_SWING = 3, V_SWING_UNIT = 4, V_PQ = 5, V_GENERATOR = 6 };
+enum { E_DIFFUSION = 1, E_DIFFUSION_UNIT = 2, E_KURAMOTO = 3, E_DIFFUSION_ODE = 4, E_DIFFUSION_ODE_FIXED = 5,
+       E_PILINE = 6 };
 enum { C_ANTISYMMETRIC = 1, C_SYMMETRIC = 2, C_DIRECTED = 3, C_FIDUCIAL = 4 };
 
-static int vdim(int vk) { return vk == V_SWING || vk == V_SWING_UNIT ? 2 : 1; }
-static int vpdim(int vk) { return vk == V_DIFFUSION ? 0 : (vk == V_KURAMOTO || vk == V_SWING_UNIT ? 1 : 3); }
+static int vdim(int vk) {
+    return vk == V_GENERATOR ? 4 : (vk == V_SWING || vk == V_SWING_UNIT || vk == V_PQ ? 2 : 1);
+}
+static int vpdim(int vk) {
+    switch (vk) {
+        case V_DIFFUSION: return 0;
+        case V_KURAMOTO: case V_SWING_UNIT: return 1;
+        case V_SWING: return 3;
+        case V_PQ: return 2;
+        default: return 11; /* generator */
+    }
+}
 static int is_ode_edge(int ek) { return ek == E_DIFFUSION_ODE || ek == E_DIFFUSION_ODE_FIXED; }
 static int edim(int ek) { return is_ode_edge(ek) ? 2 : 0; }
-static int epdim(int ek) { return ek == E_DIFFUSION_UNIT || ek == E_DIFFUSION_ODE_FIXED ? 0 : 1; }
+static int epdim(int ek) {
+    return ek == E_DIFFUSION_UNIT || ek == E_DIFFUSION_ODE_FIXED ? 0 : (ek == E_PILINE ? 4 : 1);
+}
+/* output dimension (vdepth / edepth): the power-grid components carry complex values */
+static int voutdim(int vk) { return vk == V_PQ || vk == V_GENERATOR ? 2 : 1; }
+static int eoutdim(int ek) { return ek == E_PILINE ? 2 : 1; }
 
 /*
  * Index layout of src/network_structure.jl:224-289, built as src/construction.jl:155-195
@@ -45,6 +61,7 @@ static int epdim(int ek) { return ek == E_DIFFUSION_UNIT || ek == E_DIFFUSION_OD
  */
 typedef struct {
     int64_t nv, ne;
+    int depth; /* output dimension of every vertex and edge side (vdepth = edepth) */
     const int64_t* src;
     const int64_t* dst;
     int32_t* vkind; /* [nv] kind of every vertex */
@@ -113,26 +130,37 @@ layout_t* nd_oracle_layout_new_batched(int64_t nv, int64_t ne, const int64_t* sr
     batch_order(ne, ebatch, neb, L->ebatch_order);
     const int32_t* vkind = L->vkind;
     const int32_t* ekind = L->ekind;
+    /* all vertex models and all edge models share one output dimension
+       (src/construction.jl:98-106); the library's depths agree across the two */
+    const int depth = nv > 0 ? voutdim(vkind[0]) : 1;
+    int bad = 0;
+    for (int64_t v = 0; v < nv; ++v) bad |= voutdim(vkind[v]) != depth;
+    for (int64_t e = 0; e < ne; ++e) bad |= eoutdim(ekind[e]) != depth;
+    L->depth = depth;
+    if (bad) {
+        nd_oracle_layout_free(L);
+        return NULL;
+    }
     int64_t dyn = 0, out = 0, par = 0, agg = 0;
     for (int64_t k = 0; k < nv; ++k) { /* register_vertices! */
         int64_t v = L->vbatch_order[k];
         L->v_data[v] = dyn;
         dyn += vdim(vkind[v]);
         L->v_out[v] = out;
-        out += 1;
+        out += depth;
         L->v_para[v] = par;
         par += vpdim(vkind[v]);
         L->v_aggr[v] = agg;
-        agg += 1;
+        agg += depth;
     }
     for (int64_t k = 0; k < ne; ++k) { /* register_edges!: states after every vertex state */
         int64_t e = L->ebatch_order[k];
         L->e_data[e] = dyn;
         dyn += edim(ekind[e]);
         L->e_out_src[e] = out;
-        out += 1;
+        out += depth;
         L->e_out_dst[e] = out;
-        out += 1;
+        out += depth;
         L->e_para[e] = par;
         par += epdim(ekind[e]);
     }
@@ -144,8 +172,10 @@ layout_t* nd_oracle_layout_new_batched(int64_t nv, int64_t ne, const int64_t* sr
     int64_t* full = (int64_t*)calloc((size_t)out + 1, sizeof(int64_t));
     for (int64_t k = 0; k < ne; ++k) {
         int64_t e = L->ebatch_order[k];
-        full[L->e_out_dst[e]] = L->v_aggr[dst[e]] + 1;
-        full[L->e_out_src[e]] = L->v_aggr[src[e]] + 1;
+        for (int j = 0; j < depth; ++j) {
+            full[L->e_out_dst[e] + j] = L->v_aggr[dst[e]] + j + 1;
+            full[L->e_out_src[e] + j] = L->v_aggr[src[e]] + j + 1;
+        }
     }
     int64_t first = -1, last = -1;
     for (int64_t i = 0; i < out; ++i)
@@ -167,18 +197,21 @@ layout_t* nd_oracle_layout_new_batched(int64_t nv, int64_t ne, const int64_t* sr
     /* _inv_aggregation_map (src/aggregators.jl:203-235): per vertex, its incident output
      * indices in edge-batch order, dst mapping before src mapping within an edge. */
     L->inv_ptr = (int64_t*)calloc((size_t)agg + 1, sizeof(int64_t));
-    L->inv_idx = (int64_t*)malloc(sizeof(int64_t) * (size_t)(2 * ne + 1));
-    for (int64_t e = 0; e < ne; ++e) {
-        L->inv_ptr[L->v_aggr[dst[e]] + 1]++;
-        L->inv_ptr[L->v_aggr[src[e]] + 1]++;
-    }
+    L->inv_idx = (int64_t*)malloc(sizeof(int64_t) * (size_t)(2 * depth * ne + 1));
+    for (int64_t e = 0; e < ne; ++e)
+        for (int j = 0; j < depth; ++j) {
+            L->inv_ptr[L->v_aggr[dst[e]] + j + 1]++;
+            L->inv_ptr[L->v_aggr[src[e]] + j + 1]++;
+        }
     for (int64_t a = 0; a < agg; ++a) L->inv_ptr[a + 1] += L->inv_ptr[a];
     int64_t* fill = (int64_t*)malloc(sizeof(int64_t) * ((size_t)agg + 1));
     memcpy(fill, L->inv_ptr, sizeof(int64_t) * ((size_t)agg + 1));
     for (int64_t k = 0; k < ne; ++k) {
         int64_t e = L->ebatch_order[k];
-        L->inv_idx[fill[L->v_aggr[dst[e]]]++] = L->e_out_dst[e];
-        L->inv_idx[fill[L->v_aggr[src[e]]]++] = L->e_out_src[e];
+        for (int j = 0; j < depth; ++j) {
+            L->inv_idx[fill[L->v_aggr[dst[e]] + j]++] = L->e_out_dst[e] + j;
+            L->inv_idx[fill[L->v_aggr[src[e]] + j]++] = L->e_out_src[e] + j;
+        }
     }
     free(fill);
     return L;
@@ -203,7 +236,7 @@ layout_t* nd_oracle_layout_new(int64_t nv, int64_t ne, const int64_t* src, const
         while (b < neb && ek[b] != ekind[e]) ++b;
         if (b == neb && neb < 16) {
             ek[neb] = ekind[e];
-            ec[neb++] = C_ANTISYMMETRIC;
+            ec[neb++] = ekind[e] == E_PILINE ? C_FIDUCIAL : C_ANTISYMMETRIC;
         }
         eb[e] = b;
     }
@@ -240,6 +273,9 @@ int64_t nd_oracle_v_data(const layout_t* L, int64_t v) { return L->v_data[v]; }
 int64_t nd_oracle_v_para(const layout_t* L, int64_t v) { return L->v_para[v]; }
 int64_t nd_oracle_e_para(const layout_t* L, int64_t e) { return L->e_para[e]; }
 int64_t nd_oracle_e_data(const layout_t* L, int64_t e) { return L->e_data[e]; }
+int nd_oracle_depth(const layout_t* L) { return L->depth; }
+int64_t nd_oracle_n_out(const layout_t* L) { return L->lastidx_out; }
+int64_t nd_oracle_n_aggr(const layout_t* L) { return L->lastidx_aggr; }
 
 /*
  * The RHS, once per precision.  Steps and line references follow src/coreloop.jl.
@@ -262,14 +298,61 @@ int64_t nd_oracle_e_data(const layout_t* L, int64_t e) { return L->e_data[e]; }
  *   kuramoto_inertia! (benchmarks) dv1 = v2; dv2 = P - 1.0*v2; dv2 += esum
  *                    benchmark_models.jl:37-42 (the literal 1.0 is a Float64, so for
  *                    Float32 data P - 1.0*v2 is computed in double and rounded on store)
+ * Power-grid components (outputs and inputs of dimension 2, a complex number):
+ *   piline!          two-sided π-line currents                   benchmark_models.jl:46-63
+ *   pq!              algebraic PQ bus: du = S / conj(i)          :65-73
+ *   gen!             4-state generator                           :76-109
+ * Complex arithmetic follows Julia's definitions operation by operation: the product
+ * (ac - bd, ad + bc), and division by the robust method of Baudin & Smith ("A Robust
+ * Complex Division in Scilab", 2012, with their improved r = 0 / br = 0 branches) that
+ * Julia's Base uses; its range scaling only acts near the overflow / underflow thresholds,
+ * which these models never reach, and is left out.
  */
-#define DEFINE_ORACLE_RHS(T, SFX, SIN)                                                              \
+#define DEFINE_COMPLEX(T, SFX)                                                                      \
+    static inline void cdiv2_##SFX(T a, T b, T c, T d, T r, T t, T* out) {                         \
+        if (r != 0) {                                                                               \
+            T br = b * r;                                                                           \
+            *out = br != 0 ? (a + br) * t : a * t + (b * t) * r;                                    \
+        } else {                                                                                    \
+            *out = (a + d * (b / c)) * t;                                                           \
+        }                                                                                           \
+    }                                                                                               \
+    static inline void cdiv1_##SFX(T a, T b, T c, T d, T* p, T* q) {                               \
+        T r = d / c;                                                                                \
+        T t = (T)1 / (c + d * r);                                                                   \
+        cdiv2_##SFX(a, b, c, d, r, t, p);                                                           \
+        cdiv2_##SFX(b, -a, c, d, r, t, q);                                                          \
+    }                                                                                               \
+    /* (a + bi) / (c + di) */                                                                       \
+    static inline void cdiv_##SFX(T a, T b, T c, T d, T* re, T* im) {                              \
+        T p, q;                                                                                     \
+        if (fabs((double)d) <= fabs((double)c)) {                                                   \
+            cdiv1_##SFX(a, b, c, d, &p, &q);                                                        \
+        } else {                                                                                    \
+            cdiv1_##SFX(b, a, d, c, &p, &q);                                                        \
+            q = -q;                                                                                 \
+        }                                                                                           \
+        *re = p;                                                                                    \
+        *im = q;                                                                                    \
+    }                                                                                               \
+    static inline void cmul_##SFX(T a, T b, T c, T d, T* re, T* im) {                              \
+        *re = a * c - b * d;                                                                        \
+        *im = a * d + b * c;                                                                        \
+    }
+DEFINE_COMPLEX(double, f64)
+DEFINE_COMPLEX(float, f32)
+
+/* 2π·50 as Julia evaluates 2π*50 in Float64 */
+#define PILINE_OMEGA 314.1592653589793
+
+#define DEFINE_ORACLE_RHS(T, SFX, SIN, COS)                                                              \
     static inline T edge_g_##SFX(int ek, T vs, T vd, const T* pe) {                                \
         if (ek == E_DIFFUSION) return pe[0] * (vs - vd);                                            \
         if (ek == E_DIFFUSION_UNIT) return vs - vd;                                                 \
         return pe[0] * SIN(vs - vd);                                                                \
     }                                                                                               \
-    static inline void vertex_f_##SFX(int vk, T* du, const T* u, const T* pv, T acc) {             \
+    static inline void vertex_f_##SFX(int vk, T* du, const T* u, const T* pv, const T* in) {       \
+        T acc = in[0];                                                                              \
         if (vk == V_DIFFUSION) {                                                                    \
             du[0] = acc;                                                                            \
         } else if (vk == V_KURAMOTO) {                                                              \
@@ -278,10 +361,30 @@ int64_t nd_oracle_e_data(const layout_t* L, int64_t e) { return L->e_data[e]; }
             T M = pv[0], D = pv[1], Pm = pv[2];                                                     \
             du[0] = u[1];                                                                           \
             du[1] = (T)1 / M * (Pm - D * u[1] + acc);                                               \
-        } else {                                                                                    \
+        } else if (vk == V_SWING_UNIT) {                                                            \
             du[0] = u[1];                                                                           \
             du[1] = (T)((double)pv[0] - 1.0 * (double)u[1]);                                       \
             du[1] = du[1] + acc;                                                                    \
+        } else if (vk == V_PQ) { /* uc = S / conj(ic) */                                            \
+            cdiv_##SFX(pv[0], pv[1], in[0], -in[1], &du[0], &du[1]);                                \
+        } else { /* gen! */                                                                         \
+            T H = pv[0], P = pv[1], D = pv[2], Om = pv[3], E_f = pv[4], T_d_dash = pv[5];           \
+            T T_q_dash = pv[6], X_q_dash = pv[7], X_d_dash = pv[8], X_d = pv[9], X_q = pv[10];      \
+            T Om_H = Om / ((T)2 * H);                                                               \
+            T ir = in[0], ii = in[1], ur = u[0], ui = u[1], th = u[2], w = u[3];                    \
+            T c = COS(-th), sn = SIN(-th); /* exp(-im*θ): exp(±0) = 1 times cis(-θ) */               \
+            T ic_r, ic_i, ec_r, ec_i, pr, pim;                                                      \
+            cmul_##SFX(-ii, ir, c, sn, &ic_r, &ic_i);    /* (im*i)*exp(-im*θ), im*i = (-ii, ir) */  \
+            cmul_##SFX(-ui, ur, c, sn, &ec_r, &ec_i);    /* (im*u)*exp(-im*θ) */                    \
+            cmul_##SFX(ur, ui, ir, -ii, &pr, &pim);      /* u*conj(i) */                            \
+            T de_d = (T)1 / T_q_dash * (-ec_r + (X_q - X_q_dash) * ic_i);                           \
+            T de_q = (T)1 / T_d_dash * (-ec_i - (X_d - X_d_dash) * ic_r + E_f);                     \
+            T t_r, t_i;                                                                             \
+            cmul_##SFX(de_q, -de_d, COS(th), SIN(th), &t_r, &t_i); /* (-im*de_c)*exp(im*θ) */       \
+            du[0] = t_r + (-ui) * w;                     /* + (u*im)*ω, u*im = (-ui, ur) */         \
+            du[1] = t_i + ur * w;                                                                   \
+            du[2] = w;                                                                              \
+            du[3] = (P - D * w - pr - (X_q_dash - X_d_dash) * ic_r * ic_i) * Om_H;                  \
         }                                                                                           \
     }                                                                                               \
     /* edge g: ODE edges map their states (PureStateMap, :41), static edges evaluate g */         \
@@ -292,6 +395,23 @@ int64_t nd_oracle_e_data(const layout_t* L, int64_t e) { return L->e_data[e]; }
         if (is_ode_edge(ek)) {                                                                      \
             o[L->e_out_dst[e]] = u[L->e_data[e]];                                                   \
             o[L->e_out_src[e]] = u[L->e_data[e] + 1];                                               \
+            return;                                                                                 \
+        }                                                                                           \
+        if (ek == E_PILINE) { /* piline!: two-sided, complex currents */                            \
+            const T* pe = p + L->e_para[e];                                                         \
+            T Lh = pe[0], R = pe[1], C1 = pe[2], C2 = pe[3], w = (T)PILINE_OMEGA;                   \
+            const T* vs = o + L->v_out[L->src[e]];                                                  \
+            const T* vd = o + L->v_out[L->dst[e]];                                                  \
+            T im_r, im_i;                                                                           \
+            cdiv_##SFX(vs[0] - vd[0], vs[1] - vd[1], R, w * Lh, &im_r, &im_i); /* R + im*ω*L */     \
+            T c1_r = (-vs[1]) * w * C1, c1_i = vs[0] * w * C1; /* Vsrc*im*ω*C1 */                   \
+            T c2_r = (-vd[1]) * w * C2, c2_i = vd[0] * w * C2;                                      \
+            T is_r = -(im_r + c1_r), is_i = -(im_i + c1_i);                                         \
+            T id_r = im_r - c2_r, id_i = im_i - c2_i;                                               \
+            o[L->e_out_dst[e]] = -id_r;                                                             \
+            o[L->e_out_dst[e] + 1] = -id_i;                                                         \
+            o[L->e_out_src[e]] = -is_r;                                                             \
+            o[L->e_out_src[e] + 1] = -is_i;                                                         \
             return;                                                                                 \
         }                                                                                           \
         T vs = o[L->v_out[L->src[e]]], vd = o[L->v_out[L->dst[e]]];                                 \
@@ -325,7 +445,7 @@ int64_t nd_oracle_e_data(const layout_t* L, int64_t e) { return L->e_data[e]; }
         for (i = 0; i < L->lastidx_aggr; ++i) aggbuf[i] = 0;      /* fill!(aggbuf, 0)  :30 */       \
         for (int64_t k = 0; k < L->nv; ++k) {                     /* vertex g, StateMask :39 */     \
             int64_t v = L->vbatch_order[k];                                                         \
-            o[L->v_out[v]] = u[L->v_data[v]];                                                       \
+            for (int j = 0; j < L->depth; ++j) o[L->v_out[v] + j] = u[L->v_data[v] + j];            \
         }                                                                                           \
         for (int64_t k = 0; k < L->ne; ++k) edges_g_##SFX(L, o, u, p, k);                           \
         for (int64_t k = 0; k < L->ne; ++k) edges_f_##SFX(L, du, u, o, p, k);                       \
@@ -337,7 +457,7 @@ int64_t nd_oracle_e_data(const layout_t* L, int64_t e) { return L->e_data[e]; }
         for (int64_t k = 0; k < L->nv; ++k) {                     /* vertex f :97 */                \
             int64_t v = L->vbatch_order[k];                                                         \
             vertex_f_##SFX(L->vkind[v], du + L->v_data[v], u + L->v_data[v], p + L->v_para[v],      \
-                           aggbuf[L->v_aggr[v]]);                                                   \
+                           aggbuf + L->v_aggr[v]);                                                  \
         }                                                                                           \
     }                                                                                               \
     void nd_oracle_rhs_poly_##SFX(const layout_t* L, T* du, const T* u, const T* p, T* o,           \
@@ -347,7 +467,7 @@ int64_t nd_oracle_e_data(const layout_t* L, int64_t e) { return L->e_data[e]; }
         _Pragma("omp parallel for schedule(static)") for (i = 0; i < L->lastidx_aggr; ++i) aggbuf[i] = 0; \
         _Pragma("omp parallel for schedule(static)") for (i = 0; i < L->nv; ++i) {                 \
             int64_t v = L->vbatch_order[i];                                                         \
-            o[L->v_out[v]] = u[L->v_data[v]];                                                       \
+            for (int j = 0; j < L->depth; ++j) o[L->v_out[v] + j] = u[L->v_data[v] + j];            \
         }                                                                                           \
         _Pragma("omp parallel for schedule(static)") for (i = 0; i < L->ne; ++i)                   \
             edges_g_##SFX(L, o, u, p, i);                                                           \
@@ -361,12 +481,12 @@ int64_t nd_oracle_e_data(const layout_t* L, int64_t e) { return L->e_data[e]; }
         _Pragma("omp parallel for schedule(static)") for (i = 0; i < L->nv; ++i) {                 \
             int64_t v = L->vbatch_order[i];                                                         \
             vertex_f_##SFX(L->vkind[v], du + L->v_data[v], u + L->v_data[v], p + L->v_para[v],      \
-                           aggbuf[L->v_aggr[v]]);                                                   \
+                           aggbuf + L->v_aggr[v]);                                                  \
         }                                                                                           \
     }
 
-DEFINE_ORACLE_RHS(double, f64, sin)
-DEFINE_ORACLE_RHS(float, f32, sinf)
+DEFINE_ORACLE_RHS(double, f64, sin, cos)
+DEFINE_ORACLE_RHS(float, f32, sinf, cosf)
 
 int nd_oracle_num_threads(void) {
 #ifdef _OPENMP

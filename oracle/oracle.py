@@ -27,14 +27,16 @@ SRC = HERE / "nd_oracle.c"
 BUILD_DIR = HERE / "_build"
 LIB = BUILD_DIR / "liboracle.so"
 
-V_DIFFUSION, V_KURAMOTO, V_SWING, V_SWING_UNIT = 1, 2, 3, 4
-E_DIFFUSION, E_DIFFUSION_UNIT, E_KURAMOTO, E_DIFFUSION_ODE, E_DIFFUSION_ODE_FIXED = 1, 2, 3, 4, 5
+V_DIFFUSION, V_KURAMOTO, V_SWING, V_SWING_UNIT, V_PQ, V_GENERATOR = 1, 2, 3, 4, 5, 6
+E_DIFFUSION, E_DIFFUSION_UNIT, E_KURAMOTO, E_DIFFUSION_ODE, E_DIFFUSION_ODE_FIXED, E_PILINE = 1, 2, 3, 4, 5, 6
 C_ANTISYMMETRIC, C_SYMMETRIC, C_DIRECTED, C_FIDUCIAL = 1, 2, 3, 4
 
-VDIM = {V_DIFFUSION: 1, V_KURAMOTO: 1, V_SWING: 2, V_SWING_UNIT: 2}
-VPDIM = {V_DIFFUSION: 0, V_KURAMOTO: 1, V_SWING: 3, V_SWING_UNIT: 1}
-EDIM = {E_DIFFUSION: 0, E_DIFFUSION_UNIT: 0, E_KURAMOTO: 0, E_DIFFUSION_ODE: 2, E_DIFFUSION_ODE_FIXED: 2}
-EPDIM = {E_DIFFUSION: 1, E_DIFFUSION_UNIT: 0, E_KURAMOTO: 1, E_DIFFUSION_ODE: 1, E_DIFFUSION_ODE_FIXED: 0}
+VDIM = {V_DIFFUSION: 1, V_KURAMOTO: 1, V_SWING: 2, V_SWING_UNIT: 2, V_PQ: 2, V_GENERATOR: 4}
+VPDIM = {V_DIFFUSION: 0, V_KURAMOTO: 1, V_SWING: 3, V_SWING_UNIT: 1, V_PQ: 2, V_GENERATOR: 11}
+EDIM = {E_DIFFUSION: 0, E_DIFFUSION_UNIT: 0, E_KURAMOTO: 0, E_DIFFUSION_ODE: 2, E_DIFFUSION_ODE_FIXED: 2,
+        E_PILINE: 0}
+EPDIM = {E_DIFFUSION: 1, E_DIFFUSION_UNIT: 0, E_KURAMOTO: 1, E_DIFFUSION_ODE: 1, E_DIFFUSION_ODE_FIXED: 0,
+         E_PILINE: 4}
 
 
 def build_oracle(force: bool = False) -> Path:
@@ -74,6 +76,11 @@ def load():
         lib.nd_oracle_layout_new_batched.argtypes = [i64, i64, P64, P64, C.c_int, P32, P32, C.c_int, P32, P32, P32]
         lib.nd_oracle_layout_free.argtypes = [vp]
         for fn in ("nd_oracle_dim", "nd_oracle_pdim"):
+            getattr(lib, fn).restype = i64
+            getattr(lib, fn).argtypes = [vp]
+        lib.nd_oracle_depth.restype = C.c_int
+        lib.nd_oracle_depth.argtypes = [vp]
+        for fn in ("nd_oracle_n_out", "nd_oracle_n_aggr"):
             getattr(lib, fn).restype = i64
             getattr(lib, fn).argtypes = [vp]
         for fn in ("nd_oracle_v_data", "nd_oracle_v_para", "nd_oracle_e_para", "nd_oracle_e_data"):
@@ -122,9 +129,16 @@ class OracleNetwork:
         self.L = self.lib.nd_oracle_layout_new(self.nv, self.ne, self.src.ctypes.data_as(P64),
                                                self.dst.ctypes.data_as(P64), self.vkind.ctypes.data_as(P32),
                                                self.ekind.ctypes.data_as(P32))
+        self._finish()
+
+    def _finish(self):
+        if not self.L:
+            raise ValueError("all vertex models and all edge models must have the same output dimension")
         self.dim = int(self.lib.nd_oracle_dim(self.L))
         self.pdim = int(self.lib.nd_oracle_pdim(self.L))
-        self.n_out = self.nv + 2 * self.ne
+        self.depth = int(self.lib.nd_oracle_depth(self.L))
+        self.n_out = int(self.lib.nd_oracle_n_out(self.L))
+        self.n_aggr = int(self.lib.nd_oracle_n_aggr(self.L))
 
     @classmethod
     def from_graph(cls, g, vkind, ekind):
@@ -155,9 +169,7 @@ class OracleNetwork:
             self.nv, self.ne, self.src.ctypes.data_as(P64), self.dst.ctypes.data_as(P64), len(vbk),
             vbk.ctypes.data_as(P32), vb.ctypes.data_as(P32), len(edge_batches), ebk.ctypes.data_as(P32),
             ebc.ctypes.data_as(P32), eb.ctypes.data_as(P32))
-        self.dim = int(self.lib.nd_oracle_dim(self.L))
-        self.pdim = int(self.lib.nd_oracle_pdim(self.L))
-        self.n_out = self.nv + 2 * self.ne
+        self._finish()
         return self
 
     def __del__(self):
@@ -171,7 +183,7 @@ class OracleNetwork:
         assert u.shape == (self.dim,) and p.shape == (self.pdim,)
         du = np.empty(self.dim, dtype=dtype)
         o = np.empty(self.n_out + 1, dtype=dtype)
-        ab = np.empty(self.nv + 1, dtype=dtype)
+        ab = np.empty(self.n_aggr + 1, dtype=dtype)
         fn(self.L, du.ctypes.data, u.ctypes.data, _ptr(p), o.ctypes.data, ab.ctypes.data)
         return du
 
@@ -300,6 +312,9 @@ def rhs_numpy_batched(nv, src, dst, vertex_batches, vertex_batch, edge_batches, 
     p = np.asarray(p if p is not None else np.zeros(0), dtype=dtype)
     sin = (lambda x: np.sin(x)) if dtype == np.float64 else (lambda x: np.sin(x).astype(dtype))
     du = np.zeros(L["dim"], dtype=dtype)
+    if any(k in (V_PQ, V_GENERATOR) for k in vertex_batches):
+        return _rhs_numpy_powergrid(nv, src, dst, vertex_batches, vertex_batch, edge_batches, edge_batch, u, p, L,
+                                    du)
     ov = u[L["v_data"]]                                # vertex g: StateMask(1)
     eo = L["eorder"]
     eb = np.asarray(edge_batch, dtype=np.int64)
@@ -343,6 +358,57 @@ def rhs_numpy_batched(nv, src, dst, vertex_batches, vertex_batch, edge_batches, 
             w = u[s + 1]
             du[s] = w
             du[s + 1] = (p[q].astype(np.float64) - 1.0 * w.astype(np.float64)).astype(dtype) + a
+    return du
+
+
+def _rhs_numpy_powergrid(nv, src, dst, vertex_batches, vertex_batch, edge_batches, edge_batch, u, p, L, du):
+    """The power-grid components (benchmark/benchmark_models.jl:46-109) in numpy complex
+    arithmetic: vertex outputs and edge outputs are complex numbers (depth 2)."""
+    v_data, v_para, e_para = L["v_data"], L["v_para"], L["e_para"]
+    V = u[v_data] + 1j * u[v_data + 1]                 # StateMask(1:2)
+    w = 2 * np.pi * 50
+    ne = len(src)
+    isrc = np.zeros(ne, dtype=np.complex128)
+    idst = np.zeros(ne, dtype=np.complex128)
+    eb = np.asarray(edge_batch, dtype=np.int64)
+    for b, (k, c) in enumerate(edge_batches):
+        assert k == E_PILINE
+        es = np.flatnonzero(eb == b)
+        Lh, R, C1, C2 = (p[e_para[es] + j] for j in range(4))
+        Vs, Vd = V[src[es]], V[dst[es]]
+        imain = (Vs - Vd) / (R + 1j * w * Lh)
+        i_src = -(imain + Vs * 1j * w * C1)
+        i_dst = imain - Vd * 1j * w * C2
+        isrc[es], idst[es] = -i_src, -i_dst
+    eo = L["eorder"]
+    vals = np.empty(2 * ne, dtype=np.complex128)
+    vals[0::2], vals[1::2] = isrc[eo], idst[eo]
+    tg = np.empty(2 * ne, dtype=np.int64)
+    tg[0::2], tg[1::2] = src[eo], dst[eo]
+    re, im = np.zeros(nv), np.zeros(nv)                # SequentialAggregator, per component
+    np.add.at(re, tg, vals.real)
+    np.add.at(im, tg, vals.imag)
+    isum = re + 1j * im
+    vbatch = np.asarray(vertex_batch)
+    for b, k in enumerate(vertex_batches):
+        vs = np.flatnonzero(vbatch == b)
+        s, q, i = v_data[vs], v_para[vs], isum[vs]
+        if k == V_PQ:
+            uc = (p[q] + 1j * p[q + 1]) / np.conj(i)
+            du[s], du[s + 1] = uc.real, uc.imag
+            continue
+        assert k == V_GENERATOR
+        H, P, D, Om, E_f, T_d_dash, T_q_dash, X_q_dash, X_d_dash, X_d, X_q = (p[q + j] for j in range(11))
+        uc = u[s] + 1j * u[s + 1]
+        th, om = u[s + 2], u[s + 3]
+        i_c = 1j * i * np.exp(-1j * th)
+        e_c = 1j * uc * np.exp(-1j * th)
+        pw = (uc * np.conj(i)).real
+        de_d = (1 / T_q_dash) * (-e_c.real + (X_q - X_q_dash) * i_c.imag)
+        de_q = (1 / T_d_dash) * (-e_c.imag - (X_d - X_d_dash) * i_c.real + E_f)
+        dU = -1j * (de_d + 1j * de_q) * np.exp(1j * th) + uc * 1j * om
+        du[s], du[s + 1], du[s + 2] = dU.real, dU.imag, om
+        du[s + 3] = (P - D * om - pw - (X_q_dash - X_d_dash) * i_c.real * i_c.imag) * (Om / (2 * H))
     return du
 
 

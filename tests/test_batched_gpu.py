@@ -263,3 +263,45 @@ def test_batched_errors(cuda):
     p = torch.ones(nw.pdim, dtype=torch.float64, device=cuda)
     with pytest.raises(nd.ArgumentError):
         nw(du, u, p)
+
+
+def powergrid_network(nv, seed, pq_only=False):
+    g = nd.watts_strogatz(nv, 4, 0.5, seed=seed)
+    rng = np.random.default_rng(seed)
+    kinds = np.zeros(nv, dtype=int) if pq_only else rng.integers(0, 2, nv)
+    vm = [nd.pqnode() if k == 0 else nd.generator() for k in kinds]
+    net = nd.Network(g, vm, nd.piline())
+    vb = [m.kind for m in net.vertex_batches]
+    on = O.OracleNetwork.from_batches(g.nv, g.src, g.dst, vb, net.vertex_batch, [(O.E_PILINE, O.C_FIDUCIAL)],
+                                      net.edge_batch)
+    return g, net, on
+
+
+@pytest.mark.parametrize("nv", [300, 20_000])
+def test_powergrid_parity(cuda, nv):
+    """PQ buses, generators and π-lines (benchmark/benchmark_cases.jl:68-79): complex
+    outputs on the GPU against the oracle.  Without generators there is no transcendental
+    function and the FP64 result is bitwise; generators differ through cos / sin."""
+    for pq_only in (True, False):
+        g, net, on = powergrid_network(nv, 3, pq_only)
+        rng = np.random.default_rng(4)
+        u, p = rng.normal(size=net.dim), rng.uniform(0.5, 1.5, size=net.pdim)
+        ref = on.rhs(u, p)
+        got = gpu_rhs(adapt(net, np.float64), u, p, cuda, np.float64)
+        if pq_only:
+            np.testing.assert_array_equal(got, ref)
+        else:
+            assert np.max(np.abs(got - ref) / (1 + np.abs(ref))) < 1e-12
+        got32 = gpu_rhs(adapt(net, np.float32), u, p, cuda, np.float32).astype(np.float64)
+        check_f32_isapprox(got32, ref)
+
+
+def test_powergrid_has_no_jacobian(cuda):
+    import torch
+    g, net, _ = powergrid_network(50, 1)
+    nw = adapt(net, np.float64)
+    with pytest.raises(nd.ArgumentError):
+        nd.jacobian_pattern(nw)
+    u = torch.zeros(nw.dim, dtype=torch.float64, device=cuda)
+    with pytest.raises(nd.ArgumentError):
+        nd.jvp(nw, torch.empty_like(u), u, torch.ones(nw.pdim, dtype=torch.float64, device=cuda), u)

@@ -67,7 +67,8 @@ def test_create_rejects_bad_dtype_and_coupling():
     h = C.c_void_p()
     assert lib.nd_create(C.byref(d), 3, C.byref(h)) == capi.ND_ERR_DTYPE
     for ek, coupling in ((capi.ND_E_DIFFUSION, 9), (capi.ND_E_KURAMOTO, capi.ND_FIDUCIAL),
-                         (capi.ND_E_DIFFUSION_ODE, capi.ND_ANTISYMMETRIC), (6, capi.ND_FIDUCIAL)):
+                         (capi.ND_E_DIFFUSION_ODE, capi.ND_ANTISYMMETRIC), (7, capi.ND_FIDUCIAL),
+                         (capi.ND_E_PILINE, capi.ND_ANTISYMMETRIC)):
         d2, _keep2 = _desc(g, capi.ND_V_DIFFUSION, ek, coupling=coupling)
         assert lib.nd_create(C.byref(d2), capi.ND_F64, C.byref(h)) == capi.ND_ERR_UNSUPPORTED_COMPONENT
         assert not h.value

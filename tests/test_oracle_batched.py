@@ -167,3 +167,62 @@ def test_ode_edge_relaxes_to_the_static_sine_coupling():
     np.add.at(exp, d, np.sin(th[s] - th[d]))
     np.add.at(exp, s, np.sin(th[d] - th[s]))
     np.testing.assert_allclose(du[:5], exp, atol=1e-15)
+
+
+def powergrid(nv=300, seed=0, pq_only=False):
+    """A power-grid network: PQ buses and generators on a Watts-Strogatz graph with π-line
+    edges (benchmark/benchmark_cases.jl:68-79)."""
+    g = nd.watts_strogatz(nv, 4, 0.5, seed=seed)
+    rng = np.random.default_rng(seed)
+    kinds = np.zeros(nv, dtype=int) if pq_only else rng.integers(0, 2, nv)
+    order = list(dict.fromkeys(kinds.tolist()))          # batches in order of first appearance
+    vb = [[O.V_PQ, O.V_GENERATOR][k] for k in order]
+    vbi = np.array([order.index(k) for k in kinds], dtype=np.int32)
+    return g, vb, vbi, [(O.E_PILINE, O.C_FIDUCIAL)], np.zeros(g.ne, dtype=np.int32)
+
+
+@pytest.mark.parametrize("pq_only", [False, True])
+def test_powergrid_oracle_matches_numpy_complex(pq_only):
+    """The C restatement of piline!, pq! and gen! (real arithmetic in Julia's operation order)
+    against numpy's complex arithmetic."""
+    g, vb, vbi, eb, ebi = powergrid(pq_only=pq_only)
+    on = O.OracleNetwork.from_batches(g.nv, g.src, g.dst, vb, vbi, eb, ebi)
+    assert on.depth == 2 and on.n_out == 2 * (g.nv + 2 * g.ne)
+    rng = np.random.default_rng(1)
+    u, p = rng.normal(size=on.dim), rng.uniform(0.5, 1.5, size=on.pdim)
+    ref = O.rhs_numpy_batched(g.nv, g.src, g.dst, vb, vbi, eb, ebi, u, p)
+    scale = 1 + np.abs(ref)
+    assert np.max(np.abs(on.rhs(u, p) - ref) / scale) < 1e-12
+    np.testing.assert_array_equal(on.rhs_poly(u, p), on.rhs(u, p))
+
+
+def test_piline_known_answer():
+    """One π-line between two PQ buses: the currents are the line's admittance equations,
+    i_dst = (Vs - Vd)/(R + iωL) - iωC2·Vd into the destination, and the PQ buses map them to
+    du = S / conj(i)."""
+    g = nd.Graph(2, np.array([0]), np.array([1]))
+    on = O.OracleNetwork.from_batches(2, g.src, g.dst, [O.V_PQ], [0, 0], [(O.E_PILINE, O.C_FIDUCIAL)], [0])
+    Vs, Vd = 1.0 + 0.2j, 0.9 - 0.1j
+    L, R, C1, C2 = 1e-3, 0.05, 2e-5, 3e-5
+    P = np.array([0.3, -0.4, 0.1, 0.2])                 # (P, Q) of bus 0, then of bus 1
+    u = np.array([Vs.real, Vs.imag, Vd.real, Vd.imag])
+    p = np.concatenate([P, [L, R, C1, C2]])
+    w = 2 * np.pi * 50
+    imain = (Vs - Vd) / (R + 1j * w * L)
+    i_to_src = imain + 1j * w * C1 * Vs                   # -isrc
+    i_to_dst = -(imain - 1j * w * C2 * Vd)                # -idst
+    du = on.rhs(u, p)
+    exp0 = (P[0] + 1j * P[1]) / np.conj(i_to_src)
+    exp1 = (P[2] + 1j * P[3]) / np.conj(i_to_dst)
+    np.testing.assert_allclose(du, [exp0.real, exp0.imag, exp1.real, exp1.imag], rtol=1e-13)
+
+
+def test_mixed_output_dimensions_rejected():
+    """All vertex models (and edge models) must have the same output dimension
+    (src/construction.jl:98-106)."""
+    g = nd.cycle_graph(4)
+    with pytest.raises(ValueError):
+        O.OracleNetwork.from_batches(4, g.src, g.dst, [O.V_PQ, O.V_DIFFUSION], [0, 1, 0, 1],
+                                     [(O.E_PILINE, O.C_FIDUCIAL)], [0] * 4)
+    with pytest.raises(nd.ArgumentError):
+        nd.Network(g, [nd.pqnode(), nd.diffusion_vertex(), nd.pqnode(), nd.diffusion_vertex()], nd.piline())
