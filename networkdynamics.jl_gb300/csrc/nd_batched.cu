@@ -116,9 +116,11 @@ constexpr int kWarpRowMinDegF32 = 2 * kLightMaxDeg + 1;
 // Terms per warp tile in shared memory (FP64 warp rows): 16 per lane.
 constexpr int kWarpTile = 512;
 
-// Sum of a row's n terms (y2 indices idx[0..n)) by one thread, in order, loads issued
-// kB terms ahead of the adds.  The adds of a batch stop at the longest remaining row in
-// the warp (a warp-uniform bound), so no add is issued for batch slots no lane has.
+// Sum of a row's n terms (y2 indices idx[0..n)) by one thread, in order.  The terms come in
+// batches of kB; the loads of batch k + 1 are issued before the adds of batch k, so on long
+// rows the gathers overlap the chain of dependent adds.  The adds of a batch stop at the
+// longest remaining row in the warp (a warp-uniform bound), so no add is issued for batch
+// slots no lane has.
 //   FP64  the sequential sum with the reference's zero start folded into the first term
 //         (0 + t is t; -0 gives +0);
 //   FP32  the same order, Kahan-compensated on rows longer than kLightMaxDeg.
@@ -128,27 +130,32 @@ __device__ __forceinline__ T thread_row_sum(const T* __restrict__ y2, const int3
     constexpr int kB = 12;
     const bool kahan = sizeof(T) == 4 && n > kLightMaxDeg;
     T acc = T(0), comp = T(0);
-    for (int j0 = 0; j0 < n; j0 += kB) {
-        T t[kB];
+    T cur[kB], nxt[kB];
 #pragma unroll
-        for (int k = 0; k < kB; ++k) t[k] = j0 + k < n ? __ldg(y2 + __ldg(idx + j0 + k)) : T(0);
+    for (int k = 0; k < kB; ++k) cur[k] = k < n ? __ldg(y2 + __ldg(idx + k)) : T(0);
+    for (int j0 = 0; j0 < n; j0 += kB) {
+        const int j1 = j0 + kB;
+#pragma unroll
+        for (int k = 0; k < kB; ++k) nxt[k] = j1 + k < n ? __ldg(y2 + __ldg(idx + j1 + k)) : T(0);
         const int lim = __reduce_max_sync(__activemask(), (unsigned)min(kB, n - j0));
 #pragma unroll
         for (int k = 0; k < kB; ++k) {
             if (k >= lim) break;
             if (j0 + k >= n) continue;
             if (sizeof(T) == 8 && j0 + k == 0) {
-                const double t0 = (double)t[0];
+                const double t0 = (double)cur[0];
                 acc = (T)((__double_as_longlong(t0) << 1) == 0 ? 0.0 : t0);
             } else if (kahan) {
-                const T yk = A::sub(t[k], comp);
+                const T yk = A::sub(cur[k], comp);
                 const T s2 = A::add(acc, yk);
                 comp = A::sub(A::sub(s2, acc), yk);
                 acc = s2;
             } else {
-                acc = A::add(acc, t[k]);
+                acc = A::add(acc, cur[k]);
             }
         }
+#pragma unroll
+        for (int k = 0; k < kB; ++k) cur[k] = nxt[k];
     }
     return sizeof(T) == 4 ? A::sub(acc, comp) : acc;
 }
