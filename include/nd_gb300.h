@@ -256,6 +256,18 @@ int nd_jvp(nd_handle* h, int dtype, void* jv, const void* u, const void* p, cons
 int nd_jacobian_pattern(nd_handle* h, int64_t* nnz, int32_t* rowptr, int32_t* colidx);
 int nd_jacobian(nd_handle* h, int dtype, void* values, const void* u, const void* p, double t, void* stream);
 
+/* Steady state of a network whose outputs have dimension 1 (every kind but the power-grid
+ * ones), the counterpart of find_fixpoint(nw, x0, p) (src/initialization.jl:44-144), which
+ * solves a SteadyStateProblem with NonlinearSolve: Newton's method with restarted GMRES
+ * (Krylov dimension krylov_dim <= 64, default 40; max_restarts cycles, default 20) on the
+ * sparse Jacobian of nd_jacobian, and a backtracking line search on max|F|.  u (device,
+ * FP64, length dim): x0 in, the steady state out.  Stops at max|du| <= tol.  Writes the
+ * Newton iterations and the final max|du| to the host pointers iters / resid.  An RHS
+ * with NaN at x0 and a solve that does not reach tol give ND_ERR_NOT_CONVERGED (the
+ * reference's NetworkInitError).  FP64 handles; synchronous. */
+int nd_find_fixpoint(nd_handle* h, double* u, const double* p, double t, double tol, int max_newton, int krylov_dim,
+                     int max_restarts, int32_t* iters, double* resid, void* stream);
+
 /* Result of a solve. */
 typedef struct nd_solve_stats {
     int64_t naccept; /* accepted steps                               */

@@ -205,6 +205,8 @@ SIGNATURES.update({
     "nd_jvp": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _d, _vp]),
     "nd_jacobian_pattern": (C.c_int, [_vp, C.POINTER(C.c_int64), _vp, _vp]),
     "nd_jacobian": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _d, _vp]),
+    "nd_find_fixpoint": (C.c_int, [_vp, _vp, _vp, _d, _d, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int32),
+                                   C.POINTER(C.c_double), _vp]),
     "nd_ensemble_create": (C.c_int, [C.POINTER(nd_ensemble_desc), C.c_int, C.POINTER(C.c_void_p)]),
     "nd_ensemble_destroy": (C.c_int, [_vp]),
     "nd_ensemble_get_info": (C.c_int, [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),

@@ -151,5 +151,5 @@ def test_find_fixpoint_known_answer_and_errors(cuda):
     p_bad[2::3][:4] = [20.0, -20.0, 20.0, -20.0]
     with pytest.raises(nd.NotConvergedError):
         nd.find_fixpoint(net, p_bad, max_newton=20)
-    with pytest.raises(nd.ArgumentError):
-        nd.find_fixpoint(nd.Network(g4, nd.kuramoto_first(), nd.kuramoto_edge()), np.zeros(8))
+    with pytest.raises(nd.ArgumentError):  # the swing solver takes swing networks only
+        nd.find_fixpoint(nd.Network(g4, nd.kuramoto_first(), nd.kuramoto_edge()), np.zeros(8), alg="swing")
