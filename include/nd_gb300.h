@@ -165,8 +165,8 @@ int nd_create(const nd_network_desc* desc, int dtype, nd_handle** out);
  * of additions (ascending output index).  Networks of one static AntiSymmetric edge
  * batch and one vertex batch of kinds 1-3 take the same kernels as nd_create; all others
  * a batched two-kernel RHS (edge kernel with per-batch dispatch, then row sums and
- * vertex functions).  nd_jvp and the ensemble calls do not take batched handles
- * (ND_ERR_UNSUPPORTED). */
+ * vertex functions).  nd_jvp of a batched handle assembles the sparse Jacobian
+ * (nd_jacobian) and multiplies; the ensemble calls do not take batched handles. */
 #define ND_MAX_BATCHES 32
 typedef struct nd_batch {
     int32_t kind;     /* enum nd_vertex_kind / enum nd_edge_kind */

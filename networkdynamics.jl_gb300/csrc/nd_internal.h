@@ -257,8 +257,10 @@ struct JacPlan {
     int32_t* colidx = nullptr;
     int32_t* long_slots = nullptr;  // slots of the rows that take a warp each
     int64_t n_long = 0;
+    void* values = nullptr;         // Jacobian values kept for nd_jvp of batched handles
 };
 void free_jacobian(JacPlan* j);
+
 }  // namespace nd
 
 struct nd_handle {

@@ -415,13 +415,57 @@ cudaError_t launch_values(nd_handle* h, void* values, const void* u, const void*
     return cudaGetLastError();
 }
 
+template <typename T>
+__global__ void __launch_bounds__(kJacBlock) csr_times_kernel(int64_t n, const int32_t* __restrict__ rowptr,
+                                                              const int32_t* __restrict__ col,
+                                                              const T* __restrict__ val, const T* __restrict__ x,
+                                                              T* __restrict__ y) {
+    using A = Arith<T>;
+    const int64_t i = (int64_t)blockIdx.x * kJacBlock + threadIdx.x;
+    if (i >= n) return;
+    T s = T(0);
+    for (int32_t k = __ldg(rowptr + i); k < __ldg(rowptr + i + 1); ++k)
+        s = A::add(s, A::mul(__ldg(val + k), __ldg(x + __ldg(col + k))));
+    y[i] = s;
+}
+
 }  // namespace
+
+// jv = J(u, p) v for handles without a direct JVP kernel (batched networks): the Jacobian
+// assembled into a buffer the handle keeps, then one CSR product.
+int jacobian_times(nd_handle* h, void* jv, const void* u, const void* p, const void* v, cudaStream_t s) {
+    if (!h->jac.ready) {
+        const int rc = build_plan(h);
+        if (rc != ND_OK) return rc;
+    }
+    JacPlan& J = h->jac;
+    const size_t elem = h->dtype == ND_F64 ? 8 : 4;
+    if (!J.values) {
+        const cudaError_t e = cudaMalloc(&J.values, std::max<int64_t>(J.nnz, 1) * elem);
+        if (e != cudaSuccess) return cuda_fail(e, "nd_jvp: Jacobian buffer");
+    }
+    cudaError_t err = h->dtype == ND_F64 ? launch_values<double>(h, J.values, u, p, s)
+                                         : launch_values<float>(h, J.values, u, p, s);
+    const int64_t n = h->dim;
+    const unsigned grid = (unsigned)((n + kJacBlock - 1) / kJacBlock);
+    if (err == cudaSuccess && n > 0) {
+        if (h->dtype == ND_F64)
+            csr_times_kernel<double><<<grid, kJacBlock, 0, s>>>(n, J.rowptr, J.colidx, static_cast<double*>(J.values),
+                                                                static_cast<const double*>(v), static_cast<double*>(jv));
+        else
+            csr_times_kernel<float><<<grid, kJacBlock, 0, s>>>(n, J.rowptr, J.colidx, static_cast<float*>(J.values),
+                                                               static_cast<const float*>(v), static_cast<float*>(jv));
+        err = cudaGetLastError();
+    }
+    return err == cudaSuccess ? ND_OK : cuda_fail(err, "nd_jvp");
+}
 
 void free_jacobian(JacPlan* j) {
     if (j->view.enabled) free_batched(&j->view);
     cudaFree(j->rowptr);
     cudaFree(j->colidx);
     cudaFree(j->long_slots);
+    cudaFree(j->values);
     *j = JacPlan{};
 }
 

@@ -18,6 +18,8 @@
 
 namespace nd {
 
+int jacobian_times(nd_handle* h, void* jv, const void* u, const void* p, const void* v, cudaStream_t s);
+
 namespace {
 
 // Contribution c (v_n - v_v) of one incidence (neighbour n) to row v.
@@ -136,9 +138,7 @@ extern "C" int nd_jvp(nd_handle* h, int dtype, void* jv, const void* u, const vo
     if (!h || !jv || !u || !v) return fail(ND_ERR_ARG, "nd_jvp: NULL argument");
     if (dtype != h->dtype) return fail(ND_ERR_DTYPE, "nd_jvp: element type differs from the handle's");
     if (h->pdim > 0 && !p) return fail(ND_ERR_ARG, "nd_jvp: p is NULL");
-    if (h->batched.enabled)
-        return fail(ND_ERR_UNSUPPORTED, "nd_jvp: batched networks (several batches, ODE edges, other couplings) "
-                                        "have no analytic Jacobian-vector product");
+    if (h->batched.enabled) return jacobian_times(h, jv, u, p, v, (cudaStream_t)stream);
     cudaError_t err = h->dtype == ND_F64 ? launch_jvp<double>(h, u, p, v, jv, (cudaStream_t)stream)
                                          : launch_jvp<float>(h, u, p, v, jv, (cudaStream_t)stream);
     return err == cudaSuccess ? ND_OK : cuda_fail(err, "nd_jvp");

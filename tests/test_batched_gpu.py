@@ -100,9 +100,14 @@ def test_reference_gpu_test_network(cuda):
         gpu_rhs(nw2, x0, p, cuda, np.float32)
     with pytest.raises(nd.ArgumentError):
         gpu_rhs(nw1, x0, p, cuda, np.float64)
+    # the JVP of a batched network (assembled Jacobian times v) against central differences
     u = torch.from_numpy(x0).to(cuda)
-    with pytest.raises(nd.ArgumentError):      # no analytic JVP for batched networks
-        nd.jvp(nw2, torch.empty_like(u), u, torch.from_numpy(p).to(cuda), u)
+    v = rng.normal(size=nw.dim)
+    jv = torch.empty_like(u)
+    nd.jvp(nw2, jv, u, torch.from_numpy(p).to(cuda), torch.from_numpy(v).to(cuda))
+    h = 1e-6
+    fd = (on.rhs(x0 + h * v, p) - on.rhs(x0 - h * v, p)) / (2 * h)
+    np.testing.assert_allclose(jv.cpu().numpy(), fd, rtol=1e-6, atol=1e-7)
 
 
 VKINDS = [O.V_SWING, O.V_DIFFUSION, O.V_KURAMOTO, O.V_SWING_UNIT]
