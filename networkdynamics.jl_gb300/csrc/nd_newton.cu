@@ -6,8 +6,9 @@
 //   F(u) = nw(du, u, p, t); stop when max|F| <= tol (the reference's residual norm,
 //   src/initialization.jl:129).  Before the first step the RHS is checked for NaN, as the
 //   reference does (:75-126).
-//   Newton step: J δ = -F with J = ∂F/∂u at u (nd_jacobian), solved by GMRES(m) with
-//   Arnoldi by classical Gram-Schmidt applied twice, and Givens rotations, to a relative residual
+//   Newton step: J δ = -F with J = ∂F/∂u at u (nd_jacobian), solved by GMRES(m), right-
+//   preconditioned by the Jacobian's diagonal (Jacobi), with Arnoldi by classical
+//   Gram-Schmidt applied twice and Givens rotations, to a relative residual
 //   η = min(1e-2, max|F|), at most `max_restarts` cycles; then a backtracking line search
 //   on max|F| (λ = 1, 1/2, ... 2^-10).  Singular Jacobians with a consistent right-hand
 //   side (the phase shift of Kuramoto / swing networks) are fine for GMRES started from 0.
@@ -125,6 +126,24 @@ __global__ void combine_kernel(int64_t n, int nv, const double* __restrict__ V, 
     }
 }
 
+// dinv[i] = 1 / J[i][i] (1 where the diagonal is zero or absent): the Jacobi scaling
+__global__ void diag_inverse_kernel(int64_t n, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                    const double* __restrict__ val, double* __restrict__ dinv) {
+    for (int64_t i = (int64_t)blockIdx.x * kNB + threadIdx.x; i < n; i += (int64_t)gridDim.x * kNB) {
+        double d = 0.0;
+        for (int32_t k = __ldg(rowptr + i); k < __ldg(rowptr + i + 1); ++k)
+            if (__ldg(col + k) == (int32_t)i) d = __ldg(val + k);
+        dinv[i] = d != 0.0 && d == d ? __ddiv_rn(1.0, d) : 1.0;
+    }
+}
+
+// z = dinv * x (elementwise)
+__global__ void scale_kernel(int64_t n, const double* __restrict__ dinv, const double* __restrict__ x,
+                             double* __restrict__ z) {
+    for (int64_t i = (int64_t)blockIdx.x * kNB + threadIdx.x; i < n; i += (int64_t)gridDim.x * kNB)
+        z[i] = __dmul_rn(dinv[i], x[i]);
+}
+
 unsigned grid_for(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + kNB - 1) / kNB, 152 * 8)); }
 
 struct Workspace {
@@ -158,7 +177,7 @@ extern "C" int nd_find_fixpoint(nd_handle* h, double* u, const double* p, double
     // device workspace: F, Fnew, trial u, δ, w, Krylov basis V[m+1][n], Jacobian values,
     // dot partials, scalars
     const int64_t ldv = n;
-    const size_t doubles = (size_t)n * (5 + m + 1) + (size_t)std::max<int64_t>(nnz, 1) +
+    const size_t doubles = (size_t)n * (7 + m + 1) + (size_t)std::max<int64_t>(nnz, 1) +
                            (size_t)kDotBlocks * (m + 1) + 2 * (kMaxKrylov + 2);
     Workspace ws;
     cudaError_t err = cudaMalloc(&ws.buf, doubles * sizeof(double) + 64);
@@ -168,7 +187,9 @@ extern "C" int nd_find_fixpoint(nd_handle* h, double* u, const double* p, double
     double* ut = Fn + n;
     double* dlt = ut + n;
     double* w = dlt + n;
-    double* V = w + n;
+    double* dinv = w + n;
+    double* z = dinv + n;
+    double* V = z + n;
     double* vals = V + (size_t)n * (m + 1);
     double* partial = vals + std::max<int64_t>(nnz, 1);
     double* dscal = partial + (size_t)kDotBlocks * (m + 1);
@@ -215,6 +236,7 @@ extern "C" int nd_find_fixpoint(nd_handle* h, double* u, const double* p, double
         ++it;
         // Jacobian at u, then GMRES for J δ = -F from δ = 0
         if ((rc = nd_jacobian(h, ND_F64, vals, u, p, t, s)) != ND_OK) return rc;
+        diag_inverse_kernel<<<G, kNB, 0, s>>>(n, J.rowptr, J.colidx, vals, dinv);
         cudaMemsetAsync(dlt, 0, n * sizeof(double), s);
         double bnorm2 = 0.0;
         if ((rc = multidot(F, 1, F, &bnorm2)) != ND_OK) return rc;
@@ -235,7 +257,9 @@ extern "C" int nd_find_fixpoint(nd_handle* h, double* u, const double* p, double
             double res = beta;
             for (; k < m; ++k) {
                 double* vk1 = V + (size_t)(k + 1) * ldv;
-                spmv_kernel<<<G, kNB, 0, s>>>(n, J.rowptr, J.colidx, vals, V + (size_t)k * ldv, vk1);
+                // right preconditioning: w = J D^-1 v_k
+                scale_kernel<<<G, kNB, 0, s>>>(n, dinv, V + (size_t)k * ldv, z);
+                spmv_kernel<<<G, kNB, 0, s>>>(n, J.rowptr, J.colidx, vals, z, vk1);
                 // classical Gram-Schmidt, applied twice (reorthogonalisation)
                 for (int pass = 0; pass < 2; ++pass) {
                     if ((rc = multidot(V, k + 1, vk1, dots.data())) != ND_OK) return rc;
@@ -275,8 +299,12 @@ extern "C" int nd_find_fixpoint(nd_handle* h, double* u, const double* p, double
                 const double d = H[(size_t)i * m + i];
                 y[i] = d != 0.0 ? sacc / d : 0.0;
             }
+            // δ += D^-1 V y
             cudaMemcpyAsync(dscal, y.data(), k * sizeof(double), cudaMemcpyHostToDevice, s);
-            combine_kernel<<<G, kNB, 0, s>>>(n, k, V, ldv, dscal, dlt);
+            cudaMemsetAsync(z, 0, n * sizeof(double), s);
+            combine_kernel<<<G, kNB, 0, s>>>(n, k, V, ldv, dscal, z);
+            scale_kernel<<<G, kNB, 0, s>>>(n, dinv, z, z);
+            axpby_kernel<<<G, kNB, 0, s>>>(n, 1.0, z, 1.0, dlt);
             if ((rc = sync_err("nd_find_fixpoint: gmres")) != ND_OK) return rc;
             if (res <= eta * bnorm) break;
         }

@@ -4,6 +4,7 @@
     python -m nd_gb300.benchmarks ensemble  [--instances 4096]
     python -m nd_gb300.benchmarks swing     [--nv 100000]
     python -m nd_gb300.benchmarks jacobian  [--nv 1000000]
+    python -m nd_gb300.benchmarks fixpoint  [--nv 1000000]
 
 Each prints one JSON object.  All inputs are seeded synthetic instances of the stated
 shapes; no dataset is read.
@@ -282,9 +283,35 @@ def jacobian(nv=1_000_000, m=2, seed=0, steps=100):
     return out
 
 
+def fixpoint(nv=1_000_000, m=2, seed=0):
+    """First-order Kuramoto on BA(nv, m) with zero-sum frequencies ω ~ U(-0.2, 0.2) and
+    K ~ U(4, 6): the general Newton-GMRES steady-state solve from θ = 0 (host wall time,
+    Newton iterations, final residual)."""
+    import torch
+
+    import nd_gb300 as nd
+    g = nd.barabasi_albert(nv, m, seed=seed + 1)
+    rng = np.random.default_rng(seed + 2)
+    om = rng.uniform(-0.2, 0.2, g.nv)
+    om -= om.mean()
+    K = rng.uniform(4, 6, g.ne)
+    nw = nd.adapt(nd.Network(g, nd.kuramoto_first(), nd.kuramoto_edge()), torch.float64)
+    p = np.concatenate([om, K])
+    nd.find_fixpoint(nw, p, tol=1e-10)  # builds the Jacobian pattern
+    _sync()
+    t0 = time.perf_counter()
+    u = nd.find_fixpoint(nw, p, tol=1e-10)
+    _sync()
+    el = time.perf_counter() - t0
+    st = nd.find_fixpoint.last_stats
+    return {"workload": f"Kuramoto (first order) on Barabasi-Albert N={nv}, m={m}, from theta = 0",
+            "dim": nw.dim, "seconds": el, "newton_iters": st["newton_iters"], "resid": st["resid"],
+            "theta_spread": float(u.max().item() - u.min().item())}
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("which", choices=["warmstart", "ensemble", "swing", "jacobian"])
+    ap.add_argument("which", choices=["warmstart", "ensemble", "swing", "jacobian", "fixpoint"])
     ap.add_argument("--train", type=int, default=20000)
     ap.add_argument("--test", type=int, default=2000)
     ap.add_argument("--nv", type=int, default=None)
@@ -299,6 +326,8 @@ def main():
         r = ensemble(a.instances, baseline_sample=a.sample, t_end=a.t_end)
     elif a.which == "jacobian":
         r = jacobian(a.nv or 1_000_000)
+    elif a.which == "fixpoint":
+        r = fixpoint(a.nv or 1_000_000)
     else:
         r = swing(a.nv or 100000)
     print(json.dumps(r), flush=True)

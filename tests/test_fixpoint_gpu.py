@@ -54,16 +54,18 @@ def test_kuramoto_matches_dense_newton(cuda):
     assert np.max(np.abs(on.rhs(u, p))) <= 1e-10
 
 
-def test_diffusion_converges_to_the_mean(cuda):
-    """du = -L u: every consensus state is a fixpoint; Newton-GMRES from u0 (a Krylov step
-    in the range of L, orthogonal to the constants) lands on mean(u0) everywhere."""
+def test_diffusion_converges_to_the_weighted_mean(cuda):
+    """du = -L u: every consensus state is a fixpoint.  The Newton step from u0 lies in
+    D^-1 range(L) (GMRES from 0, right-preconditioned by the diagonal D of the weighted
+    Laplacian), which keeps Σ d_i u_i: the solve lands on the degree-weighted mean of u0."""
     g = nd.barabasi_albert(2000, 3, seed=5)
     net = nd.Network(g, nd.diffusion_vertex(), nd.diffusion_edge())
     rng = np.random.default_rng(5)
     u0 = rng.normal(size=g.nv)
     w = rng.uniform(0.5, 1.5, g.ne)
     u = nd.find_fixpoint(adapt(net), w, x0=u0).cpu().numpy()
-    np.testing.assert_allclose(u, u0.mean(), atol=1e-9)
+    d = np.bincount(g.src, weights=w, minlength=g.nv) + np.bincount(g.dst, weights=w, minlength=g.nv)
+    np.testing.assert_allclose(u, (d * u0).sum() / d.sum(), atol=1e-9)
 
 
 def test_batched_network_with_ode_edges(cuda):
