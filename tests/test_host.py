@@ -104,3 +104,25 @@ def test_ba_is_power_law_with_hubs():
     deg = g.degree()
     assert deg.min() == 4
     assert deg.max() > 300  # hubs well beyond the thread-per-vertex bucket
+
+
+def test_batch_limit_and_power_grid_layout():
+    """More distinct components than the batch table holds are rejected; a power-grid
+    network lays PQ buses (2 states) and generators (4 states) out batch by batch, with the
+    π-line parameters after every vertex parameter."""
+    g = nd.cycle_graph(6)
+    vf = [nd.pqnode(), nd.generator(), nd.pqnode(), nd.generator(), nd.generator(), nd.pqnode()]
+    nw = nd.Network(g, vf, nd.piline())
+    assert [m.name for m in nw.vertex_batches] == ["pqnode", "generator"]
+    assert [nw.vertex_state_index(v) for v in range(6)] == [0, 6, 2, 10, 14, 4]
+    assert nw.dim == 3 * 2 + 3 * 4 and nw.pdim == 3 * 2 + 3 * 11 + 6 * 4
+    assert [nw.edge_param_index(e) for e in range(6)] == [39 + 4 * e for e in range(6)]
+    with pytest.raises(nd.ArgumentError):
+        nw.pflat()  # P, Q and the machine data have no defaults
+    many = [nd.EdgeModel(f"e{i}", pdim=0, kind=nd.capi.ND_E_DIFFUSION_UNIT, coupling=c)
+            for i, c in enumerate(["AntiSymmetric", "Symmetric", "Directed"])]
+    assert len(nd.Network(g, nd.diffusion_vertex(), [many[i % 3] for i in range(6)]).edge_batches) == 3
+    big = nd.cycle_graph(40)
+    kinds = [nd.EdgeModel(f"e{i}", pdim=0, kind=i + 100, coupling="AntiSymmetric") for i in range(40)]
+    with pytest.raises(nd.UnsupportedComponentError):
+        nd.Network(big, nd.diffusion_vertex(), kinds)
