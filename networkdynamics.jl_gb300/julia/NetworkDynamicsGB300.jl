@@ -29,6 +29,7 @@ using NetworkDynamics: NetworkDynamics, Network, ExecutionStyle, AntiSymmetric, 
                        executionstyle
 using CUDA: CUDA, CuArray, CuPtr
 using Adapt: Adapt
+using SparseArrays: SparseArrays
 
 export GB300Execution, GB300Aggregator, register_gb300_vertex!, register_gb300_edge!
 
@@ -186,6 +187,46 @@ function (nw::Network{<:GB300Execution})(du::CuArray{T}, u::CuArray{T}, p, t) wh
                 a.handle, dtype, pointer(du), length(du), pointer(u), length(u), pp, np, Float64(t),
                 CUDA.stream().handle))
     nothing
+end
+
+# Sparsity pattern of ∂f/∂u, the method get_jac_prototype takes for GB300 networks
+# (ext/NetworkDynamicsSparsityExt.jl:57-127 traces the RHS instead): the structural pattern
+# of the library components from nd_jacobian_pattern, as the SparseMatrixCSC that
+# set_jac_prototype! stores.
+function NetworkDynamics.get_jac_prototype(nw::Network{<:GB300Execution}; kwargs...)
+    a = nw.layer.aggregator
+    a.handle == C_NULL && throw(ArgumentError("adapt the network with adapt(CuArray{T}, nw) first"))
+    nnz = Ref{Int64}(0)
+    check(ccall((:nd_jacobian_pattern, libnd), Cint, (Ptr{Cvoid}, Ref{Int64}, Ptr{Int32}, Ptr{Int32}),
+                a.handle, nnz, C_NULL, C_NULL))
+    n = NetworkDynamics.dim(nw)
+    rowptr = Vector{Int32}(undef, n + 1)
+    colidx = Vector{Int32}(undef, nnz[])
+    check(ccall((:nd_jacobian_pattern, libnd), Cint, (Ptr{Cvoid}, Ref{Int64}, Ptr{Int32}, Ptr{Int32}),
+                a.handle, nnz, rowptr, colidx))
+    rows = Int[]
+    for i in 1:n, _ in (rowptr[i] + 1):rowptr[i + 1]
+        push!(rows, i)
+    end
+    SparseArrays.sparse(rows, Int.(colidx) .+ 1, trues(length(colidx)), n, n)
+end
+
+# find_fixpoint(nw, x0, p) for GB300 networks: Newton-GMRES on the device (nd_find_fixpoint)
+# instead of a SteadyStateProblem on the host (src/initialization.jl:44-144).
+function NetworkDynamics.find_fixpoint(nw::Network{<:GB300Execution}, x0::CuArray{Float64}, p::CuArray{Float64};
+                                       t=NaN, tol=1e-10, maxiters=50, kwargs...)
+    a = nw.layer.aggregator
+    u = copy(x0)
+    iters = Ref{Int32}(0)
+    resid = Ref{Float64}(NaN)
+    code = ccall((:nd_find_fixpoint, libnd), Cint,
+                 (Ptr{Cvoid}, CuPtr{Float64}, CuPtr{Float64}, Cdouble, Cdouble, Cint, Cint, Cint, Ref{Int32},
+                  Ref{Float64}, Ptr{Cvoid}),
+                 a.handle, pointer(u), pointer(p), Float64(t), tol, maxiters, 0, 0, iters, resid,
+                 CUDA.stream().handle)
+    code == Cint(-8) && throw(NetworkDynamics.NetworkInitError(last_error()))
+    check(code)
+    u
 end
 
 end # module
