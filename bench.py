@@ -452,7 +452,7 @@ def run_gb300(args, rank, world, local):
 # The reference's benchmark cases (benchmark/benchmark_cases.jl:20-102) at their largest N.
 # Graphs.jl's watts_strogatz(N, 3, 0.8) links div(3, 2) = 1 ring neighbour per side before
 # rewiring, which is k = 2 here.  powergrid_inhomogeneous_pq gives every PQ bus its own
-# component (its own batch), beyond the batch table of the GPU path.
+# component, so 50,001 vertex batches at N = 10^5.
 def _case_networks(N, name):
     import nd_gb300 as nd
     if name == "diffusion_static_edge":
@@ -465,13 +465,18 @@ def _case_networks(N, name):
     if name == "powergrid":
         kinds = np.random.default_rng(1).permutation(np.repeat([0, 1], N // 2))
         return g, [nd.pqnode() if k == 0 else nd.generator() for k in kinds], nd.piline()
+    if name == "powergrid_inhomogeneous_pq":  # every PQ bus closes over its own P, Q
+        rng = np.random.default_rng(1)
+        P, Q = -rng.random(N // 2), -rng.random(N // 2)
+        vm = [nd.pqnode_inhomogeneous(P[i], Q[i]) for i in range(N // 2)] + [nd.generator() for _ in range(N - N // 2)]
+        return g, [vm[i] for i in rng.permutation(N)], nd.piline()
     kinds = np.random.default_rng(1).permutation(np.repeat([0, 1], N // 2))
     return g, [nd.kuramoto_vertex_1d() if k == 0 else nd.kuramoto_vertex_2d() for k in kinds], \
         nd.static_kuramoto_edge()
 
 
 CASES = (("diffusion_static_edge", 3000), ("diffusion_ode_edge", 3000), ("kuramoto_homogeneous", 100_000),
-         ("kuramoto_heterogeneous", 100_000), ("powergrid", 100_000))
+         ("kuramoto_heterogeneous", 100_000), ("powergrid", 100_000), ("powergrid_inhomogeneous_pq", 100_000))
 
 
 def run_cases(args):
@@ -492,7 +497,7 @@ def run_cases(args):
         rng = np.random.default_rng(2)
         u = rng.normal(size=net.dim)
         p = rng.uniform(0.5, 1.5, size=net.pdim)
-        if name == "powergrid":  # line and machine data in the ranges of per-unit grid models
+        if name.startswith("powergrid"):  # line and machine data in the ranges of per-unit grid models
             p = net.pflat(vertex={"P": rng.uniform(-1, 1, g.nv), "Q": rng.uniform(-1, 1, g.nv), "H": 5.0,
                                   "D": 0.1, "Ω": 2 * np.pi * 50, "E_f": 1.0, "T_d_dash": 7.0, "T_q_dash": 0.5,
                                   "X_d_dash": 0.3, "X_q_dash": 0.6, "X_d": 1.8, "X_q": 1.7},
@@ -526,7 +531,9 @@ def run_cases(args):
                          "path": "batched" if "batched_rows" in launches else "homogeneous"}
         vb = [m.kind for m in net.vertex_batches]
         eb = [(m.kind, capi.COUPLINGS[m.coupling]) for m in net.edge_batches]
-        on = O.OracleNetwork.from_batches(g.nv, g.src, g.dst, vb, net.vertex_batch, eb, net.edge_batch)
+        consts = [m.constants or (0.0, 0.0) for m in net.vertex_batches]
+        on = O.OracleNetwork.from_batches(g.nv, g.src, g.dst, vb, net.vertex_batch, eb, net.edge_batch,
+                                          vertex_constants=consts)
         for tag, fn, threads in (("cpu_sequential", on.rhs, 1), ("cpu_threaded", on.rhs_poly, os.cpu_count() or 1)):
             O.load().nd_oracle_set_num_threads(threads)
             fn(u, p)

@@ -56,8 +56,10 @@ enum nd_vertex_kind {
     /* Power-grid vertices: complex voltage output (StateMask(1:2)), complex current input. */
     ND_V_PQ = 5,        /* pq!  algebraic PQ bus (mass matrix 0): du = S / conj(i), S = P + iQ
                            benchmark/benchmark_models.jl:65-74                                 dim 2, pdim 2 (P,Q)    */
-    ND_V_GENERATOR = 6  /* gen!  generator with states (u_r, u_i, θ, ω)
+    ND_V_GENERATOR = 6, /* gen!  generator with states (u_r, u_i, θ, ω)
                            benchmark/benchmark_models.jl:76-111                                dim 4, pdim 11         */
+    ND_V_PQ_CONST = 7   /* pq! of pqnode_inhomogeneous: the PQ bus closing over its own P, Q,
+                           taken from its batch's constants (P, Q)   benchmark_models.jl:113-123  dim 2, pdim 0 */
 };
 enum nd_edge_kind {
     ND_E_DIFFUSION = 1,      /* diffusionedge!   e = w·(vs-vd)   test/ComponentLibrary.jl:8-13   pdim 1 (w) */
@@ -160,14 +162,17 @@ int nd_create(const nd_network_desc* desc, int dtype, nd_handle** out);
  *                    enum nd_edge_kind with its enum nd_coupling (ND_ERR_UNSUPPORTED_COMPONENT
  *                    for a pair outside the library)
  *   n_*_batches      1..ND_MAX_BATCHES vertex batches; 0..ND_MAX_BATCHES edge batches (0
- *                    only without edges).  A batch may be empty.
+ *                    only without edges).  A batch may be empty.  Components that close
+ *                    over values of their own (pqnode_inhomogeneous) are one batch per
+ *                    distinct value, their values in vertex_constants.
  * The RHS follows the reference's order of operations and SequentialAggregator's order
  * of additions (ascending output index).  Networks of one static AntiSymmetric edge
  * batch and one vertex batch of kinds 1-3 take the same kernels as nd_create; all others
  * a batched two-kernel RHS (edge kernel with per-batch dispatch, then row sums and
  * vertex functions).  nd_jvp of a batched handle assembles the sparse Jacobian
  * (nd_jacobian) and multiplies; the ensemble calls do not take batched handles. */
-#define ND_MAX_BATCHES 32
+#define ND_MAX_BATCHES (1 << 20)
+#define ND_BATCH_CONSTANTS 2 /* numbers per vertex batch in vertex_constants */
 typedef struct nd_batch {
     int32_t kind;     /* enum nd_vertex_kind / enum nd_edge_kind */
     int32_t coupling; /* edge batches: enum nd_coupling; vertex batches: 0 */
@@ -185,6 +190,9 @@ typedef struct nd_batched_network_desc {
     const int32_t* edge_batch;      /* [ne] host: batch index of every edge            */
     int32_t flags;                  /* reserved, must be 0                             */
     int32_t reserved;
+    const double* vertex_constants; /* [n_vertex_batches * ND_BATCH_CONSTANTS] host, or
+                                       NULL: values a component closes over (the P, Q of
+                                       ND_V_PQ_CONST); required when that kind is used  */
 } nd_batched_network_desc;
 int nd_create_batched(const nd_batched_network_desc* desc, int dtype, nd_handle** out);
 

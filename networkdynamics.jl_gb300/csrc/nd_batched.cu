@@ -20,6 +20,7 @@
 // Homogeneous networks of the static AntiSymmetric kinds keep the two-phase kernels of
 // nd_rhs_edge.cu; this path covers everything else in the library.
 #include <algorithm>
+#include <cstring>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -51,8 +52,7 @@ struct BatchedKArgs {
     const void* u;
     const void* p;
     int64_t nv, ne, n_warp_rows;
-    const BatchTable* vb;  // device copies of the batch tables
-    const BatchTable* eb;
+    BatchTableDev vb, eb;  // the batch tables (device arrays)
     const int2* eu;
     const uint32_t* tptr;
     const int32_t* tidx;
@@ -78,15 +78,15 @@ __global__ void __launch_bounds__(kBlock) batched_edge_kernel(BatchedKArgs a) {
     V2* __restrict__ y2 = static_cast<V2*>(a.y2);
     for (int64_t k = (int64_t)blockIdx.x * kBlock + threadIdx.x; k < a.ne; k += (int64_t)gridDim.x * kBlock) {
         const int b = find_batch(a.eb, k);
-        const int kind = __ldg(&a.eb->kind[b]);
-        const int64_t r = k - __ldg(&a.eb->pos0[b]);
+        const int kind = __ldg(a.eb.kind + b);
+        const int64_t r = k - __ldg(a.eb.pos0 + b);
         const int2 uv = __ldg(a.eu + k);
         const T vs = __ldg(u + uv.x), vd = __ldg(u + uv.y);  // vertex outputs: StateMask(1)
         V2 y;
         if (kind == ND_E_DIFFUSION_ODE || kind == ND_E_DIFFUSION_ODE_FIXED) {
-            const int64_t s = __ldg(&a.eb->s0[b]) + 2 * r;
+            const int64_t s = __ldg(a.eb.s0 + b) + 2 * r;
             const T e1 = __ldg(u + s), e2 = __ldg(u + s + 1);
-            const T rate = kind == ND_E_DIFFUSION_ODE ? A::div(T(1), __ldg(p + __ldg(&a.eb->p0[b]) + r)) : T(100);
+            const T rate = kind == ND_E_DIFFUSION_ODE ? A::div(T(1), __ldg(p + __ldg(a.eb.p0 + b) + r)) : T(100);
             T d1, d2;
             ode_edge_f<T>(rate, vs, vd, e1, e2, d1, d2);
             du[s] = d1;
@@ -94,9 +94,9 @@ __global__ void __launch_bounds__(kBlock) batched_edge_kernel(BatchedKArgs a) {
             y.x = e2;  // Fiducial(dst=1:1, src=2:2): y_src = e2, y_dst = e1
             y.y = e1;
         } else {
-            const T w = kind == ND_E_DIFFUSION_UNIT ? T(0) : __ldg(p + __ldg(&a.eb->p0[b]) + r);
+            const T w = kind == ND_E_DIFFUSION_UNIT ? T(0) : __ldg(p + __ldg(a.eb.p0 + b) + r);
             const T yd = static_edge_g<T>(kind, vs, vd, w);
-            const int c = __ldg(&a.eb->coupling[b]);
+            const int c = __ldg(a.eb.coupling + b);
             // AntiSymmetric and the two-sided diffusionedge_fid!: y_src = -y_dst (a sign
             // flip); Symmetric: y_src = y_dst; Directed: y_src = +0 (fill! with zero)
             y.x = c == ND_SYMMETRIC ? yd : (c == ND_DIRECTED ? T(0) : -yd);
@@ -223,9 +223,9 @@ __device__ __forceinline__ T warp_row_sum(const T* __restrict__ y2, const int32_
 template <typename T>
 __device__ __forceinline__ void batched_vertex_f(const BatchedKArgs& a, int64_t pos, T acc) {
     const int b = find_batch(a.vb, pos);
-    const int kind = __ldg(&a.vb->kind[b]);
-    const int64_t r = pos - __ldg(&a.vb->pos0[b]);
-    const int64_t s0 = __ldg(&a.vb->s0[b]), q0 = __ldg(&a.vb->p0[b]);
+    const int kind = __ldg(a.vb.kind + b);
+    const int64_t r = pos - __ldg(a.vb.pos0 + b);
+    const int64_t s0 = __ldg(a.vb.s0 + b), q0 = __ldg(a.vb.p0 + b);
     T* du = static_cast<T*>(a.du);
     const T* u = static_cast<const T*>(a.u);
     const T* p = static_cast<const T*>(a.p);
@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(kBlock) batched_edge_kernel2(BatchedKArgs a) {
     V2* __restrict__ y2 = static_cast<V2*>(a.y2);
     for (int64_t k = (int64_t)blockIdx.x * kBlock + threadIdx.x; k < a.ne; k += (int64_t)gridDim.x * kBlock) {
         const int b = find_batch(a.eb, k);  // every edge batch is a pi-line batch
-        const int64_t q = __ldg(&a.eb->p0[b]) + 4 * (k - __ldg(&a.eb->pos0[b]));
+        const int64_t q = __ldg(a.eb.p0 + b) + 4 * (k - __ldg(a.eb.pos0 + b));
         const int2 uv = __ldg(a.eu + k);
         const Cx<T> vs = {__ldg(u + uv.x), __ldg(u + uv.x + 1)}, vd = {__ldg(u + uv.y), __ldg(u + uv.y + 1)};
         Cx<T> ys, yd;
@@ -326,15 +326,23 @@ __global__ void __launch_bounds__(kRowBlock) batched_row_kernel2(BatchedKArgs a)
     }
     const int64_t pos = __ldg(a.slot_vpos + slot);
     const int b = find_batch(a.vb, pos);
-    const int64_t r = pos - __ldg(&a.vb->pos0[b]);
-    const int64_t s0 = __ldg(&a.vb->s0[b]), q0 = __ldg(&a.vb->p0[b]);
+    const int64_t r = pos - __ldg(a.vb.pos0 + b);
+    const int64_t s0 = __ldg(a.vb.s0 + b), q0 = __ldg(a.vb.p0 + b);
     T* du = static_cast<T*>(a.du);
     const T* u = static_cast<const T*>(a.u);
     const T* p = static_cast<const T*>(a.p);
-    if (__ldg(&a.vb->kind[b]) == ND_V_PQ)
+    const int kind = __ldg(a.vb.kind + b);
+    if (kind == ND_V_PQ) {
         vertex_f2_at<T, ND_V_PQ>(du, u, p, s0 + 2 * r, q0 + 2 * r, {re, im});
-    else
+    } else if (kind == ND_V_PQ_CONST) {  // P, Q are the batch's constants
+        const Cx<T> uc = cdiv<T>({(T)__ldg(a.vb.consts + kBatchConstants * b),
+                                  (T)__ldg(a.vb.consts + kBatchConstants * b + 1)},
+                                 {re, -im});
+        du[s0 + 2 * r] = uc.r;
+        du[s0 + 2 * r + 1] = uc.i;
+    } else {
         vertex_f2_at<T, ND_V_GENERATOR>(du, u, p, s0 + 4 * r, q0 + 11 * r, {re, im});
+    }
 }
 
 template <typename T>
@@ -347,8 +355,8 @@ cudaError_t launch_typed(const BatchedNet& b, void* du, const void* u, const voi
     a.nv = b.nv;
     a.ne = b.ne;
     a.n_warp_rows = b.n_warp_rows;
-    a.vb = b.d_vb;
-    a.eb = b.d_eb;
+    a.vb = b.dvb;
+    a.eb = b.deb;
     a.eu = b.eu;
     a.tptr = b.tptr;
     a.tidx = b.tidx;
@@ -399,9 +407,43 @@ int check_edge_component(int ek, int coupling) {
     return ND_OK;
 }
 
+// Both batch tables in one device allocation, and their device views.
+static cudaError_t upload_tables(BatchedNet& bn) {
+    auto bytes_of = [](const BatchTable& t) {
+        return (size_t)t.n * (2 * sizeof(int32_t) + 2 * sizeof(int64_t) + kBatchConstants * sizeof(double)) +
+               ((size_t)t.n + 1) * sizeof(int64_t);
+    };
+    const size_t total = bytes_of(bn.vb) + bytes_of(bn.eb) + 256;
+    cudaError_t err = cudaMalloc(&bn.table_mem, total);
+    if (err != cudaSuccess) return err;
+    std::vector<unsigned char> host(total, 0);
+    size_t off = 0;
+    auto place = [&](const void* src, size_t n) -> size_t {
+        off = (off + 7) & ~size_t(7);
+        const size_t at = off;
+        if (n) std::memcpy(host.data() + at, src, n);
+        off += n;
+        return at;
+    };
+    auto build = [&](const BatchTable& t, BatchTableDev& d) {
+        const unsigned char* base = static_cast<unsigned char*>(bn.table_mem);
+        d.n = t.n;
+        d.kind = reinterpret_cast<const int32_t*>(base + place(t.kind.data(), t.n * sizeof(int32_t)));
+        d.coupling = reinterpret_cast<const int32_t*>(base + place(t.coupling.data(), t.n * sizeof(int32_t)));
+        d.pos0 = reinterpret_cast<const int64_t*>(base + place(t.pos0.data(), (t.n + 1) * sizeof(int64_t)));
+        d.s0 = reinterpret_cast<const int64_t*>(base + place(t.s0.data(), t.n * sizeof(int64_t)));
+        d.p0 = reinterpret_cast<const int64_t*>(base + place(t.p0.data(), t.n * sizeof(int64_t)));
+        d.consts = t.consts.empty() ? nullptr
+                                    : reinterpret_cast<const double*>(
+                                          base + place(t.consts.data(), t.consts.size() * sizeof(double)));
+    };
+    build(bn.vb, bn.dvb);
+    build(bn.eb, bn.deb);
+    return cudaMemcpy(bn.table_mem, host.data(), off, cudaMemcpyHostToDevice);
+}
+
 void free_batched(BatchedNet* b) {
-    cudaFree(b->d_vb);
-    cudaFree(b->d_eb);
+    cudaFree(b->table_mem);
     cudaFree(b->eu);
     cudaFree(b->tptr);
     cudaFree(b->tidx);
@@ -426,11 +468,13 @@ int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out) {
     if (2 * ne > (int64_t)INT32_MAX) return fail(ND_ERR_UNSUPPORTED, "more than 2^30-1 edges in a batched network");
     for (int b = 0; b < nvb; ++b) {
         const nd_batch& vb = d->vertex_batches[b];
-        if (vb.kind < ND_V_DIFFUSION || vb.kind > ND_V_GENERATOR)
+        if (vb.kind < ND_V_DIFFUSION || vb.kind > ND_V_PQ_CONST)
             return fail(ND_ERR_UNSUPPORTED_COMPONENT,
                         "vertex model is not in the GB300 component library (diffusion, kuramoto first order, "
                         "swing, benchmark swing, PQ bus, generator); no CPU fallback exists");
         if (vb.coupling != 0) return fail(ND_ERR_ARG, "vertex batches take coupling 0");
+        if (vb.kind == ND_V_PQ_CONST && !d->vertex_constants)
+            return fail(ND_ERR_ARG, "the PQ bus with its own P, Q needs vertex_constants");
     }
     for (int b = 0; b < neb; ++b) {
         const int rc = check_edge_component(d->edge_batches[b].kind, d->edge_batches[b].coupling);
@@ -464,12 +508,21 @@ int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out) {
     BatchTable vb, eb;
     int64_t pos = 0, st = 0, par = 0;
     vb.n = nvb;
+    vb.kind.resize(nvb);
+    vb.coupling.assign(nvb, 0);
+    vb.pos0.resize(nvb + 1);
+    vb.s0.resize(nvb);
+    vb.p0.resize(nvb);
+    vb.consts.assign((size_t)nvb * kBatchConstants, 0.0);
     for (int b = 0; b < nvb; ++b) {
         const int k = d->vertex_batches[b].kind;
         vb.kind[b] = k;
         vb.pos0[b] = pos;
         vb.s0[b] = st;
         vb.p0[b] = par;
+        if (d->vertex_constants)
+            for (int c = 0; c < kBatchConstants; ++c)
+                vb.consts[(size_t)b * kBatchConstants + c] = d->vertex_constants[(size_t)b * kBatchConstants + c];
         pos += vcount[b];
         st += vcount[b] * vertex_dim(k);
         par += vcount[b] * vertex_pdim(k);
@@ -477,6 +530,11 @@ int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out) {
     vb.pos0[nvb] = pos;
     const int64_t vdim_total = st;
     eb.n = neb;
+    eb.kind.resize(neb);
+    eb.coupling.resize(neb);
+    eb.pos0.resize(neb + 1);
+    eb.s0.resize(neb);
+    eb.p0.resize(neb);
     pos = 0;
     for (int b = 0; b < neb; ++b) {
         const int k = d->edge_batches[b].kind;
@@ -494,7 +552,7 @@ int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out) {
     (void)vdim_total;
 
     // vertex positions and the u index of every vertex output (its first state)
-    std::vector<int64_t> fill(vb.pos0, vb.pos0 + nvb);
+    std::vector<int64_t> fill(vb.pos0.begin(), vb.pos0.begin() + nvb);
     std::vector<int32_t> vpos(nv), vdata(nv);
     for (int64_t v = 0; v < nv; ++v) {
         const int b = d->vertex_batch[v];
@@ -503,7 +561,7 @@ int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out) {
         vdata[v] = (int32_t)(vb.s0[b] + (k - vb.pos0[b]) * vertex_dim(vb.kind[b]));
     }
     // edge positions
-    std::vector<int64_t> efill(eb.pos0, eb.pos0 + std::max(neb, 0));
+    std::vector<int64_t> efill(eb.pos0.begin(), eb.pos0.begin() + neb);
     std::vector<int64_t> order(ne);
     for (int64_t e = 0; e < ne; ++e) order[efill[d->edge_batch[e]]++] = e;
     std::vector<int2> eu(ne);
@@ -574,8 +632,7 @@ int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out) {
         return err;
     };
     cudaError_t err;
-    if ((err = upload((void**)&bn.d_vb, &vb, sizeof(BatchTable))) != cudaSuccess ||
-        (err = upload((void**)&bn.d_eb, &eb, sizeof(BatchTable))) != cudaSuccess ||
+    if ((err = upload_tables(bn)) != cudaSuccess ||
         (err = upload((void**)&bn.eu, eu.data(), eu.size() * sizeof(int2))) != cudaSuccess ||
         (err = upload((void**)&bn.tptr, tptr.data(), tptr.size() * sizeof(uint32_t))) != cudaSuccess ||
         (err = upload((void**)&bn.tidx, tidx.data(), tidx.size() * sizeof(int32_t))) != cudaSuccess ||

@@ -33,11 +33,12 @@ constexpr int32_t kSrcSideBit = int32_t(0x80000000u);
 
 // Dimensions of the library components.
 inline int vertex_dim(int vk) {
-    return vk == ND_V_GENERATOR ? 4 : (vk == ND_V_SWING || vk == ND_V_SWING_UNIT || vk == ND_V_PQ ? 2 : 1);
+    return vk == ND_V_GENERATOR ? 4
+                                : (vk == ND_V_SWING || vk == ND_V_SWING_UNIT || vk == ND_V_PQ || vk == ND_V_PQ_CONST ? 2 : 1);
 }
 inline int vertex_pdim(int vk) {
     switch (vk) {
-        case ND_V_DIFFUSION: return 0;
+        case ND_V_DIFFUSION: case ND_V_PQ_CONST: return 0;
         case ND_V_KURAMOTO: case ND_V_SWING_UNIT: return 1;
         case ND_V_SWING: return 3;
         case ND_V_PQ: return 2;
@@ -49,7 +50,7 @@ inline int edge_pdim(int ek) {
     return ek == ND_E_DIFFUSION_UNIT || ek == ND_E_DIFFUSION_ODE_FIXED ? 0 : (ek == ND_E_PILINE ? 4 : 1);
 }
 // output dimension (vdepth / edepth)
-inline int vertex_outdim(int vk) { return vk == ND_V_PQ || vk == ND_V_GENERATOR ? 2 : 1; }
+inline int vertex_outdim(int vk) { return vk == ND_V_PQ || vk == ND_V_GENERATOR || vk == ND_V_PQ_CONST ? 2 : 1; }
 inline int edge_outdim(int ek) { return ek == ND_E_PILINE ? 2 : 1; }
 
 // Degree buckets.  Rows with degree <= kMediumMaxDeg are processed in windows: a block
@@ -167,19 +168,31 @@ enum KernelKind : int {
 };
 
 // ---- batched (heterogeneous) networks -------------------------------------------------------
-// Batch table of one component class (vertices or edges), passed to the kernels by value.
-// Components are numbered by "position": their rank in the reference's batch-major order;
-// batch b holds positions [pos0[b], pos0[b+1]), its states start at s0[b] with stride
-// dim(kind), its parameters at p0[b] with stride pdim(kind) (the BatchStride of
-// src/utils.jl:1-35).
-constexpr int kMaxBatches = ND_MAX_BATCHES;
+// Batch table of one component class (vertices or edges).  Components are numbered by
+// "position": their rank in the reference's batch-major order; batch b holds positions
+// [pos0[b], pos0[b+1]), its states start at s0[b] with stride dim(kind), its parameters at
+// p0[b] with stride pdim(kind) (the BatchStride of src/utils.jl:1-35).  consts holds
+// kBatchConstants numbers per batch for components that close over values of their own
+// (the PQ bus of pqnode_inhomogeneous).  Tables can hold many batches (one per component
+// when every component is distinct), so the kernels read them from device memory.
+constexpr int64_t kMaxBatches = ND_MAX_BATCHES;
+constexpr int kBatchConstants = ND_BATCH_CONSTANTS;
 struct BatchTable {
     int32_t n = 0;
-    int32_t kind[kMaxBatches] = {};
-    int32_t coupling[kMaxBatches] = {};
-    int64_t pos0[kMaxBatches + 1] = {};
-    int64_t s0[kMaxBatches] = {};
-    int64_t p0[kMaxBatches] = {};
+    std::vector<int32_t> kind, coupling;
+    std::vector<int64_t> pos0;  // n + 1 entries
+    std::vector<int64_t> s0, p0;
+    std::vector<double> consts;  // kBatchConstants per batch
+};
+// The device copy, passed to the kernels by value.
+struct BatchTableDev {
+    int32_t n = 0;
+    const int32_t* kind = nullptr;
+    const int32_t* coupling = nullptr;
+    const int64_t* pos0 = nullptr;
+    const int64_t* s0 = nullptr;
+    const int64_t* p0 = nullptr;
+    const double* consts = nullptr;
 };
 
 // Device data of a batched network.  Edge values go to y2, two per edge position k:
@@ -189,9 +202,9 @@ struct BatchTable {
 // additions (src/aggregators.jl:140-151).
 struct BatchedNet {
     bool enabled = false;
-    BatchTable vb, eb;                                 // host copies
-    BatchTable* d_vb = nullptr;                        // device copies, read by the kernels
-    BatchTable* d_eb = nullptr;
+    BatchTable vb, eb;                // host copies
+    BatchTableDev dvb, deb;           // device copies, read by the kernels
+    void* table_mem = nullptr;        // the device memory behind dvb and deb
     int64_t nv = 0, ne = 0, dim = 0, pdim = 0;
     int32_t max_degree = 0;
     int32_t depth = 1;           // output dimension of vertices and edge sides (2: complex)
@@ -204,15 +217,28 @@ struct BatchedNet {
 };
 
 #ifdef __CUDACC__
-// Batch of position `pos`: the last batch whose first position is <= pos (batches are few;
-// empty batches are skipped because the next one starts at the same position).
-__device__ __forceinline__ int find_batch(const BatchTable* __restrict__ t, int64_t pos) {
-    const int n = __ldg(&t->n);
-    int b = 0;
-    while (b + 1 < n && pos >= __ldg(&t->pos0[b + 1])) ++b;
-    return b;
+// Batch of position `pos`: the last batch whose first position is <= pos, by binary search
+// (an empty batch starts where the next one does, so it is never the answer).
+__device__ __forceinline__ int find_batch(const BatchTableDev& t, int64_t pos) {
+    int lo = 0, hi = t.n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(t.pos0 + mid) <= pos) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
 }
 #endif
+// The same on the host table.
+inline int host_find_batch(const BatchTable& t, int64_t pos) {
+    int lo = 0, hi = t.n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (t.pos0[mid] <= pos) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
 
 int check_edge_component(int edge_kind, int coupling);  // ND_OK or ND_ERR_UNSUPPORTED_COMPONENT
 // elem: scratch element size (4 / 8); 0 builds the structure without the y2 scratch (a

@@ -35,11 +35,6 @@ constexpr int kJacBlock = 128;
 bool is_ode(int ek) { return ek == ND_E_DIFFUSION_ODE || ek == ND_E_DIFFUSION_ODE_FIXED; }
 bool is_swing(int vk) { return vk == ND_V_SWING || vk == ND_V_SWING_UNIT; }
 
-int host_find_batch(const BatchTable& t, int64_t pos) {
-    int b = 0;
-    while (b + 1 < t.n && pos >= t.pos0[b + 1]) ++b;
-    return b;
-}
 
 template <typename T>
 struct JacArgs {
@@ -49,8 +44,7 @@ struct JacArgs {
     const int32_t* rowptr;
     const int32_t* colidx;
     int64_t nv, ne;
-    const BatchTable* vb;
-    const BatchTable* eb;
+    BatchTableDev vb, eb;
     const int2* eu;
     const uint32_t* tptr;
     const int32_t* tidx;
@@ -112,11 +106,11 @@ __global__ void __launch_bounds__(kJacBlock) jac_vertex_kernel(JacArgs<T> a) {
     if (__ldg(a.tptr + slot + 1) - __ldg(a.tptr + slot) > kJacLongRow) return;
     const int64_t pos = __ldg(a.slot_vpos + slot);
     const int b = find_batch(a.vb, pos);
-    const int vk = __ldg(&a.vb->kind[b]);
-    const int64_t r = pos - __ldg(&a.vb->pos0[b]);
+    const int vk = __ldg(a.vb.kind + b);
+    const int64_t r = pos - __ldg(a.vb.pos0 + b);
     const int dim = vk == ND_V_SWING || vk == ND_V_SWING_UNIT ? 2 : 1;
     const int pd = vk == ND_V_DIFFUSION ? 0 : (vk == ND_V_SWING ? 3 : 1);
-    const int64_t s = __ldg(&a.vb->s0[b]) + dim * r, q = __ldg(&a.vb->p0[b]) + pd * r;
+    const int64_t s = __ldg(a.vb.s0 + b) + dim * r, q = __ldg(a.vb.p0 + b) + pd * r;
     T scale = T(1);
     if (dim == 2) {
         // dθ = ω
@@ -143,18 +137,18 @@ __global__ void __launch_bounds__(kJacBlock) jac_vertex_kernel(JacArgs<T> a) {
         const int64_t k = t >> 1;
         const bool dst_side = t & 1;
         const int eb = find_batch(a.eb, k);
-        const int ek = __ldg(&a.eb->kind[eb]);
-        const int64_t re = k - __ldg(&a.eb->pos0[eb]);
+        const int ek = __ldg(a.eb.kind + eb);
+        const int64_t re = k - __ldg(a.eb.pos0 + eb);
         if (ek == ND_E_DIFFUSION_ODE || ek == ND_E_DIFFUSION_ODE_FIXED) {
             // Fiducial(dst=1:1, src=2:2): this vertex receives e1 (destination) or e2 (source)
-            const int64_t es = __ldg(&a.eb->s0[eb]) + 2 * re + (dst_side ? 0 : 1);
+            const int64_t es = __ldg(a.eb.s0 + eb) + 2 * re + (dst_side ? 0 : 1);
             jadd<T>(vals, cols, n, (int32_t)es, scale);
             continue;
         }
-        const int c = __ldg(&a.eb->coupling[eb]);
+        const int c = __ldg(a.eb.coupling + eb);
         if (!dst_side && c == ND_DIRECTED) continue;  // y_src = 0
         const int2 o = __ldg(a.eu + k);
-        const T w = ek == ND_E_DIFFUSION_UNIT ? T(0) : __ldg(a.p + __ldg(&a.eb->p0[eb]) + re);
+        const T w = ek == ND_E_DIFFUSION_UNIT ? T(0) : __ldg(a.p + __ldg(a.eb.p0 + eb) + re);
         T gs, gd;
         static_edge_dg<T>(ek, __ldg(a.u + o.x), __ldg(a.u + o.y), w, gs, gd);
         // source side: y_src = -y_dst (AntiSymmetric, two-sided fiducial) or y_dst (Symmetric)
@@ -178,11 +172,11 @@ __global__ void __launch_bounds__(kJacBlock) jac_long_row_kernel(JacArgs<T> a, c
     const int64_t slot = __ldg(slots + w);
     const int64_t pos = __ldg(a.slot_vpos + slot);
     const int b = find_batch(a.vb, pos);
-    const int vk = __ldg(&a.vb->kind[b]);
-    const int64_t r = pos - __ldg(&a.vb->pos0[b]);
+    const int vk = __ldg(a.vb.kind + b);
+    const int64_t r = pos - __ldg(a.vb.pos0 + b);
     const int dim = vk == ND_V_SWING || vk == ND_V_SWING_UNIT ? 2 : 1;
     const int pd = vk == ND_V_DIFFUSION ? 0 : (vk == ND_V_SWING ? 3 : 1);
-    const int64_t s = __ldg(&a.vb->s0[b]) + dim * r, q = __ldg(&a.vb->p0[b]) + pd * r;
+    const int64_t s = __ldg(a.vb.s0 + b) + dim * r, q = __ldg(a.vb.p0 + b) + pd * r;
     T scale = T(1);
     if (dim == 2) {
         T dw = T(-1);
@@ -209,16 +203,16 @@ __global__ void __launch_bounds__(kJacBlock) jac_long_row_kernel(JacArgs<T> a, c
         const int64_t k = t >> 1;
         const bool dst_side = t & 1;
         const int eb = find_batch(a.eb, k);
-        const int ek = __ldg(&a.eb->kind[eb]);
-        const int64_t re = k - __ldg(&a.eb->pos0[eb]);
+        const int ek = __ldg(a.eb.kind + eb);
+        const int64_t re = k - __ldg(a.eb.pos0 + eb);
         if (ek == ND_E_DIFFUSION_ODE || ek == ND_E_DIFFUSION_ODE_FIXED) {
-            jadd_atomic<T>(vals, cols, n, (int32_t)(__ldg(&a.eb->s0[eb]) + 2 * re + (dst_side ? 0 : 1)), scale);
+            jadd_atomic<T>(vals, cols, n, (int32_t)(__ldg(a.eb.s0 + eb) + 2 * re + (dst_side ? 0 : 1)), scale);
             continue;
         }
-        const int c = __ldg(&a.eb->coupling[eb]);
+        const int c = __ldg(a.eb.coupling + eb);
         if (!dst_side && c == ND_DIRECTED) continue;
         const int2 o = __ldg(a.eu + k);
-        const T wgt = ek == ND_E_DIFFUSION_UNIT ? T(0) : __ldg(a.p + __ldg(&a.eb->p0[eb]) + re);
+        const T wgt = ek == ND_E_DIFFUSION_UNIT ? T(0) : __ldg(a.p + __ldg(a.eb.p0 + eb) + re);
         T gs, gd;
         static_edge_dg<T>(ek, __ldg(a.u + o.x), __ldg(a.u + o.y), wgt, gs, gd);
         const T f = dst_side || c == ND_SYMMETRIC ? scale : -scale;
@@ -239,12 +233,12 @@ __global__ void __launch_bounds__(kJacBlock) jac_ode_edge_kernel(JacArgs<T> a) {
     const int64_t k = (int64_t)blockIdx.x * kJacBlock + threadIdx.x;
     if (k >= a.ne) return;
     const int eb = find_batch(a.eb, k);
-    const int ek = __ldg(&a.eb->kind[eb]);
+    const int ek = __ldg(a.eb.kind + eb);
     if (ek != ND_E_DIFFUSION_ODE && ek != ND_E_DIFFUSION_ODE_FIXED) return;
-    const int64_t re = k - __ldg(&a.eb->pos0[eb]);
-    const int64_t es = __ldg(&a.eb->s0[eb]) + 2 * re;
+    const int64_t re = k - __ldg(a.eb.pos0 + eb);
+    const int64_t es = __ldg(a.eb.s0 + eb) + 2 * re;
     const int2 o = __ldg(a.eu + k);
-    const T rate = ek == ND_E_DIFFUSION_ODE ? A::div(T(1), __ldg(a.p + __ldg(&a.eb->p0[eb]) + re)) : T(100);
+    const T rate = ek == ND_E_DIFFUSION_ODE ? A::div(T(1), __ldg(a.p + __ldg(a.eb.p0 + eb) + re)) : T(100);
     const T c = A::mul(rate, A::cos_phase(A::sub(__ldg(a.u + o.x), __ldg(a.u + o.y))));
     // de1 = rate (sin(vs - vd) - e1), de2 = rate (sin(vd - vs) - e2)
     for (int i = 0; i < 2; ++i) {
@@ -399,8 +393,8 @@ cudaError_t launch_values(nd_handle* h, void* values, const void* u, const void*
     a.colidx = J.colidx;
     a.nv = b.nv;
     a.ne = b.ne;
-    a.vb = b.d_vb;
-    a.eb = b.d_eb;
+    a.vb = b.dvb;
+    a.eb = b.deb;
     a.eu = b.eu;
     a.tptr = b.tptr;
     a.tidx = b.tidx;

@@ -9,7 +9,7 @@ from ._capi import ArgumentError, NDError, NotConvergedError, UnsupportedCompone
 from .components import (AntiSymmetric, Directed, EdgeModel, Symmetric, VertexModel, diffusion_dedge, diffusion_edge,
                          diffusion_edge_fid, diffusion_edge_unit, diffusion_odeedge, diffusion_vertex, kuramoto_edge,
                          kuramoto_first, kuramoto_second, kuramoto_vertex_1d, kuramoto_vertex_2d, static_kuramoto_edge,
-                         static_line, swing_vertex, piline, pqnode, generator)
+                         static_line, swing_vertex, piline, pqnode, pqnode_inhomogeneous, generator)
 from .graphs import Graph, barabasi_albert, complete_graph, cycle_graph, random_geometric, simple_graph, watts_strogatz
 from .network import (ExecutionStyle, GB300Aggregator, GB300Execution, Network, adapt, get_aggr_constructor,
                       iscudacompatible, jacobian, jacobian_pattern, jvp)
@@ -21,7 +21,7 @@ __all__ = [
     "AntiSymmetric", "Directed", "EdgeModel", "Symmetric", "VertexModel", "diffusion_dedge", "diffusion_edge",
     "diffusion_edge_fid", "diffusion_edge_unit", "diffusion_odeedge", "diffusion_vertex", "kuramoto_edge",
     "kuramoto_first", "kuramoto_second", "kuramoto_vertex_1d", "kuramoto_vertex_2d", "static_kuramoto_edge",
-    "static_line", "swing_vertex", "piline", "pqnode", "generator",
+    "static_line", "swing_vertex", "piline", "pqnode", "pqnode_inhomogeneous", "generator",
     "Graph", "barabasi_albert", "complete_graph", "cycle_graph", "random_geometric", "simple_graph",
     "watts_strogatz",
     "ExecutionStyle", "GB300Aggregator", "GB300Execution", "Network", "adapt", "get_aggr_constructor",

@@ -29,6 +29,7 @@ ND_V_SWING = 3
 ND_V_SWING_UNIT = 4
 ND_V_PQ = 5
 ND_V_GENERATOR = 6
+ND_V_PQ_CONST = 7
 
 ND_E_DIFFUSION = 1
 ND_E_DIFFUSION_UNIT = 2
@@ -44,7 +45,8 @@ ND_FIDUCIAL = 4
 COUPLINGS = {"AntiSymmetric": ND_ANTISYMMETRIC, "Symmetric": ND_SYMMETRIC, "Directed": ND_DIRECTED,
              "Fiducial": ND_FIDUCIAL}
 
-ND_MAX_BATCHES = 32
+ND_MAX_BATCHES = 1 << 20
+ND_BATCH_CONSTANTS = 2
 
 ND_ORDER_SEQUENTIAL = 0
 ND_ORDER_TREE = 1
@@ -97,7 +99,7 @@ class nd_batched_network_desc(C.Structure):
                 ("n_vertex_batches", C.c_int32), ("n_edge_batches", C.c_int32),
                 ("vertex_batches", C.POINTER(nd_batch)), ("edge_batches", C.POINTER(nd_batch)),
                 ("vertex_batch", C.POINTER(C.c_int32)), ("edge_batch", C.POINTER(C.c_int32)),
-                ("flags", C.c_int32), ("reserved", C.c_int32)]
+                ("flags", C.c_int32), ("reserved", C.c_int32), ("vertex_constants", C.POINTER(C.c_double))]
 
 
 # Every symbol include/nd_gb300.h declares, with (restype, argtypes).

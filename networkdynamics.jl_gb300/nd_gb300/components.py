@@ -28,6 +28,7 @@ class VertexModel:
     g: object = 1                       # StateMask(1): the first state is the output
     outdim: int = 1                     # StateMask(1:outdim)
     mass_matrix: Optional[float] = None  # 0: algebraic states (the PQ bus); None: identity
+    constants: tuple = ()               # values the component function closes over
 
 
 @dataclass
@@ -174,3 +175,11 @@ def generator() -> VertexModel:
                        psym=("H", "P", "D", "Ω", "E_f", "T_d_dash", "T_q_dash", "X_d_dash", "X_q_dash", "X_d",
                              "X_q"),
                        pdef=(None,) * 11, kind=capi.ND_V_GENERATOR, outdim=2)
+
+
+def pqnode_inhomogeneous(P: float, Q: float) -> VertexModel:
+    """pq! closing over its own P and Q (pqnode_inhomogeneous, benchmark/benchmark_models.jl:
+    113-123): no parameters; every distinct (P, Q) is a component of its own, hence a batch
+    of its own."""
+    return VertexModel("pqnode_inhomogeneous", dim=2, pdim=0, sym=("u_r", "u_i"), kind=capi.ND_V_PQ_CONST, outdim=2,
+                       mass_matrix=0.0, constants=(float(P), float(Q)))

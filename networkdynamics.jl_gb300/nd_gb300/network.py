@@ -86,16 +86,14 @@ def _batches(models, key):
     """Batches of identical components in order of first appearance, as find_identical
     groups them (src/utils.jl:197-216, src/construction.jl:155-168): the model of every
     batch and the batch index of every component."""
-    keys, reps = [], []
+    index, reps = {}, []
     ids = np.empty(len(models), dtype=np.int32)
     for i, m in enumerate(models):
         k = key(m)
-        try:
-            b = keys.index(k)
-        except ValueError:
-            keys.append(k)
+        b = index.get(k)
+        if b is None:
+            b = index[k] = len(reps)
             reps.append(m)
-            b = len(keys) - 1
         ids[i] = b
     if len(reps) > capi.ND_MAX_BATCHES:
         raise capi.UnsupportedComponentError(capi.ND_ERR_UNSUPPORTED_COMPONENT,
@@ -143,7 +141,7 @@ class Network:
         if isinstance(vertexm, VertexModel):
             self.vertex_batches, self.vertex_batch = [vertexm], np.zeros(g.nv, dtype=np.int32)
         else:
-            self.vertex_batches, self.vertex_batch = _batches(vms, lambda m: m.kind)
+            self.vertex_batches, self.vertex_batch = _batches(vms, lambda m: (m.kind, m.constants))
         if isinstance(edgem, EdgeModel):
             self.edge_batches, self.edge_batch = [edgem], np.zeros(g.ne, dtype=np.int32)
         else:
@@ -225,7 +223,7 @@ class Network:
         dst = np.ascontiguousarray(g.dst, dtype=np.int64)
         P = C.POINTER(C.c_int64)
         h = C.c_void_p()
-        if self.homogeneous:
+        if self.homogeneous and not self.vertex_batches[0].constants:
             vm, em = self.vertex_batches[0], self.edge_batches[0]
             desc = capi.nd_network_desc(g.nv, g.ne, src.ctypes.data_as(P), dst.ctypes.data_as(P), vm.kind, em.kind,
                                         capi.COUPLINGS[em.coupling], 0)
@@ -237,9 +235,14 @@ class Network:
             vbi = np.ascontiguousarray(self.vertex_batch, dtype=np.int32)
             ebi = np.ascontiguousarray(self.edge_batch, dtype=np.int32)
             P32 = C.POINTER(C.c_int32)
+            nc = capi.ND_BATCH_CONSTANTS
+            consts = np.zeros((len(self.vertex_batches), nc), dtype=np.float64)
+            for b, m in enumerate(self.vertex_batches):
+                consts[b, :len(m.constants)] = m.constants
             desc = capi.nd_batched_network_desc(g.nv, g.ne, src.ctypes.data_as(P), dst.ctypes.data_as(P),
                                                 len(self.vertex_batches), len(self.edge_batches), vb, eb,
-                                                vbi.ctypes.data_as(P32), ebi.ctypes.data_as(P32), 0, 0)
+                                                vbi.ctypes.data_as(P32), ebi.ctypes.data_as(P32), 0, 0,
+                                                consts.ctypes.data_as(C.POINTER(C.c_double)))
             capi.check(lib.nd_create_batched(C.byref(desc), code, C.byref(h)))
         self._handle = h
         self._dtype = code

@@ -26,17 +26,17 @@
 #endif
 
 /* Component kinds and output wrappers: same numbering as the C ABI of the GB300 library. */
-enum { V_DIFFUSION = 1, V_KURAMOTO = 2, V_SWING = 3, V_SWING_UNIT = 4, V_PQ = 5, V_GENERATOR = 6 };
+enum { V_DIFFUSION = 1, V_KURAMOTO = 2, V_SWING = 3, V_SWING_UNIT = 4, V_PQ = 5, V_GENERATOR = 6, V_PQ_CONST = 7 };
 enum { E_DIFFUSION = 1, E_DIFFUSION_UNIT = 2, E_KURAMOTO = 3, E_DIFFUSION_ODE = 4, E_DIFFUSION_ODE_FIXED = 5,
        E_PILINE = 6 };
 enum { C_ANTISYMMETRIC = 1, C_SYMMETRIC = 2, C_DIRECTED = 3, C_FIDUCIAL = 4 };
 
 static int vdim(int vk) {
-    return vk == V_GENERATOR ? 4 : (vk == V_SWING || vk == V_SWING_UNIT || vk == V_PQ ? 2 : 1);
+    return vk == V_GENERATOR ? 4 : (vk == V_SWING || vk == V_SWING_UNIT || vk == V_PQ || vk == V_PQ_CONST ? 2 : 1);
 }
 static int vpdim(int vk) {
     switch (vk) {
-        case V_DIFFUSION: return 0;
+        case V_DIFFUSION: case V_PQ_CONST: return 0;
         case V_KURAMOTO: case V_SWING_UNIT: return 1;
         case V_SWING: return 3;
         case V_PQ: return 2;
@@ -49,7 +49,7 @@ static int epdim(int ek) {
     return ek == E_DIFFUSION_UNIT || ek == E_DIFFUSION_ODE_FIXED ? 0 : (ek == E_PILINE ? 4 : 1);
 }
 /* output dimension (vdepth / edepth): the power-grid components carry complex values */
-static int voutdim(int vk) { return vk == V_PQ || vk == V_GENERATOR ? 2 : 1; }
+static int voutdim(int vk) { return vk == V_PQ || vk == V_GENERATOR || vk == V_PQ_CONST ? 2 : 1; }
 static int eoutdim(int ek) { return ek == E_PILINE ? 2 : 1; }
 
 /*
@@ -65,6 +65,7 @@ typedef struct {
     const int64_t* src;
     const int64_t* dst;
     int32_t* vkind; /* [nv] kind of every vertex */
+    double* vconst; /* [2 nv] the constants of every vertex's batch (pqnode_inhomogeneous's P, Q) */
     int32_t* ekind; /* [ne] kind of every edge */
     int32_t* ecoup; /* [ne] output wrapper of every edge */
     /* layout, 0-based offsets */
@@ -86,12 +87,14 @@ typedef struct {
     int64_t* inv_idx;
 } layout_t;
 
-/* Batch order: batches in index order, components ascending inside a batch. */
+/* Batch order: batches in index order, components ascending inside a batch (a stable
+ * counting sort by batch). */
 static void batch_order(int64_t n, const int32_t* batch, int nb, int64_t* order) {
-    int64_t pos = 0;
-    for (int b = 0; b < nb; ++b)
-        for (int64_t i = 0; i < n; ++i)
-            if (batch[i] == b) order[pos++] = i;
+    int64_t* start = (int64_t*)calloc((size_t)nb + 1, sizeof(int64_t));
+    for (int64_t i = 0; i < n; ++i) start[batch[i] + 1]++;
+    for (int b = 0; b < nb; ++b) start[b + 1] += start[b];
+    for (int64_t i = 0; i < n; ++i) order[start[batch[i]]++] = i;
+    free(start);
 }
 
 void nd_oracle_layout_free(layout_t* L);
@@ -102,7 +105,8 @@ void nd_oracle_layout_free(layout_t* L);
  * order of first appearance when the caller numbers them that way. */
 layout_t* nd_oracle_layout_new_batched(int64_t nv, int64_t ne, const int64_t* src, const int64_t* dst,
                                        int nvb, const int32_t* vb_kind, const int32_t* vbatch, int neb,
-                                       const int32_t* eb_kind, const int32_t* eb_coup, const int32_t* ebatch) {
+                                       const int32_t* eb_kind, const int32_t* eb_coup, const int32_t* ebatch,
+                                       const double* vb_const) {
     layout_t* L = (layout_t*)calloc(1, sizeof(layout_t));
     L->nv = nv;
     L->ne = ne;
@@ -111,7 +115,14 @@ layout_t* nd_oracle_layout_new_batched(int64_t nv, int64_t ne, const int64_t* sr
     L->vkind = (int32_t*)malloc(sizeof(int32_t) * (nv + 1));
     L->ekind = (int32_t*)malloc(sizeof(int32_t) * (ne + 1));
     L->ecoup = (int32_t*)malloc(sizeof(int32_t) * (ne + 1));
-    for (int64_t v = 0; v < nv; ++v) L->vkind[v] = vb_kind[vbatch[v]];
+    L->vconst = (double*)calloc((size_t)(2 * nv + 2), sizeof(double));
+    for (int64_t v = 0; v < nv; ++v) {
+        L->vkind[v] = vb_kind[vbatch[v]];
+        if (vb_const) {
+            L->vconst[2 * v] = vb_const[2 * vbatch[v]];
+            L->vconst[2 * v + 1] = vb_const[2 * vbatch[v] + 1];
+        }
+    }
     for (int64_t e = 0; e < ne; ++e) {
         L->ekind[e] = eb_kind[ebatch[e]];
         L->ecoup[e] = eb_coup[ebatch[e]];
@@ -240,7 +251,7 @@ layout_t* nd_oracle_layout_new(int64_t nv, int64_t ne, const int64_t* src, const
         }
         eb[e] = b;
     }
-    layout_t* L = nd_oracle_layout_new_batched(nv, ne, src, dst, nvb, vk, vb, neb, ek, ec, eb);
+    layout_t* L = nd_oracle_layout_new_batched(nv, ne, src, dst, nvb, vk, vb, neb, ek, ec, eb, NULL);
     free(vb);
     free(eb);
     return L;
@@ -249,6 +260,7 @@ layout_t* nd_oracle_layout_new(int64_t nv, int64_t ne, const int64_t* src, const
 void nd_oracle_layout_free(layout_t* L) {
     if (!L) return;
     free(L->vkind);
+    free(L->vconst);
     free(L->ekind);
     free(L->ecoup);
     free(L->e_data);
@@ -351,7 +363,8 @@ DEFINE_COMPLEX(float, f32)
         if (ek == E_DIFFUSION_UNIT) return vs - vd;                                                 \
         return pe[0] * SIN(vs - vd);                                                                \
     }                                                                                               \
-    static inline void vertex_f_##SFX(int vk, T* du, const T* u, const T* pv, const T* in) {       \
+    static inline void vertex_f_##SFX(int vk, T* du, const T* u, const T* pv, const T* in,         \
+                                      const double* cst) {                                          \
         T acc = in[0];                                                                              \
         if (vk == V_DIFFUSION) {                                                                    \
             du[0] = acc;                                                                            \
@@ -367,6 +380,8 @@ DEFINE_COMPLEX(float, f32)
             du[1] = du[1] + acc;                                                                    \
         } else if (vk == V_PQ) { /* uc = S / conj(ic) */                                            \
             cdiv_##SFX(pv[0], pv[1], in[0], -in[1], &du[0], &du[1]);                                \
+        } else if (vk == V_PQ_CONST) { /* the same with the P, Q the closure captured */            \
+            cdiv_##SFX((T)cst[0], (T)cst[1], in[0], -in[1], &du[0], &du[1]);                        \
         } else { /* gen! */                                                                         \
             T H = pv[0], P = pv[1], D = pv[2], Om = pv[3], E_f = pv[4], T_d_dash = pv[5];           \
             T T_q_dash = pv[6], X_q_dash = pv[7], X_d_dash = pv[8], X_d = pv[9], X_q = pv[10];      \
@@ -457,7 +472,7 @@ DEFINE_COMPLEX(float, f32)
         for (int64_t k = 0; k < L->nv; ++k) {                     /* vertex f :97 */                \
             int64_t v = L->vbatch_order[k];                                                         \
             vertex_f_##SFX(L->vkind[v], du + L->v_data[v], u + L->v_data[v], p + L->v_para[v],      \
-                           aggbuf + L->v_aggr[v]);                                                  \
+                           aggbuf + L->v_aggr[v], L->vconst + 2 * v);                               \
         }                                                                                           \
     }                                                                                               \
     void nd_oracle_rhs_poly_##SFX(const layout_t* L, T* du, const T* u, const T* p, T* o,           \
@@ -481,7 +496,7 @@ DEFINE_COMPLEX(float, f32)
         _Pragma("omp parallel for schedule(static)") for (i = 0; i < L->nv; ++i) {                 \
             int64_t v = L->vbatch_order[i];                                                         \
             vertex_f_##SFX(L->vkind[v], du + L->v_data[v], u + L->v_data[v], p + L->v_para[v],      \
-                           aggbuf + L->v_aggr[v]);                                                  \
+                           aggbuf + L->v_aggr[v], L->vconst + 2 * v);                               \
         }                                                                                           \
     }
 

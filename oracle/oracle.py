@@ -27,12 +27,12 @@ SRC = HERE / "nd_oracle.c"
 BUILD_DIR = HERE / "_build"
 LIB = BUILD_DIR / "liboracle.so"
 
-V_DIFFUSION, V_KURAMOTO, V_SWING, V_SWING_UNIT, V_PQ, V_GENERATOR = 1, 2, 3, 4, 5, 6
+V_DIFFUSION, V_KURAMOTO, V_SWING, V_SWING_UNIT, V_PQ, V_GENERATOR, V_PQ_CONST = 1, 2, 3, 4, 5, 6, 7
 E_DIFFUSION, E_DIFFUSION_UNIT, E_KURAMOTO, E_DIFFUSION_ODE, E_DIFFUSION_ODE_FIXED, E_PILINE = 1, 2, 3, 4, 5, 6
 C_ANTISYMMETRIC, C_SYMMETRIC, C_DIRECTED, C_FIDUCIAL = 1, 2, 3, 4
 
-VDIM = {V_DIFFUSION: 1, V_KURAMOTO: 1, V_SWING: 2, V_SWING_UNIT: 2, V_PQ: 2, V_GENERATOR: 4}
-VPDIM = {V_DIFFUSION: 0, V_KURAMOTO: 1, V_SWING: 3, V_SWING_UNIT: 1, V_PQ: 2, V_GENERATOR: 11}
+VDIM = {V_DIFFUSION: 1, V_KURAMOTO: 1, V_SWING: 2, V_SWING_UNIT: 2, V_PQ: 2, V_GENERATOR: 4, V_PQ_CONST: 2}
+VPDIM = {V_DIFFUSION: 0, V_KURAMOTO: 1, V_SWING: 3, V_SWING_UNIT: 1, V_PQ: 2, V_GENERATOR: 11, V_PQ_CONST: 0}
 EDIM = {E_DIFFUSION: 0, E_DIFFUSION_UNIT: 0, E_KURAMOTO: 0, E_DIFFUSION_ODE: 2, E_DIFFUSION_ODE_FIXED: 2,
         E_PILINE: 0}
 EPDIM = {E_DIFFUSION: 1, E_DIFFUSION_UNIT: 0, E_KURAMOTO: 1, E_DIFFUSION_ODE: 1, E_DIFFUSION_ODE_FIXED: 0,
@@ -73,7 +73,8 @@ def load():
         lib.nd_oracle_layout_new.restype = vp
         lib.nd_oracle_layout_new.argtypes = [i64, i64, P64, P64, P32, P32]
         lib.nd_oracle_layout_new_batched.restype = vp
-        lib.nd_oracle_layout_new_batched.argtypes = [i64, i64, P64, P64, C.c_int, P32, P32, C.c_int, P32, P32, P32]
+        lib.nd_oracle_layout_new_batched.argtypes = [i64, i64, P64, P64, C.c_int, P32, P32, C.c_int, P32, P32, P32,
+                                                     vp]
         lib.nd_oracle_layout_free.argtypes = [vp]
         for fn in ("nd_oracle_dim", "nd_oracle_pdim"):
             getattr(lib, fn).restype = i64
@@ -145,7 +146,7 @@ class OracleNetwork:
         return cls(g.nv, g.src, g.dst, vkind, ekind)
 
     @classmethod
-    def from_batches(cls, nv, src, dst, vertex_batches, vertex_batch, edge_batches, edge_batch):
+    def from_batches(cls, nv, src, dst, vertex_batches, vertex_batch, edge_batches, edge_batch, vertex_constants=None):
         """Network with explicit batches (the reference's order of first appearance):
         ``vertex_batches`` lists the vertex kind of every batch, ``edge_batches`` the
         (edge kind, coupling) of every batch; ``vertex_batch`` / ``edge_batch`` give each
@@ -163,12 +164,14 @@ class OracleNetwork:
         eb = np.ascontiguousarray(edge_batch if self.ne else np.zeros(1), dtype=np.int32)
         self.vkind = vbk[vb]
         self.ekind = ebk[eb[:self.ne]] if self.ne else np.zeros(0, dtype=np.int32)
+        self._vconst = (None if vertex_constants is None
+                        else np.ascontiguousarray(vertex_constants, dtype=np.float64).reshape(-1))
         P64 = C.POINTER(C.c_int64)
         P32 = C.POINTER(C.c_int32)
         self.L = self.lib.nd_oracle_layout_new_batched(
             self.nv, self.ne, self.src.ctypes.data_as(P64), self.dst.ctypes.data_as(P64), len(vbk),
             vbk.ctypes.data_as(P32), vb.ctypes.data_as(P32), len(edge_batches), ebk.ctypes.data_as(P32),
-            ebc.ctypes.data_as(P32), eb.ctypes.data_as(P32))
+            ebc.ctypes.data_as(P32), eb.ctypes.data_as(P32), _ptr(self._vconst))
         self._finish()
         return self
 
@@ -302,7 +305,7 @@ def layout_batched(nv, src, dst, vertex_batches, vertex_batch, edge_batches, edg
 
 
 def rhs_numpy_batched(nv, src, dst, vertex_batches, vertex_batch, edge_batches, edge_batch, u, p,
-                      dtype=np.float64):
+                      dtype=np.float64, vertex_constants=None):
     """Independent numpy restatement of the sequential RHS of a batched network (several
     vertex / edge batches, ODE edges, Symmetric / Directed / Fiducial outputs)."""
     src = np.asarray(src, dtype=np.int64)
@@ -312,9 +315,9 @@ def rhs_numpy_batched(nv, src, dst, vertex_batches, vertex_batch, edge_batches, 
     p = np.asarray(p if p is not None else np.zeros(0), dtype=dtype)
     sin = (lambda x: np.sin(x)) if dtype == np.float64 else (lambda x: np.sin(x).astype(dtype))
     du = np.zeros(L["dim"], dtype=dtype)
-    if any(k in (V_PQ, V_GENERATOR) for k in vertex_batches):
+    if any(k in (V_PQ, V_GENERATOR, V_PQ_CONST) for k in vertex_batches):
         return _rhs_numpy_powergrid(nv, src, dst, vertex_batches, vertex_batch, edge_batches, edge_batch, u, p, L,
-                                    du)
+                                    du, vertex_constants)
     ov = u[L["v_data"]]                                # vertex g: StateMask(1)
     eo = L["eorder"]
     eb = np.asarray(edge_batch, dtype=np.int64)
@@ -361,7 +364,8 @@ def rhs_numpy_batched(nv, src, dst, vertex_batches, vertex_batch, edge_batches, 
     return du
 
 
-def _rhs_numpy_powergrid(nv, src, dst, vertex_batches, vertex_batch, edge_batches, edge_batch, u, p, L, du):
+def _rhs_numpy_powergrid(nv, src, dst, vertex_batches, vertex_batch, edge_batches, edge_batch, u, p, L, du,
+                         vertex_constants=None):
     """The power-grid components (benchmark/benchmark_models.jl:46-109) in numpy complex
     arithmetic: vertex outputs and edge outputs are complex numbers (depth 2)."""
     v_data, v_para, e_para = L["v_data"], L["v_para"], L["e_para"]
@@ -393,8 +397,9 @@ def _rhs_numpy_powergrid(nv, src, dst, vertex_batches, vertex_batch, edge_batche
     for b, k in enumerate(vertex_batches):
         vs = np.flatnonzero(vbatch == b)
         s, q, i = v_data[vs], v_para[vs], isum[vs]
-        if k == V_PQ:
-            uc = (p[q] + 1j * p[q + 1]) / np.conj(i)
+        if k in (V_PQ, V_PQ_CONST):
+            S = (p[q] + 1j * p[q + 1]) if k == V_PQ else complex(*np.asarray(vertex_constants).reshape(-1, 2)[b])
+            uc = S / np.conj(i)
             du[s], du[s + 1] = uc.real, uc.imag
             continue
         assert k == V_GENERATOR

@@ -310,3 +310,25 @@ def test_powergrid_has_no_jacobian(cuda):
     u = torch.zeros(nw.dim, dtype=torch.float64, device=cuda)
     with pytest.raises(nd.ArgumentError):
         nd.jvp(nw, torch.empty_like(u), u, torch.ones(nw.pdim, dtype=torch.float64, device=cuda), u)
+
+
+def test_inhomogeneous_pq_parity(cuda):
+    """powergrid_inhomogeneous_pq (benchmark/benchmark_cases.jl:82-102): half the buses are
+    PQ buses closing over their own P, Q (one batch each, ~1500 batches), half generators."""
+    nv = 3000
+    g = nd.watts_strogatz(nv, 4, 0.5, seed=6)
+    rng = np.random.default_rng(6)
+    gen = rng.permutation(np.repeat([False, True], nv // 2))
+    vm = [nd.generator() if x else nd.pqnode_inhomogeneous(-rng.random(), -rng.random()) for x in gen]
+    net = nd.Network(g, vm, nd.piline())
+    assert len(net.vertex_batches) == nv // 2 + 1
+    vb = [m.kind for m in net.vertex_batches]
+    consts = [m.constants or (0.0, 0.0) for m in net.vertex_batches]
+    on = O.OracleNetwork.from_batches(g.nv, g.src, g.dst, vb, net.vertex_batch, [(O.E_PILINE, O.C_FIDUCIAL)],
+                                      net.edge_batch, vertex_constants=consts)
+    assert (on.dim, on.pdim) == (net.dim, net.pdim)
+    u, p = rng.normal(size=net.dim), rng.uniform(0.5, 1.5, size=net.pdim)
+    ref = on.rhs(u, p)
+    got = gpu_rhs(adapt(net, np.float64), u, p, cuda, np.float64)
+    assert np.max(np.abs(got - ref) / (1 + np.abs(ref))) < 1e-12
+    check_f32_isapprox(gpu_rhs(adapt(net, np.float32), u, p, cuda, np.float32).astype(np.float64), ref)

@@ -106,10 +106,10 @@ def test_ba_is_power_law_with_hubs():
     assert deg.max() > 300  # hubs well beyond the thread-per-vertex bucket
 
 
-def test_batch_limit_and_power_grid_layout():
-    """More distinct components than the batch table holds are rejected; a power-grid
-    network lays PQ buses (2 states) and generators (4 states) out batch by batch, with the
-    π-line parameters after every vertex parameter."""
+def test_power_grid_layout_and_closure_batches():
+    """A power-grid network lays PQ buses (2 states) and generators (4 states) out batch by
+    batch, with the π-line parameters after every vertex parameter; components closing over
+    distinct values form one batch each."""
     g = nd.cycle_graph(6)
     vf = [nd.pqnode(), nd.generator(), nd.pqnode(), nd.generator(), nd.generator(), nd.pqnode()]
     nw = nd.Network(g, vf, nd.piline())
@@ -122,7 +122,9 @@ def test_batch_limit_and_power_grid_layout():
     many = [nd.EdgeModel(f"e{i}", pdim=0, kind=nd.capi.ND_E_DIFFUSION_UNIT, coupling=c)
             for i, c in enumerate(["AntiSymmetric", "Symmetric", "Directed"])]
     assert len(nd.Network(g, nd.diffusion_vertex(), [many[i % 3] for i in range(6)]).edge_batches) == 3
+    # one batch per distinct closure value (pqnode_inhomogeneous), equal values share one
     big = nd.cycle_graph(40)
-    kinds = [nd.EdgeModel(f"e{i}", pdim=0, kind=i + 100, coupling="AntiSymmetric") for i in range(40)]
-    with pytest.raises(nd.UnsupportedComponentError):
-        nd.Network(big, nd.diffusion_vertex(), kinds)
+    buses = [nd.pqnode_inhomogeneous(-0.01 * (i % 30), -0.02) for i in range(40)]
+    pg = nd.Network(big, buses, nd.piline())
+    assert len(pg.vertex_batches) == 30 and pg.vertex_batch.tolist() == [i % 30 for i in range(40)]
+    assert pg.pdim == 40 * 4 and pg.vertex_state_index(30) == 2

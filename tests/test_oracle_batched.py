@@ -226,3 +226,30 @@ def test_mixed_output_dimensions_rejected():
                                      [(O.E_PILINE, O.C_FIDUCIAL)], [0] * 4)
     with pytest.raises(nd.ArgumentError):
         nd.Network(g, [nd.pqnode(), nd.diffusion_vertex(), nd.pqnode(), nd.diffusion_vertex()], nd.piline())
+
+
+def test_inhomogeneous_pq_batches():
+    """powergrid_inhomogeneous_pq (benchmark/benchmark_cases.jl:82-102): every PQ bus closes
+    over its own P, Q and is a batch of its own; the constants ride with the batches."""
+    g = nd.watts_strogatz(60, 4, 0.5, seed=4)
+    rng = np.random.default_rng(4)
+    gen_at = rng.permutation(g.nv)[:30]
+    vb, vbi, consts = [], np.empty(g.nv, dtype=np.int32), []
+    gen_batch = None
+    for v in range(g.nv):                               # batches in order of first appearance
+        if v in gen_at:
+            if gen_batch is None:
+                gen_batch = len(vb)
+                vb.append(O.V_GENERATOR)
+                consts.append((0.0, 0.0))
+            vbi[v] = gen_batch
+        else:
+            vbi[v] = len(vb)
+            vb.append(O.V_PQ_CONST)
+            consts.append((-rng.random(), -rng.random()))
+    eb, ebi = [(O.E_PILINE, O.C_FIDUCIAL)], np.zeros(g.ne, dtype=np.int32)
+    on = O.OracleNetwork.from_batches(g.nv, g.src, g.dst, vb, vbi, eb, ebi, vertex_constants=consts)
+    assert len(vb) == 31 and on.pdim == 30 * 11 + g.ne * 4
+    u, p = rng.normal(size=on.dim), rng.uniform(0.5, 1.5, size=on.pdim)
+    ref = O.rhs_numpy_batched(g.nv, g.src, g.dst, vb, vbi, eb, ebi, u, p, vertex_constants=consts)
+    assert np.max(np.abs(on.rhs(u, p) - ref) / (1 + np.abs(ref))) < 1e-12
