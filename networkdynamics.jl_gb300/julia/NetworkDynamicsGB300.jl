@@ -65,6 +65,7 @@ struct nd_batched_network_desc
     edge_batch::Ptr{Int32}
     flags::Int32
     reserved::Int32
+    vertex_constants::Ptr{Cdouble}  # values a component closes over (C_NULL: none)
 end
 
 """
@@ -167,7 +168,8 @@ function Adapt.adapt_structure(::Type{<:CuArray{T}}, a::GB300Aggregator) where {
     GC.@preserve a begin
         desc = nd_batched_network_desc(a.nv, length(a.src), pointer(a.src), pointer(a.dst),
                                        length(a.vertex_batches), length(a.edge_batches), pointer(a.vertex_batches),
-                                       pointer(a.edge_batches), pointer(a.vertex_batch), pointer(a.edge_batch), 0, 0)
+                                       pointer(a.edge_batches), pointer(a.vertex_batch), pointer(a.edge_batch), 0, 0,
+                                       C_NULL)
         check(ccall((:nd_create_batched, libnd), Cint, (Ref{nd_batched_network_desc}, Cint, Ref{Ptr{Cvoid}}),
                     desc, dtype, h))
     end
