@@ -452,7 +452,8 @@ void free_batched(BatchedNet* b) {
     *b = BatchedNet{};
 }
 
-int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out) {
+// Every check on a description, on the host: no device resource is touched before it passes.
+int validate_batched(const nd_batched_network_desc* d) {
     const int64_t nv = d->nv, ne = d->ne;
     const int nvb = d->n_vertex_batches, neb = d->n_edge_batches;
     if (nv <= 0) return fail(ND_ERR_ARG, "network has no vertices");
@@ -488,11 +489,9 @@ int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out) {
     for (int b = 0; b < neb; ++b)
         if (edge_outdim(d->edge_batches[b].kind) != depth)
             return fail(ND_ERR_ARG, "All edge models must have the same output dimension as the vertex models!");
-    std::vector<int64_t> vcount(nvb, 0), ecount(std::max(neb, 1), 0);
     for (int64_t v = 0; v < nv; ++v) {
         const int32_t b = d->vertex_batch[v];
         if (b < 0 || b >= nvb) return fail(ND_ERR_ARG, "vertex " + std::to_string(v) + " has no valid batch");
-        vcount[b]++;
     }
     for (int64_t e = 0; e < ne; ++e) {
         const int32_t b = d->edge_batch[e];
@@ -500,8 +499,19 @@ int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out) {
         const int64_t s = d->src[e], t = d->dst[e];
         if (s < 0 || s >= nv || t < 0 || t >= nv)
             return fail(ND_ERR_ARG, "edge " + std::to_string(e) + " has endpoint out of range");
-        ecount[b]++;
     }
+    return ND_OK;
+}
+
+int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out) {
+    const int rc0 = validate_batched(d);
+    if (rc0 != ND_OK) return rc0;
+    const int64_t nv = d->nv, ne = d->ne;
+    const int nvb = d->n_vertex_batches, neb = d->n_edge_batches;
+    const int depth = vertex_outdim(d->vertex_batches[0].kind);
+    std::vector<int64_t> vcount(nvb, 0), ecount(std::max(neb, 1), 0);
+    for (int64_t v = 0; v < nv; ++v) vcount[d->vertex_batch[v]]++;
+    for (int64_t e = 0; e < ne; ++e) ecount[d->edge_batch[e]]++;
     // Batch tables: vertex batches first (register_vertices!), then edge batches whose
     // states follow every vertex state and whose parameters follow every vertex parameter
     // (register_edges!, src/network_structure.jl:224-258).

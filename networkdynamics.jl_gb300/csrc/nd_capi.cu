@@ -331,8 +331,10 @@ static bool homogeneous_kinds(int vk, int ek, int coupling) {
 }
 
 static int create_batched(const nd_batched_network_desc* d, int dtype, nd_handle** out) {
+    int rc = validate_batched(d);  // before any device resource
+    if (rc != ND_OK) return rc;
     nd_handle* h = nullptr;
-    int rc = new_handle(dtype, &h);
+    rc = new_handle(dtype, &h);
     if (rc != ND_OK) return rc;
     rc = build_batched(d, dtype == ND_F64 ? 8 : 4, &h->batched);
     if (rc != ND_OK) {

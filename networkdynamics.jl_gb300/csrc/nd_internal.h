@@ -242,7 +242,8 @@ inline int host_find_batch(const BatchTable& t, int64_t pos) {
 
 int check_edge_component(int edge_kind, int coupling);  // ND_OK or ND_ERR_UNSUPPORTED_COMPONENT
 // elem: scratch element size (4 / 8); 0 builds the structure without the y2 scratch (a
-// view of a network for the Jacobian).
+// view of a network for the Jacobian).  validate_batched runs every check on the host.
+int validate_batched(const nd_batched_network_desc* d);
 int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out);
 void free_batched(BatchedNet* b);
 cudaError_t launch_batched(int dtype, const BatchedNet& b, void* du, const void* u, const void* p, int mode,
