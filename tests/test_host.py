@@ -128,3 +128,28 @@ def test_power_grid_layout_and_closure_batches():
     pg = nd.Network(big, buses, nd.piline())
     assert len(pg.vertex_batches) == 30 and pg.vertex_batch.tolist() == [i % 30 for i in range(40)]
     assert pg.pdim == 40 * 4 and pg.vertex_state_index(30) == 2
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_python_layout_matches_oracle_layout(seed):
+    """The host-side layout of a batched network (Network.v_data / v_para / e_data / e_para)
+    equals the oracle's restatement of register_vertices! / register_edges!
+    (src/network_structure.jl:224-258) on random mixes of every kind and wrapper."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed)
+    g = nd.barabasi_albert(120, 3, seed=seed)
+    vms = [nd.diffusion_vertex, nd.kuramoto_first, nd.kuramoto_second, nd.kuramoto_vertex_2d]
+    ems = [nd.diffusion_edge, nd.diffusion_edge_unit, nd.kuramoto_edge, nd.diffusion_odeedge, nd.diffusion_dedge,
+           nd.diffusion_edge_fid, lambda: nd.Symmetric(nd.kuramoto_edge()), lambda: nd.Directed(nd.diffusion_edge())]
+    net = nd.Network(g, [vms[i]() for i in rng.integers(0, len(vms), g.nv)],
+                     [ems[i]() for i in rng.integers(0, len(ems), g.ne)])
+    on = O.OracleNetwork.from_batches(g.nv, g.src, g.dst, [m.kind for m in net.vertex_batches], net.vertex_batch,
+                                      [(m.kind, nd.capi.COUPLINGS[m.coupling]) for m in net.edge_batches],
+                                      net.edge_batch)
+    assert (on.dim, on.pdim) == (net.dim, net.pdim)
+    lib = on.lib
+    assert [lib.nd_oracle_v_data(on.L, v) for v in range(g.nv)] == net.v_data.tolist()
+    assert [lib.nd_oracle_v_para(on.L, v) for v in range(g.nv)] == net.v_para.tolist()
+    assert [lib.nd_oracle_e_para(on.L, e) for e in range(g.ne)] == net.e_para.tolist()
+    ode = [e for e in range(g.ne) if net.edge_batches[net.edge_batch[e]].dim == 2]
+    assert [lib.nd_oracle_e_data(on.L, e) for e in ode] == net.e_data[ode].tolist()
