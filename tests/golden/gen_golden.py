@@ -11,6 +11,10 @@ outputs.  The known answers they are checked against come from the reference's o
 * ``swing_ws4.npz``          the 4-node swing fixpoint of test/initialization_test.jl:15-38
                              (P = [1,-1,1,-1], K = 6 on watts_strogatz(4, 2, 0) = C4).
 * ``swing_ba200.npz``        swing + static line on BA(200, 2): one RHS in F64 and F32.
+* ``batched_gpu_test.npz``   the network of test/GPU_test.jl:12-21 (complete graph on 4
+                             vertices; swing and diffusion vertices; ODE, Kuramoto and
+                             two-sided fiducial edges) with its batches, x0, p ~ U(0, 1): one RHS.
+* ``powergrid_ws300.npz``    PQ buses and generators with π-lines on WS(300, 4, 0.5): one RHS.
 
 Run: python tests/golden/gen_golden.py
 """
@@ -63,7 +67,33 @@ def main():
     p = np.concatenate([pv, rng.uniform(5, 10, size=g.ne)])
     np.savez(HERE / "swing_ba200.npz", nv=g.nv, src=g.src, dst=g.dst, u=u, p=p, du=on.rhs(u, p),
              du32=on.rhs(u, p, dtype=np.float32))
+    batched_fixtures()
     print("golden fixtures written to", HERE)
+
+
+def batched_fixtures():
+    rng = np.random.default_rng(7)
+    g = nd.complete_graph(4)
+    vb, vbi = [O.V_SWING, O.V_DIFFUSION], np.array([0, 1, 0, 1], dtype=np.int32)
+    eb = np.array([(O.E_DIFFUSION_ODE, O.C_FIDUCIAL), (O.E_KURAMOTO, O.C_ANTISYMMETRIC),
+                   (O.E_DIFFUSION, O.C_FIDUCIAL)], dtype=np.int32)
+    ebi = np.array([0, 1, 1, 2, 0, 2], dtype=np.int32)
+    on = O.OracleNetwork.from_batches(g.nv, g.src, g.dst, vb, vbi, [tuple(x) for x in eb], ebi)
+    x0, p = rng.random(on.dim), rng.random(on.pdim)
+    np.savez(HERE / "batched_gpu_test.npz", nv=g.nv, src=g.src, dst=g.dst, vb=np.array(vb), vbi=vbi, eb=eb,
+             ebi=ebi, u=x0, p=p, du=on.rhs(x0, p))
+
+    g = nd.watts_strogatz(300, 4, 0.5, seed=3)
+    kinds = rng.integers(0, 2, g.nv)
+    order = list(dict.fromkeys(kinds.tolist()))
+    vb = np.array([[O.V_PQ, O.V_GENERATOR][k] for k in order], dtype=np.int32)
+    vbi = np.array([order.index(k) for k in kinds], dtype=np.int32)
+    eb = np.array([(O.E_PILINE, O.C_FIDUCIAL)], dtype=np.int32)
+    ebi = np.zeros(g.ne, dtype=np.int32)
+    on = O.OracleNetwork.from_batches(g.nv, g.src, g.dst, vb, vbi, [tuple(x) for x in eb], ebi)
+    u, p = 1.0 + 0.1 * rng.normal(size=on.dim), rng.uniform(0.5, 1.5, size=on.pdim)
+    np.savez(HERE / "powergrid_ws300.npz", nv=g.nv, src=g.src, dst=g.dst, vb=vb, vbi=vbi, eb=eb, ebi=ebi, u=u,
+             p=p, du=on.rhs(u, p))
 
 
 if __name__ == "__main__":

@@ -6,6 +6,8 @@ The network of the reference's GPU test (test/GPU_test.jl:12-21) is the first ca
 complete graph on 4 vertices with swing and diffusion vertices and ODE, Kuramoto and
 two-sided Fiducial edges.
 """
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -253,3 +255,12 @@ def test_inhomogeneous_pq_batches():
     u, p = rng.normal(size=on.dim), rng.uniform(0.5, 1.5, size=on.pdim)
     ref = O.rhs_numpy_batched(g.nv, g.src, g.dst, vb, vbi, eb, ebi, u, p, vertex_constants=consts)
     assert np.max(np.abs(on.rhs(u, p) - ref) / (1 + np.abs(ref))) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["batched_gpu_test", "powergrid_ws300"])
+def test_batched_golden_fixtures_reproduce(name):
+    """The oracle reproduces its committed fixtures bit for bit (tests/golden/gen_golden.py)."""
+    d = np.load(Path(__file__).resolve().parent / "golden" / f"{name}.npz")
+    on = O.OracleNetwork.from_batches(int(d["nv"]), d["src"], d["dst"], d["vb"].tolist(), d["vbi"],
+                                      [tuple(x) for x in d["eb"].tolist()], d["ebi"])
+    np.testing.assert_array_equal(on.rhs(d["u"], d["p"]), d["du"])
