@@ -38,7 +38,9 @@ void free_topology(Topology* t) {
     EdgeLayout& el = t->edge;
     cudaFree(el.esrc);
     cudaFree(el.edst);
-    cudaFree(el.q);
+    cudaFree(el.lslot);
+    cudaFree(el.run_start);
+    cudaFree(el.run_base);
     cudaFree(el.dptr);
     cudaFree(el.loc);
     cudaFree(el.sptr);
@@ -58,7 +60,8 @@ static bool is_canonical(int64_t ne, const int64_t* src, const int64_t* dst) {
 
 // Host side of the edge-centric layout (see EdgeLayout in nd_internal.h).
 struct EdgeLayoutHost {
-    std::vector<int32_t> esrc, edst, q, loc;
+    std::vector<int32_t> esrc, edst, loc, run_base;
+    std::vector<uint16_t> lslot, run_start;
     std::vector<uint32_t> dptr, sptr;
     int64_t n_chunks = 0;
 };
@@ -87,20 +90,34 @@ static void build_edge_layout(int64_t nv, int64_t ne, const int64_t* src, const 
     // buckets of destination-CSR positions; ybkt is bucket-major, chunk-major inside a
     // bucket, edge order inside a (bucket, chunk) run
     const int64_t bsize = std::max<int64_t>(1, (ne + kBuckets - 1) / kBuckets);
-    h.n_chunks = (ne + kEdgeChunk - 1) / kEdgeChunk;
-    std::vector<int64_t> cnt((size_t)kBuckets * std::max<int64_t>(h.n_chunks, 1), 0);
-    for (int64_t e = 0; e < ne; ++e) cnt[(tpos[e] / bsize) * h.n_chunks + e / kEdgeChunk]++;
+    const int64_t nch = (ne + kEdgeChunk - 1) / kEdgeChunk;
+    h.n_chunks = nch;
+    std::vector<int64_t> cnt((size_t)kBuckets * std::max<int64_t>(nch, 1), 0);  // [bucket][chunk]
+    for (int64_t e = 0; e < ne; ++e) cnt[(tpos[e] / bsize) * nch + e / kEdgeChunk]++;
+    // staging order inside a chunk: bucket-major, edge order inside a bucket
+    h.run_start.assign((size_t)nch * (kBuckets + 1), 0);
+    for (int64_t c = 0; c < nch; ++c)
+        for (int b = 0; b < kBuckets; ++b)
+            h.run_start[c * (kBuckets + 1) + b + 1] =
+                (uint16_t)(h.run_start[c * (kBuckets + 1) + b] + cnt[(size_t)b * nch + c]);
+    std::vector<int64_t> next_slot((size_t)kBuckets * std::max<int64_t>(nch, 1));  // [bucket][chunk]
+    for (int64_t c = 0; c < nch; ++c)
+        for (int b = 0; b < kBuckets; ++b) next_slot[(size_t)b * nch + c] = h.run_start[c * (kBuckets + 1) + b];
     int64_t run = 0;
     for (size_t i = 0; i < cnt.size(); ++i) {
         const int64_t c = cnt[i];
         cnt[i] = run;
         run += c;
     }
-    h.q.resize(ne);
+    h.run_base.resize((size_t)nch * kBuckets);
+    for (int64_t c = 0; c < nch; ++c)
+        for (int b = 0; b < kBuckets; ++b) h.run_base[c * kBuckets + b] = (int32_t)cnt[(size_t)b * nch + c];
+    h.lslot.resize(ne);
     h.loc.resize(ne);
     for (int64_t e = 0; e < ne; ++e) {
-        const int64_t qe = cnt[(tpos[e] / bsize) * h.n_chunks + e / kEdgeChunk]++;
-        h.q[e] = (int32_t)qe;
+        const size_t key = (size_t)(tpos[e] / bsize) * nch + e / kEdgeChunk;
+        const int64_t qe = cnt[key]++;
+        h.lslot[e] = (uint16_t)next_slot[key]++;
         h.loc[tpos[e]] = (int32_t)qe;
     }
 }
@@ -234,7 +251,11 @@ int build_topology(int64_t nv, int64_t ne, const int64_t* src, const int64_t* ds
         el.n_chunks = h.n_chunks;
         if ((err = upload((void**)&el.esrc, h.esrc.data(), h.esrc.size() * sizeof(int32_t))) != cudaSuccess ||
             (err = upload((void**)&el.edst, h.edst.data(), h.edst.size() * sizeof(int32_t))) != cudaSuccess ||
-            (err = upload((void**)&el.q, h.q.data(), h.q.size() * sizeof(int32_t))) != cudaSuccess ||
+            (err = upload((void**)&el.lslot, h.lslot.data(), h.lslot.size() * sizeof(uint16_t))) != cudaSuccess ||
+            (err = upload((void**)&el.run_start, h.run_start.data(), h.run_start.size() * sizeof(uint16_t))) !=
+                cudaSuccess ||
+            (err = upload((void**)&el.run_base, h.run_base.data(), h.run_base.size() * sizeof(int32_t))) !=
+                cudaSuccess ||
             (err = upload((void**)&el.dptr, h.dptr.data(), h.dptr.size() * sizeof(uint32_t))) != cudaSuccess ||
             (err = upload((void**)&el.loc, h.loc.data(), h.loc.size() * sizeof(int32_t))) != cudaSuccess ||
             (err = upload((void**)&el.sptr, h.sptr.data(), h.sptr.size() * sizeof(uint32_t))) != cudaSuccess ||
@@ -537,7 +558,9 @@ int nd_rhs(nd_handle* h, int dtype, void* du, int64_t n_du, const void* u, int64
     a.n_chunks = el.n_chunks;
     a.esrc = el.esrc;
     a.edst = el.edst;
-    a.q = el.q;
+    a.lslot = el.lslot;
+    a.run_start = el.run_start;
+    a.run_base = el.run_base;
     a.dptr = el.dptr;
     a.loc = el.loc;
     a.sptr = el.sptr;

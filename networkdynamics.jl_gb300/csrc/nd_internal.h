@@ -78,7 +78,8 @@ constexpr int kWindowIncidences = 2048;  // light window: at most this many inci
 // a contiguous edge range], so the RHS can run in two phases:
 //   E: each edge's value y_e = g(u_src, u_dst, p_e) once, in edge order, written to y
 //      (edge order) and to ybkt, the same values grouped into kBuckets buckets of
-//      destination-CSR positions (each block writes contiguous runs per bucket);
+//      destination-CSR positions: a block stages its chunk's values in shared memory in
+//      (bucket, edge) order and writes each bucket's run of them as one contiguous piece;
 //   R: each row sums its dst-side values (gathered from one bucket, which stays in L2
 //      while the rows of that range run) and then -y over its source block.
 // Each edge's function is evaluated once instead of twice, and the edge parameters and
@@ -91,7 +92,9 @@ struct EdgeLayout {
     int64_t n_chunks = 0;
     int32_t* esrc = nullptr;   // [ne]
     int32_t* edst = nullptr;   // [ne]
-    int32_t* q = nullptr;      // [ne] position of edge e's value in ybkt
+    uint16_t* lslot = nullptr;     // [ne] slot of edge e in its chunk's (bucket, edge)-ordered staging
+    uint16_t* run_start = nullptr;  // [n_chunks][kBuckets+1] first staging slot of each bucket's run
+    int32_t* run_base = nullptr;    // [n_chunks][kBuckets] ybkt position of each bucket's run
     uint32_t* dptr = nullptr;  // [nv+1] each vertex's range in destination-CSR order
     int32_t* loc = nullptr;    // [ne] ybkt position of destination-CSR entry k
     uint32_t* sptr = nullptr;  // [nv+1] each vertex's source block (edge ids)
@@ -142,7 +145,9 @@ struct RhsArgs {
     int64_t ne, n_chunks;
     const int32_t* esrc;
     const int32_t* edst;
-    const int32_t* q;
+    const uint16_t* lslot;
+    const uint16_t* run_start;
+    const int32_t* run_base;
     const uint32_t* dptr;
     const int32_t* loc;
     const uint32_t* sptr;

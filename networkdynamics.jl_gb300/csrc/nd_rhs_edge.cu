@@ -40,18 +40,27 @@ struct Pair<float> {
 };
 
 // A thread evaluates two consecutive edges per step, so the in-order streams (src, dst,
-// bucket slot, parameter, y) move as 8- or 16-byte vectors.
+// staging slot, parameter, y) move as 4-, 8- or 16-byte vectors.  The values bound for
+// ybkt go to shared memory first, in (bucket, edge) order, and leave the block as one
+// contiguous run per bucket: written one by one, the scattered 8-byte stores reached L2
+// as separate partial-sector requests and took more than half of the phase's time.
 template <typename T, int VK, int EK>
 __global__ void __launch_bounds__(kBlock) edge_phase_kernel(RhsArgs a) {
     using P2 = typename Pair<T>::type;
     constexpr int DV = VertexDims<VK>::dim;
+    __shared__ T stage[kEdgeChunk];
+    __shared__ uint16_t rstart[kBuckets + 1];
+    __shared__ int32_t rbase[kBuckets];
     const T* __restrict__ u = static_cast<const T*>(a.u);
     const T* __restrict__ pe = static_cast<const T*>(a.p) + a.nv * VertexDims<VK>::pdim;
     T* __restrict__ y = static_cast<T*>(a.y);
     T* __restrict__ ybkt = static_cast<T*>(a.ybkt);
     const uint64_t keep = policy_evict_last(), stream = policy_evict_first();
-    const int64_t e0 = (int64_t)blockIdx.x * kEdgeChunk;  // even: kEdgeChunk is
+    const int64_t chunk = blockIdx.x;
+    const int64_t e0 = chunk * kEdgeChunk;  // even: kEdgeChunk is
     const int64_t e1 = min(e0 + (int64_t)kEdgeChunk, a.ne);
+    if (threadIdx.x <= kBuckets) rstart[threadIdx.x] = __ldg(a.run_start + chunk * (kBuckets + 1) + threadIdx.x);
+    if (threadIdx.x < kBuckets) rbase[threadIdx.x] = __ldg(a.run_base + chunk * kBuckets + threadIdx.x);
     // the parameter block starts after nv * pdim vertex parameters: pairs of it are
     // vector-aligned only when that offset is even
     const bool wvec = EK == ND_E_DIFFUSION_UNIT || (reinterpret_cast<uintptr_t>(pe) % sizeof(P2)) == 0;
@@ -61,7 +70,7 @@ __global__ void __launch_bounds__(kBlock) edge_phase_kernel(RhsArgs a) {
         const int64_t e = e0 + 2 * k;
         const int2 s = ld_hint(reinterpret_cast<const int2*>(a.esrc + e), stream);
         const int2 d = ld_hint(reinterpret_cast<const int2*>(a.edst + e), stream);
-        const int2 q = ld_hint(reinterpret_cast<const int2*>(a.q + e), stream);
+        const uint32_t ls = ld_hint(reinterpret_cast<const uint32_t*>(a.lslot + e), stream);
         T w0, w1;
         if constexpr (EK == ND_E_DIFFUSION_UNIT) {
             w0 = w1 = T(0);
@@ -83,8 +92,8 @@ __global__ void __launch_bounds__(kBlock) edge_phase_kernel(RhsArgs a) {
         // the outputs stream through L2 ahead of the row phase: evict them first so the
         // gathered u stays resident
         st_hint(reinterpret_cast<P2*>(y + e), yv, stream);
-        st_hint(ybkt + q.x, yv.x, stream);
-        st_hint(ybkt + q.y, yv.y, stream);
+        stage[ls & 0xffffu] = yv.x;
+        stage[ls >> 16] = yv.y;
     }
     if (((e1 - e0) & 1) && threadIdx.x == 0) {  // odd tail of the last chunk
         const int64_t e = e1 - 1;
@@ -93,7 +102,15 @@ __global__ void __launch_bounds__(kBlock) edge_phase_kernel(RhsArgs a) {
         const T w = edge_param<T, EK>(pe, (int32_t)e, stream);
         const T yv = edge_g_w<T, EK>(ld_hint(u + (int64_t)s * DV, keep), ld_hint(u + (int64_t)d * DV, keep), w);
         y[e] = yv;
-        ybkt[ld_hint(a.q + e, stream)] = yv;
+        stage[a.lslot[e]] = yv;
+    }
+    __syncthreads();
+    // one bucket run per warp step, its lanes writing consecutive ybkt positions
+    const int lane = threadIdx.x & 31;
+    for (int b = threadIdx.x >> 5; b < kBuckets; b += kWarpsPerBlock) {
+        const int s0 = rstart[b], n = rstart[b + 1] - s0;
+        T* __restrict__ dst = ybkt + rbase[b];
+        for (int j = lane; j < n; j += 32) st_hint(dst + j, stage[s0 + j], stream);
     }
 }
 
