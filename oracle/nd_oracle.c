@@ -568,8 +568,13 @@ static double rms_scaled(int64_t n, const double* e, const double* u0, const dou
     return sqrt(s / (double)(n > 0 ? n : 1));
 }
 
-int nd_oracle_tsit5(const layout_t* L, double* u, const double* p, double t0, double t1, double reltol,
-                    double abstol, int64_t maxsteps, tsit5_stats_t* st) {
+/* threaded != 0: the RHS is the PolyesterExecution restatement and the stage updates run on
+ * all threads.  Both give the same bits as the sequential code (the RHS per vertex sums in
+ * the same order; the stage updates are elementwise); the error norm stays sequential. */
+static int tsit5_impl(const layout_t* L, double* u, const double* p, double t0, double t1, double reltol,
+                      double abstol, int64_t maxsteps, tsit5_stats_t* st, int threaded) {
+#define TS_RHS(out, in) \
+    (threaded ? nd_oracle_rhs_poly_f64(L, out, in, p, o, ab) : nd_oracle_rhs_f64(L, out, in, p, o, ab))
     int64_t n = L->lastidx_dynamic;
     double* k[7];
     for (int i = 0; i < 7; ++i) k[i] = (double*)malloc(sizeof(double) * (size_t)(n + 1));
@@ -580,7 +585,7 @@ int nd_oracle_tsit5(const layout_t* L, double* u, const double* p, double t0, do
     double* ab = (double*)malloc(sizeof(double) * (size_t)(L->lastidx_aggr + 1));
     memset(st, 0, sizeof(*st));
     double t = t0, tdir = t1 >= t0 ? 1.0 : -1.0;
-    nd_oracle_rhs_f64(L, k[0], u, p, o, ab);
+    TS_RHS(k[0], u);
     st->nf++;
     /* Hairer–Wanner initial step (order 5). */
     double d0 = 0, d1 = 0;
@@ -594,7 +599,7 @@ int nd_oracle_tsit5(const layout_t* L, double* u, const double* p, double t0, do
     double h0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
     h0 = fmin(h0, fabs(t1 - t0));
     for (int64_t i = 0; i < n; ++i) y[i] = u[i] + tdir * h0 * k[0][i];
-    nd_oracle_rhs_f64(L, k[1], y, p, o, ab);
+    TS_RHS(k[1], y);
     st->nf++;
     double d2 = 0;
     for (int64_t i = 0; i < n; ++i) {
@@ -617,16 +622,18 @@ int nd_oracle_tsit5(const layout_t* L, double* u, const double* p, double t0, do
         if (fabs(t1 - t) < dt * (1 + 1e-12)) dt = fabs(t1 - t);
         double h = tdir * dt;
         for (int s = 1; s < 7; ++s) {
-            for (int64_t i = 0; i < n; ++i) {
+            int64_t i;
+            _Pragma("omp parallel for schedule(static) if (threaded)") for (i = 0; i < n; ++i) {
                 double acc = 0;
                 for (int j = 0; j < s; ++j) acc += TS_A[s][j] * k[j][i];
                 y[i] = u[i] + h * acc;
             }
-            nd_oracle_rhs_f64(L, k[s], y, p, o, ab);
+            TS_RHS(k[s], y);
             st->nf++;
             if (s == 6) memcpy(un, y, sizeof(double) * (size_t)n);
         }
-        for (int64_t i = 0; i < n; ++i) {
+        int64_t i;
+        _Pragma("omp parallel for schedule(static) if (threaded)") for (i = 0; i < n; ++i) {
             double acc = 0;
             for (int j = 0; j < 7; ++j) acc += TS_BTILDE[j] * k[j][i];
             err[i] = h * acc;
@@ -662,4 +669,126 @@ int nd_oracle_tsit5(const layout_t* L, double* u, const double* p, double t0, do
     free(o);
     free(ab);
     return status;
+#undef TS_RHS
+}
+
+int nd_oracle_tsit5(const layout_t* L, double* u, const double* p, double t0, double t1, double reltol,
+                    double abstol, int64_t maxsteps, tsit5_stats_t* st) {
+    return tsit5_impl(L, u, p, t0, t1, reltol, abstol, maxsteps, st, 0);
+}
+
+int nd_oracle_tsit5_threaded(const layout_t* L, double* u, const double* p, double t0, double t1, double reltol,
+                             double abstol, int64_t maxsteps, tsit5_stats_t* st) {
+    return tsit5_impl(L, u, p, t0, t1, reltol, abstol, maxsteps, st, 1);
+}
+
+/* ------------------------------------------------------------------------------------------
+ * Barabási–Albert graph for the CPU reference arm of the benchmark, so that the arm loads
+ * nothing outside this directory.  It restates the package's seeded generator (splitmix64-
+ * seeded xoshiro256**, unbiased bounded draws, m initial isolated vertices, every later
+ * vertex attaching m edges to distinct earlier vertices drawn from the endpoint list) and
+ * returns the edges(g) order: (src < dst), sorted lexicographically.  A CPU test checks
+ * that both generators give the same edge lists.
+ * ------------------------------------------------------------------------------------------ */
+typedef struct {
+    uint64_t s[4];
+} gen_rng_t;
+
+static uint64_t gen_rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+static void gen_seed(gen_rng_t* r, uint64_t seed) {
+    uint64_t x = seed;
+    for (int i = 0; i < 4; ++i) {
+        x += 0x9E3779B97F4A7C15ull;
+        uint64_t z = x;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        r->s[i] = z ^ (z >> 31);
+    }
+}
+
+static uint64_t gen_next(gen_rng_t* r) {
+    const uint64_t out = gen_rotl(r->s[1] * 5, 7) * 9;
+    const uint64_t t = r->s[1] << 17;
+    r->s[2] ^= r->s[0];
+    r->s[3] ^= r->s[1];
+    r->s[1] ^= r->s[2];
+    r->s[0] ^= r->s[3];
+    r->s[2] ^= t;
+    r->s[3] = gen_rotl(r->s[3], 45);
+    return out;
+}
+
+static uint64_t gen_below(gen_rng_t* r, uint64_t n) {
+    const uint64_t lim = UINT64_MAX - UINT64_MAX % n;
+    uint64_t x;
+    do x = gen_next(r);
+    while (x >= lim);
+    return x % n;
+}
+
+static int cmp_i64(const void* a, const void* b) {
+    const int64_t x = *(const int64_t*)a, y = *(const int64_t*)b;
+    return (x > y) - (x < y);
+}
+
+/* Returns the number of edges (written up to cap), -1 on bad arguments, -2 out of memory. */
+int64_t nd_oracle_gen_barabasi_albert(int64_t n, int64_t m, uint64_t seed, int64_t* src, int64_t* dst, int64_t cap) {
+    if (m < 1 || n <= m) return -1;
+    const int64_t np = m * (n - m);
+    int64_t* ends = (int64_t*)malloc(sizeof(int64_t) * (size_t)(2 * np));
+    int64_t* ps = (int64_t*)malloc(sizeof(int64_t) * (size_t)np);
+    int64_t* pd = (int64_t*)malloc(sizeof(int64_t) * (size_t)np);
+    int64_t* chosen = (int64_t*)malloc(sizeof(int64_t) * (size_t)m);
+    int64_t* cnt = (int64_t*)calloc((size_t)(n + 1), sizeof(int64_t));
+    int64_t* col = (int64_t*)malloc(sizeof(int64_t) * (size_t)np);
+    if (!ends || !ps || !pd || !chosen || !cnt || !col) {
+        free(ends), free(ps), free(pd), free(chosen), free(cnt), free(col);
+        return -2;
+    }
+    gen_rng_t rng;
+    gen_seed(&rng, seed);
+    int64_t ne_ends = 0, npairs = 0;
+    for (int64_t v = m; v < n; ++v) {
+        int64_t nc = 0;
+        if (v == m) {
+            for (int64_t t = 0; t < m; ++t) chosen[nc++] = t;
+        } else {
+            while (nc < m) {
+                const int64_t t = ends[gen_below(&rng, (uint64_t)ne_ends)];
+                int dup = 0;
+                for (int64_t q = 0; q < nc; ++q) dup |= chosen[q] == t;
+                if (!dup) chosen[nc++] = t;
+            }
+        }
+        for (int64_t q = 0; q < m; ++q) {
+            ps[npairs] = chosen[q];
+            pd[npairs] = v;
+            ++npairs;
+            ends[ne_ends++] = chosen[q];
+            ends[ne_ends++] = v;
+        }
+    }
+    /* counting sort by source (chosen < v always), then each source's targets sorted */
+    for (int64_t i = 0; i < npairs; ++i) cnt[ps[i] + 1]++;
+    for (int64_t i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
+    int64_t* fill = ends; /* reused: n entries are enough (2 np >= n since m >= 1, n > m) */
+    for (int64_t i = 0; i < n; ++i) fill[i] = cnt[i];
+    for (int64_t i = 0; i < npairs; ++i) col[fill[ps[i]]++] = pd[i];
+    int64_t ne = 0;
+    for (int64_t s = 0; s < n; ++s) {
+        qsort(col + cnt[s], (size_t)(cnt[s + 1] - cnt[s]), sizeof(int64_t), cmp_i64);
+        int64_t last = -1;
+        for (int64_t k = cnt[s]; k < cnt[s + 1]; ++k) {
+            if (col[k] == last || col[k] == s) continue;
+            last = col[k];
+            if (ne < cap) {
+                src[ne] = s;
+                dst[ne] = col[k];
+            }
+            ++ne;
+        }
+    }
+    free(ends), free(ps), free(pd), free(chosen), free(cnt), free(col);
+    return ne;
 }

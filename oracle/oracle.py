@@ -76,6 +76,8 @@ def load():
         lib.nd_oracle_layout_new_batched.argtypes = [i64, i64, P64, P64, C.c_int, P32, P32, C.c_int, P32, P32, P32,
                                                      vp]
         lib.nd_oracle_layout_free.argtypes = [vp]
+        lib.nd_oracle_gen_barabasi_albert.restype = i64
+        lib.nd_oracle_gen_barabasi_albert.argtypes = [i64, i64, C.c_uint64, P64, P64, i64]
         for fn in ("nd_oracle_dim", "nd_oracle_pdim"):
             getattr(lib, fn).restype = i64
             getattr(lib, fn).argtypes = [vp]
@@ -92,12 +94,39 @@ def load():
             getattr(lib, fn).argtypes = [vp, vp, vp, vp, vp, vp]
         lib.nd_oracle_num_threads.restype = C.c_int
         lib.nd_oracle_set_num_threads.argtypes = [C.c_int]
-        lib.nd_oracle_tsit5.restype = C.c_int
-        lib.nd_oracle_tsit5.argtypes = [vp, vp, vp, C.c_double, C.c_double, C.c_double, C.c_double, i64,
-                                        C.POINTER(Tsit5Stats)]
+        for fn in (lib.nd_oracle_tsit5, lib.nd_oracle_tsit5_threaded):
+            fn.restype = C.c_int
+            fn.argtypes = [vp, vp, vp, C.c_double, C.c_double, C.c_double, C.c_double, i64, C.POINTER(Tsit5Stats)]
         lib.nd_oracle_tsit5_tableau.argtypes = [vp, vp, vp]
         _lib = lib
     return _lib
+
+
+class EdgeList:
+    """An undirected graph as the oracle's generators return it: 0-based (src < dst) pairs in
+    edges(g) order."""
+
+    def __init__(self, nv, src, dst):
+        self.nv, self.src, self.dst = int(nv), src, dst
+
+    @property
+    def ne(self):
+        return int(self.src.shape[0])
+
+
+def barabasi_albert(n, m, seed=1):
+    """The package's seeded Barabási–Albert graph, generated by the oracle's own copy of the
+    generator (the benchmark's CPU reference arm uses it so that it loads nothing of the
+    package)."""
+    lib = load()
+    P64 = C.POINTER(C.c_int64)
+    ne = lib.nd_oracle_gen_barabasi_albert(n, m, seed, P64(), P64(), 0)
+    if ne < 0:
+        raise ValueError("invalid Barabasi-Albert arguments" if ne == -1 else "out of memory")
+    src = np.empty(max(ne, 1), dtype=np.int64)
+    dst = np.empty(max(ne, 1), dtype=np.int64)
+    lib.nd_oracle_gen_barabasi_albert(n, m, seed, src.ctypes.data_as(P64), dst.ctypes.data_as(P64), ne)
+    return EdgeList(n, src[:ne].copy(), dst[:ne].copy())
 
 
 def tsit5_tableau():
@@ -198,11 +227,14 @@ class OracleNetwork:
         fn = self.lib.nd_oracle_rhs_poly_f64 if dtype == np.float64 else self.lib.nd_oracle_rhs_poly_f32
         return self._rhs(fn, dtype, u, p)
 
-    def tsit5(self, u0, p, t0, t1, reltol=1e-8, abstol=1e-10, maxsteps=10_000_000):
+    def tsit5(self, u0, p, t0, t1, reltol=1e-8, abstol=1e-10, maxsteps=10_000_000, threaded=False):
+        """Tsit5 from t0 to t1.  ``threaded`` runs the RHS and the stage updates on all host
+        threads; the result has the same bits as the sequential solve."""
         u = np.array(u0, dtype=np.float64, copy=True)
         p = np.ascontiguousarray(p if p is not None else np.zeros(0), dtype=np.float64)
         st = Tsit5Stats()
-        self.lib.nd_oracle_tsit5(self.L, u.ctypes.data, _ptr(p), t0, t1, reltol, abstol, maxsteps, C.byref(st))
+        fn = self.lib.nd_oracle_tsit5_threaded if threaded else self.lib.nd_oracle_tsit5
+        fn(self.L, u.ctypes.data, _ptr(p), t0, t1, reltol, abstol, maxsteps, C.byref(st))
         return u, st
 
     def abs_terms(self, u, p):

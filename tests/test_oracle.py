@@ -117,3 +117,33 @@ def test_golden_fixtures_reproduce():
     d = np.load(GOLDEN / "swing_ba200.npz")
     on = O.OracleNetwork(int(d["nv"]), d["src"], d["dst"], O.V_SWING, O.E_KURAMOTO)
     np.testing.assert_array_equal(on.rhs(d["u"], d["p"]), d["du"])
+
+
+def test_threaded_tsit5_equals_sequential_tsit5():
+    """The threaded oracle Tsit5 (PolyesterExecution restatement of the RHS, parallel stage
+    updates) takes the same steps and ends in the same bits as the sequential one: the GPU
+    tests use it for long solves on large networks."""
+    g = nd.barabasi_albert(3000, 2, seed=7)
+    on = O.OracleNetwork.from_graph(g, O.V_SWING, O.E_KURAMOTO)
+    rng = np.random.default_rng(3)
+    u0 = np.zeros(on.dim)
+    u0[0::2] = rng.uniform(-np.pi, np.pi, g.nv)
+    pm = rng.uniform(0.5, 1.5, g.nv) * np.where(np.arange(g.nv) % 2 == 0, 1, -1)
+    pm -= pm.mean()
+    p = np.concatenate([np.stack([np.ones(g.nv), np.full(g.nv, 0.1), pm], 1).ravel(),
+                        rng.uniform(5, 10, g.ne)])
+    a, sa = on.tsit5(u0, p, 0.0, 1.0, reltol=1e-8, abstol=1e-10)
+    b, sb = on.tsit5(u0, p, 0.0, 1.0, reltol=1e-8, abstol=1e-10, threaded=True)
+    assert (sa.naccept, sa.nreject, sa.status) == (sb.naccept, sb.nreject, sb.status)
+    np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("n,m,seed", [(10, 5, 42), (1000, 1, 3), (20_000, 4, 1), (5000, 3, 9)])
+def test_oracle_barabasi_albert_equals_package_generator(n, m, seed):
+    """The oracle's copy of the seeded Barabási–Albert generator (used by the benchmark's CPU
+    reference arm) returns the package generator's edge list."""
+    a = O.barabasi_albert(n, m, seed)
+    b = nd.barabasi_albert(n, m, seed=seed)
+    assert a.nv == b.nv
+    np.testing.assert_array_equal(a.src, b.src)
+    np.testing.assert_array_equal(a.dst, b.dst)
