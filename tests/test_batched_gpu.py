@@ -209,6 +209,33 @@ def test_reference_benchmark_cases(cuda, case):
         check_sine_f64(got, ref, g, nw, u, p)
 
 
+@pytest.mark.parametrize("case,N", __import__("bench").CASES)
+def test_reference_benchmark_cases_at_timed_size(cuda, case, N):
+    """The six reference benchmark networks exactly as `bench.py --cases` times them (largest
+    N, same graphs and inputs), FP64 and FP32 against the oracle: bitwise where no
+    transcendental function enters, within the sine / cos bounds elsewhere, FP32 by the
+    reference's isapprox."""
+    import bench
+    g, vm, em = bench._case_networks(N, case)
+    net = nd.Network(g, vm, em)
+    u, p = bench.case_inputs(case, net, g)
+    vb = [m.kind for m in net.vertex_batches]
+    eb = [(m.kind, capi.COUPLINGS[m.coupling]) for m in net.edge_batches]
+    consts = [m.constants or (0.0, 0.0) for m in net.vertex_batches]
+    on = O.OracleNetwork.from_batches(g.nv, g.src, g.dst, vb, net.vertex_batch, eb, net.edge_batch,
+                                      vertex_constants=consts)
+    ref = on.rhs_poly(u, p)
+    got = gpu_rhs(adapt(net, np.float64), u, p, cuda, np.float64)
+    if case == "diffusion_static_edge":
+        np.testing.assert_array_equal(got, ref)
+    elif case.startswith("powergrid"):
+        assert np.max(np.abs(got - ref) / (1 + np.abs(ref))) < 1e-12
+    else:
+        check_sine_f64(got, ref, g, net, u, p)
+    got32 = gpu_rhs(adapt(net, np.float32), u, p, cuda, np.float32).astype(np.float64)
+    check_f32_isapprox(got32, ref)
+
+
 def test_kernel_counts_of_batched_rhs(cuda):
     g = nd.barabasi_albert(2000, 3, seed=3)
     rng = np.random.default_rng(3)

@@ -187,25 +187,33 @@ def test_wrong_precision_and_sizes_raise(cuda):
         nw64(du64.cpu(), u64, p64, 0.0)
 
 
-def test_full_size_ba10m_properties(cuda):
-    """BA(1e7, m=4) diffusion, F64: exact sequential rows on a sample of vertices
-    (including the largest hubs), f(2u) == 2 f(u) bitwise, and Σ du ≈ 0."""
+def test_full_size_ba10m_against_oracle(cuda):
+    """The headline workload, BA(1e7, m=4) diffusion with the benchmark's seeded inputs: the
+    whole FP64 du equals the sequential oracle (SequentialExecution + SequentialAggregator)
+    bit for bit, f(2u) == 2 f(u) bitwise, and the whole FP32 du is within
+    4e-6 (Σ|terms| + |du|) of the FP64 oracle on the rounded inputs."""
     import torch
     g = nd.barabasi_albert(10_000_000, 4, seed=1)
-    nw = make(g, O.V_DIFFUSION, O.E_DIFFUSION, np.float64)
-    rng = np.random.default_rng(0)
+    rng = np.random.default_rng(1)
     u = rng.normal(size=g.nv)
     p = rng.uniform(0.0, 1.0, size=g.ne)
+    on = O.OracleNetwork.from_graph(g, O.V_DIFFUSION, O.E_DIFFUSION)
+    nw = make(g, O.V_DIFFUSION, O.E_DIFFUSION, np.float64)
     du = gpu_rhs(nw, u, p, cuda, np.float64)
-    deg = g.degree()
-    sample = np.concatenate([np.argsort(deg)[-20:], rng.integers(0, g.nv, size=400)])
-    rows = exact_rows(g, O.V_DIFFUSION, O.E_DIFFUSION, u, p, sample)
-    for v, (val,) in rows.items():
-        assert du[v] == val, (v, deg[v], du[v], val)
+    np.testing.assert_array_equal(du, on.rhs(u, p))
     du2 = gpu_rhs(nw, 2.0 * u, p, cuda, np.float64)
     np.testing.assert_array_equal(du2, 2.0 * du)
-    assert abs(du.sum()) <= 1e-9 * np.abs(du).sum()
     del nw
+    torch.cuda.empty_cache()
+    nw32 = make(g, O.V_DIFFUSION, O.E_DIFFUSION, np.float32)
+    u32, p32 = u.astype(np.float32), p.astype(np.float32)
+    got = gpu_rhs(nw32, u32, p32, cuda, np.float32).astype(np.float64)
+    ref = on.rhs_poly(u32.astype(np.float64), p32.astype(np.float64))
+    terms = on.abs_terms(u32.astype(np.float64), p32.astype(np.float64))
+    d = np.abs(got - ref)
+    ok = d <= 4e-6 * (terms + np.abs(ref))
+    assert ok.all(), f"{(~ok).sum()} entries off; worst {d[~ok].max():.3e}"
+    del nw32
     torch.cuda.empty_cache()
 
 
