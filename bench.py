@@ -47,6 +47,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-f32", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true",
+                    help="skip the basin-stability ensemble (FP32 vs FP64 solves/s) leg")
+    ap.add_argument("--no-warmstart", action="store_true", help="skip the learned warm-start leg")
     ap.add_argument("--cases", action="store_true",
                     help="instead of the headline workload: the reference's benchmark cases at their largest size, "
                          "one JSON line each")
@@ -92,20 +95,24 @@ def kernel_bytes(g, s):
     }
 
 
-def profiled_traffic(dtype_tag, nv, kind):
-    """DRAM bytes per launch of `kind` from the committed ncu summary of this workload
-    (a line `traffic_bytes_per_launch <kind>: <bytes>`), or None."""
+def profiled_traffic(dtype_tag, nv):
+    """DRAM bytes of one RHS from the committed ncu summary of this workload: lines
+    `traffic_bytes_per_launch <kernel>: <bytes>`, summed over the kernels; None when absent."""
     f = ROOT / "profiles" / f"rhs_ba{nv // 1_000_000}m_{dtype_tag}.txt"
     if not f.exists():
         return None
-    key = f"traffic_bytes_per_launch {kind}:"
+    key = "traffic_bytes_per_launch "
+    per = {}
     for line in f.read_text().splitlines():
         if line.startswith(key):
+            name, _, val = line[len(key):].partition(":")
             try:
-                return float(line.split(":", 1)[1].strip())
+                per[name.strip()] = float(val.strip())
             except ValueError:
-                return None
-    return None
+                pass
+    if not per:
+        return None
+    return {"total": sum(per.values()), "kernels": per, "source": f"profiles/{f.name}"}
 
 
 class ClockSampler:
@@ -161,9 +168,7 @@ class ClockSampler:
 def make_workload(nv):
     import nd_gb300 as nd
     g = nd.barabasi_albert(nv, M_BA, seed=SEED)
-    rng = np.random.default_rng(SEED)
-    u = rng.normal(size=nv)
-    w = rng.uniform(0.0, 1.0, size=g.ne)
+    u, w = make_inputs(nv, g.ne)
     return g, u, w
 
 
@@ -218,23 +223,41 @@ def cpu_baseline(g, u, w, seconds=12.0):
     return res
 
 
+def workload_config(g):
+    """The config dict both arms print: the workload and its sizes, nothing arm-specific."""
+    deg = np.bincount(g.src, minlength=g.nv) + np.bincount(g.dst, minlength=g.nv)
+    B = algorithmic_bytes(g.nv, g.ne, 8)
+    return {"workload": f"diffusion on Barabasi-Albert N={g.nv}, m={M_BA}, F64 RHS", "nv": g.nv, "ne": g.ne,
+            "incidences": 2 * g.ne, "max_degree": int(deg.max()), "hub_rows": int((deg > 32).sum()),
+            "sum_order": "sequential (bitwise = SequentialAggregator)",
+            "l2": "no flush: inputs+topology %.2f GB > 129 MB L2" % (B / 1e9)}
+
+
+def make_inputs(nv, ne):
+    rng = np.random.default_rng(SEED)
+    return rng.normal(size=nv), rng.uniform(0.0, 1.0, size=ne)
+
+
 def run_reference(args, rank, world):
     """CPU reference arm: the threaded oracle restatement (PolyesterExecution +
-    PolyesterAggregator) on all host cores, same workload and metric."""
+    PolyesterAggregator) on all host cores, same workload, config and metric.  It loads
+    nothing of the package: the graph comes from the oracle's copy of the generator."""
     if rank != 0:
         return
     from oracle import oracle as O
-    g, u, w = make_workload(args.nv)
+    g = O.barabasi_albert(args.nv, M_BA, SEED)
+    u, w = make_inputs(g.nv, g.ne)
     on = O.OracleNetwork.from_graph(g, O.V_DIFFUSION, O.E_DIFFUSION)
     threads = os.cpu_count() or 1
     O.load().nd_oracle_set_num_threads(threads)
-    for _ in range(min(args.warmup, 3)):
+    for _ in range(max(args.warmup, 3)):
         on.rhs_poly(u, w)
-    # each step is one full RHS; the number of timed steps is capped at ~60 s of CPU time
+    # each step is one full RHS; a run asked for more steps than ~3 minutes of host time
+    # holds is cut to that many (the line says how many ran)
     t0 = time.perf_counter()
     on.rhs_poly(u, w)
     one = time.perf_counter() - t0
-    steps = max(1, min(args.steps, int(60.0 / max(one, 1e-6))))
+    steps = max(1, min(args.steps, int(180.0 / max(one, 1e-6))))
     t0 = time.perf_counter()
     for _ in range(steps):
         on.rhs_poly(u, w)
@@ -242,12 +265,12 @@ def run_reference(args, rank, world):
     val = g.ne * steps / el
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": "edges/s", "n_gpus": args.gpus,
-        "steps": steps, "warmup": min(args.warmup, 3), "ms_per_step": 1e3 * el / steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"diffusion on Barabasi-Albert N={args.nv}, m={M_BA}, F64 RHS", "nv": args.nv,
-                   "ne": g.ne, "parallelism": "host threads"},
+        "steps": steps, "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * el / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded BA graph, w~U(0,1), u~N(0,1))", "config": workload_config(g),
+        "execution": f"host threads ({threads})",
         "cpu_baseline": {"value": val, "unit": "edges/s", "cores": threads, "kind": "port",
-                         "sample": f"{steps} full RHS evaluations (steps capped at ~60 s of CPU time) of the "
+                         "sample": f"{steps} full RHS evaluations (at most ~3 minutes of host time) of the "
                                    "PolyesterExecution+PolyesterAggregator restatement"},
         "e2e": {"value": val, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -322,26 +345,27 @@ def run_gb300(args, rank, world, local):
         k["stream"] = "side (overlapped)" if kind == "heavy_rows" else "caller"
         k["share"] = k["avg_ms"] * k["launches"] / total_ms if (total_ms and kind in main) else None
     dom = max(main, key=lambda k: kernels[k]["avg_ms"] * kernels[k]["launches"])
-    achieved = kernels[dom]["achieved_gbs"]
-    traffic = profiled_traffic("f64", nv, dom)
+    traffic = profiled_traffic("f64", nv)
+    rhs_gbs = B / (t / args.steps) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded BA graph, w~U(0,1), u~N(0,1))",
-        "config": {"workload": f"diffusion on Barabasi-Albert N={nv}, m={M_BA}, F64 RHS", "nv": nv, "ne": ne,
-                   "incidences": 2 * ne, "max_degree": info.max_degree, "hub_rows": info.n_hubs,
-                   "sum_order": "sequential (bitwise = SequentialAggregator)",
-                   "l2": "no flush: inputs+topology %.2f GB > 129 MB L2" % (B / 1e9),
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": workload_config(g),
+        "execution": "replicas, one per GPU" if world > 1 else "single GPU",
         "edges_per_s": value, "incidences_per_s": 2 * value, "rhs_evals_per_s": world * args.steps / t,
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
-                     "rhs_achieved_gbs": B / (t / args.steps) / 1e9, "rhs_frac": B / (t / args.steps) / 1e9 / hbm,
-                     "kernels": kernels,
-                     "note": "achieved = algorithmic bytes of one launch of the dominant kernel / its mean "
-                             "CUDA-event duration (%d event-bracketed RHS calls after the timed region); "
-                             "rhs_achieved_gbs = whole-RHS algorithmic bytes 8(2N+E) + 4(N+1) + 16E / "
-                             "timed ms_per_step" % kt},
+        "roofline": {"bound": "hbm", "kernel": "whole RHS (%s)" % " + ".join(kernels), "achieved": rhs_gbs,
+                     "peak": hbm, "unit": "GB/s", "frac": rhs_gbs / hbm, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_rhs": B,
+                     "traffic": traffic["total"] if traffic else None,
+                     "traffic_per_kernel": traffic["kernels"] if traffic else None,
+                     "traffic_source": traffic["source"] if traffic else None,
+                     "dominant_kernel": dom, "kernels": kernels,
+                     "note": "achieved = the RHS's algorithmic bytes 8(2N+E) + 4(N+1) + 16E (read u, write du, "
+                             "read w; CSR row pointers and incidences, each byte once) / timed ms_per_step; "
+                             "traffic = DRAM bytes of one RHS, summed over its kernels, from the committed ncu "
+                             "summary; kernels[*].bytes_per_launch are each kernel's own design bytes "
+                             "(intermediate buffers included), timed over %d event-bracketed RHS calls" % kt},
         "gpu_launches": sum(n for n, _ in counts.values()),
         "gpu_launches_by_kernel": {k: n for k, (n, _) in counts.items() if n},
     }
@@ -354,6 +378,18 @@ def run_gb300(args, rank, world, local):
         tm = time_device(nw, du, u, p, ks, stream)
         modes[mode] = {"ms_per_step": 1e3 * tm / ks, "edges_per_s": ne * ks / tm}
     nw.set_sum_order("sequential")
+    # the single fused kernel over the destination-sorted CSR (every incidence evaluates its
+    # edge from u and p; the layout for edge lists in any order)
+    nw.set_layout("fused")
+    nw(du, u, p, 0.0)
+    tm = time_device(nw, du, u, p, ks, stream)
+    fused_out = du.clone()
+    nw.set_layout("auto")
+    nw(du, u, p, 0.0)
+    torch.cuda.synchronize()
+    modes["fused"] = {"ms_per_step": 1e3 * tm / ks, "edges_per_s": ne * ks / tm,
+                      "same_bits_as_two_phase": bool(torch.equal(fused_out, du))}
+    del fused_out
     line["f64_modes"] = modes
     # FP32 variant (compensated sums at hubs)
     if not args.no_f32:
@@ -435,6 +471,27 @@ def run_gb300(args, rank, world, local):
         ok = np.array_equal(duh[(ke - 1) & 1].numpy(), dub[(ke - 1) & 1].cpu().numpy())
         line["e2e"]["result_matches_device"] = bool(ok)
     line["clocks"] = clk.summary()
+    # the second half of the headline metric: ensemble solves/s, FP32 vs FP64, and the
+    # learned warm start (single-GPU runs; the instances are independent replicas)
+    if world == 1 and not (args.no_ensemble and args.no_warmstart):
+        from nd_gb300 import benchmarks as NB
+        del nw, u, p, du
+        torch.cuda.empty_cache()
+        if not args.no_ensemble:
+            ens = NB.ensemble(4096)
+            line["ensemble"] = {
+                "metric": "ensemble solves/s FP32 vs FP64 @1e-6", "workload": ens["workload"],
+                "solves_per_s_f32_batched": ens["f32"]["solves_per_s"],
+                "solves_per_s_f64_batched": ens["f64"]["solves_per_s"],
+                "solves_per_s_plain_f64": ens["plain_f64_per_instance"]["solves_per_s"],
+                "f32_batched_vs_plain_f64": ens["f32_batched_vs_plain_f64"],
+                "f32_batched_vs_f64_batched": ens["f32"]["solves_per_s"] / ens["f64"]["solves_per_s"],
+                "details": ens}
+            torch.cuda.empty_cache()
+        if not args.no_warmstart:
+            ws = NB.warmstart()
+            line["warm_start"] = {"metric": "Newton iterations to residual 1e-10, cold / warm", **ws}
+            torch.cuda.empty_cache()
     if rank == 0 and world == 1 and not args.no_cpu:
         res = cpu_baseline(g, u_h, w_h)
         v, n, thr, el = res["poly"]
@@ -475,6 +532,21 @@ def _case_networks(N, name):
         nd.static_kuramoto_edge()
 
 
+def case_inputs(name, net, g):
+    """Seeded u, p of a benchmark case: N(0,1) states and U(0.5,1.5) parameters; the power
+    grids get line and machine data in the ranges of per-unit grid models."""
+    rng = np.random.default_rng(2)
+    u = rng.normal(size=net.dim)
+    p = rng.uniform(0.5, 1.5, size=net.pdim)
+    if name.startswith("powergrid"):
+        p = net.pflat(vertex={"P": rng.uniform(-1, 1, g.nv), "Q": rng.uniform(-1, 1, g.nv), "H": 5.0,
+                              "D": 0.1, "Ω": 2 * np.pi * 50, "E_f": 1.0, "T_d_dash": 7.0, "T_q_dash": 0.5,
+                              "X_d_dash": 0.3, "X_q_dash": 0.6, "X_d": 1.8, "X_q": 1.7},
+                      edge={"L": 1e-3, "R": 0.05, "C1": 1e-5, "C2": 1e-5})
+        u = 1.0 + 0.1 * rng.normal(size=net.dim)
+    return u, p
+
+
 CASES = (("diffusion_static_edge", 3000), ("diffusion_ode_edge", 3000), ("kuramoto_homogeneous", 100_000),
          ("kuramoto_heterogeneous", 100_000), ("powergrid", 100_000), ("powergrid_inhomogeneous_pq", 100_000))
 
@@ -494,15 +566,7 @@ def run_cases(args):
     for name, N in CASES:
         g, vm, em = _case_networks(N, name)
         net = nd.Network(g, vm, em)
-        rng = np.random.default_rng(2)
-        u = rng.normal(size=net.dim)
-        p = rng.uniform(0.5, 1.5, size=net.pdim)
-        if name.startswith("powergrid"):  # line and machine data in the ranges of per-unit grid models
-            p = net.pflat(vertex={"P": rng.uniform(-1, 1, g.nv), "Q": rng.uniform(-1, 1, g.nv), "H": 5.0,
-                                  "D": 0.1, "Ω": 2 * np.pi * 50, "E_f": 1.0, "T_d_dash": 7.0, "T_q_dash": 0.5,
-                                  "X_d_dash": 0.3, "X_q_dash": 0.6, "X_d": 1.8, "X_q": 1.7},
-                          edge={"L": 1e-3, "R": 0.05, "C1": 1e-5, "C2": 1e-5})
-            u = 1.0 + 0.1 * rng.normal(size=net.dim)
+        u, p = case_inputs(name, net, g)
         line = {"case": name, "N": N, "ne": g.ne, "dim": net.dim, "pdim": net.pdim,
                 "vertex_batches": len(net.vertex_batches), "edge_batches": len(net.edge_batches)}
         for tag, dt, s in (("f64", torch.float64, 8), ("f32", torch.float32, 4)):
