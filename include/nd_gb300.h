@@ -298,20 +298,26 @@ int nd_solve_tsit5(nd_handle* h, double* u, const void* p, double t0, double t1,
                    int64_t max_steps, nd_solve_stats* stats, void* stream);
 
 /* Allocation-free RHS.  This entry point has no counterpart in the reference.  It is for
- * callers that must not allocate device memory while they evaluate the RHS, for example
- * code recording a solver step into a CUDA graph during a stream capture (where cudaMalloc
- * is not allowed), or a process whose device memory belongs to a caching allocator.  It
- * calls no cudaMalloc / cudaFree: the caller passes the topology as device arrays, and
- * the edge values go to one file-scope device array of 64 MiB (8 Mi FP64 or 16 Mi FP32
- * edges) that every GPU loading the library holds until the process exits.
+ * callers that must not allocate device memory while they evaluate the RHS: a process
+ * whose device memory belongs to a caching allocator (CUDA.jl's or PyTorch's pool), where a
+ * library's own cudaMalloc can fail or fragment the pool, or a host program that budgets
+ * its device memory once up front.  It calls no cudaMalloc / cudaFree: the caller passes
+ * the topology as device arrays, and the edge values go to one file-scope device array of
+ * 64 MiB (8 Mi FP64 or 16 Mi FP32 edges) that every GPU loading the library holds until the
+ * process exits.
  *   edges  canonical list (sorted by source, src < dst): src[ne], dst[ne] (0-based int32)
  *   src_ptr[nv+1]  first edge of each vertex's source block
  *   dst_ptr[nv+1], dst_eid[ne]  each vertex's destination-side edge ids, ascending
  *   du, u, p  as for nd_rhs, element type `dtype`
+ * The arrays must describe a canonical list exactly as nd_create would sort it; they are
+ * device arrays and are not checked.  Another order still gives the network's RHS, but its
+ * sums run in that order, not the reference's.
  * Result: the same du as nd_rhs on the same network.  ne above the scratch size returns
  * ND_ERR_ARG.  The first call on a device looks up the scratch array's device address
- * (cudaGetSymbolAddress) and should come before any stream capture.  All calls share the
- * scratch: calls that overlap on the GPU (other streams, other host threads) race. */
+ * (cudaGetSymbolAddress, with that device current) and should come before any stream
+ * capture; the lookup is repeated only after the device's context was reset.  All calls
+ * share the scratch and it keeps the last call's values: calls that overlap on the GPU
+ * (other streams, other host threads) race. */
 int nd_rhs_static_scratch(int dtype, int vertex_kind, int edge_kind, int64_t nv, int64_t ne, const int32_t* src,
                           const int32_t* dst, const uint32_t* src_ptr, const uint32_t* dst_ptr,
                           const int32_t* dst_eid, void* du, const void* u, const void* p, void* stream);
@@ -347,9 +353,12 @@ int nd_ensemble_rhs(nd_ensemble* e, int dtype, void* du, const void* u, const vo
 /* Every instance integrated from t0 to t1 by Tsit5 with its own adaptive steps (FP64
  * state, error norm and control; RHS in the ensemble's precision), in one persistent
  * kernel replayed from a CUDA graph.  u: packed FP64 device state (in: u0, out: u(t1)).
- * status[i] (device int32): ND_OK, ND_ERR_MAXITERS (step budget max_steps, <= 0 = none)
- * or ND_ERR_NOT_CONVERGED; nsteps[i] (device int64): steps taken.  threads per instance:
+ * status[i] (device int32): ND_OK, ND_ERR_MAXITERS (more than max_steps steps, the
+ * per-instance budget; max_steps <= 0 means ND_ENSEMBLE_DEFAULT_MAX_STEPS, the 1e5 of
+ * SciML's default maxiters, so that no solve can keep the GPU busy without end) or
+ * ND_ERR_NOT_CONVERGED; nsteps[i] (device int64): steps taken.  threads per instance:
  * 64/128/256/512, or 0 for the autotuned / default choice.  Stream-ordered. */
+#define ND_ENSEMBLE_DEFAULT_MAX_STEPS 100000
 int nd_ensemble_solve_tsit5(nd_ensemble* e, double* u, const void* p, double t0, double t1, double reltol,
                             double abstol, int64_t max_steps, int threads, int32_t* status, int64_t* nsteps,
                             void* stream);

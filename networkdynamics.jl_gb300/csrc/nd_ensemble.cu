@@ -682,7 +682,7 @@ int nd_ensemble_solve_tsit5(nd_ensemble* e, double* u, const void* p, double t0,
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device);
     const int blocks = (int)std::min<int64_t>(e->n_inst, (int64_t)sms * std::max(1, per_sm));
-    SolveParams sp{t0, t1, reltol, abstol, max_steps > 0 ? max_steps : (int64_t)1 << 40, e->dim};
+    SolveParams sp{t0, t1, reltol, abstol, max_steps > 0 ? max_steps : (int64_t)ND_ENSEMBLE_DEFAULT_MAX_STEPS, e->dim};
     const EnsArgs a = args_of(e);
     // The persistent kernel (and the reset of its work queue) run as one captured graph.
     cudaStream_t s = (cudaStream_t)stream;

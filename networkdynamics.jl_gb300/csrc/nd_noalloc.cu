@@ -1,13 +1,12 @@
 // Allocation-free RHS entry point: nd_rhs_static_scratch (include/nd_gb300.h).
 //
-// Who needs it: a caller that must not allocate device memory while it runs the RHS --
-// for example code that records the solver's step into a CUDA graph while a stream
-// capture is open (cudaMalloc is not allowed inside the capture), or a process whose
-// device memory is entirely owned by a caching allocator (CUDA.jl's or PyTorch's pool),
-// where a stray cudaMalloc from a library can fail or fragment the pool.  nd_create
-// allocates the network's topology and its scratch; this entry point allocates nothing:
-// the caller passes the topology arrays and the input / output buffers, and the scratch
-// comes from one file-scope __device__ array of fixed size.
+// Who needs it: a caller that must not allocate device memory while it runs the RHS,
+// for example a process whose device memory is owned by a caching allocator (CUDA.jl's
+// or PyTorch's pool), where a library's own cudaMalloc can fail once the pool holds the
+// memory or fragment it, or a host program with a fixed device-memory budget that it
+// allocates once up front.  nd_create allocates the network's topology and its scratch;
+// this entry point allocates nothing: the caller passes the topology arrays and the input /
+// output buffers, and the scratch comes from one file-scope __device__ array of fixed size.
 //
 // The computation is the two-phase RHS of nd_rhs_edge.cu in its simplest form: phase E
 // writes each edge's value y_e = g(u_src, u_dst, p_e) to the scratch array, phase R sums
@@ -33,19 +32,41 @@ __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mutex;
 void* g_scratch_ptr[kMaxDevices] = {};
+void* g_scratch_ctx[kMaxDevices] = {};  // the context the cached address belongs to
 
-// Device address of the scratch on the current device; looked up once per device.
+// The current driver context (cuCtxGetCurrent through the runtime's entry-point query, so
+// the library needs no link to libcuda); nullptr when the query is unavailable.
+void* current_context() {
+    using GetCurrent = int (*)(void**);
+    static GetCurrent fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return reinterpret_cast<GetCurrent>(f);
+    }();
+    void* ctx = nullptr;
+    if (fn && fn(&ctx) != 0) ctx = nullptr;
+    return ctx;
+}
+
+// Device address of the scratch on the current device.  The set-up (cudaGetSymbolAddress
+// with the device current) runs on the first call on a device, and again only if that
+// device's context was replaced since (cudaDeviceReset), which reloads the module.
 cudaError_t scratch_address(void** out) {
     int dev = 0;
     cudaError_t err = cudaGetDevice(&dev);
     if (err != cudaSuccess) return err;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_ptr[dev]) {
+    void* ctx = g_scratch_ptr[dev] ? current_context() : nullptr;
+    if (!g_scratch_ptr[dev] || ctx != g_scratch_ctx[dev]) {
         void* p = nullptr;
         err = cudaGetSymbolAddress(&p, g_static_scratch);
         if (err != cudaSuccess) return err;
         g_scratch_ptr[dev] = p;
+        g_scratch_ctx[dev] = current_context();
     }
     *out = g_scratch_ptr[dev];
     return cudaSuccess;

@@ -46,6 +46,7 @@ COUPLINGS = {"AntiSymmetric": ND_ANTISYMMETRIC, "Symmetric": ND_SYMMETRIC, "Dire
              "Fiducial": ND_FIDUCIAL}
 
 ND_MAX_BATCHES = 1 << 20
+ND_ENSEMBLE_DEFAULT_MAX_STEPS = 100000  # per-instance step budget of nd_ensemble_solve_tsit5 for max_steps <= 0
 ND_BATCH_CONSTANTS = 2
 
 ND_ORDER_SEQUENTIAL = 0

@@ -88,6 +88,9 @@ class Ensemble:
                                              p.data_ptr() if p is not None else None, self._stream(stream)))
 
     def solve_tsit5(self, u0, p, tspan, reltol=1e-6, abstol=1e-8, max_steps=0, threads=0, stream=None):
+        """Tsit5 of every instance over tspan.  max_steps is the per-instance step budget;
+        0 means capi.ND_ENSEMBLE_DEFAULT_MAX_STEPS (1e5, SciML's default maxiters).  An
+        instance that runs out gets status ND_ERR_MAXITERS."""
         import torch
         u = u0.to(torch.float64).clone() if isinstance(u0, torch.Tensor) else torch.tensor(u0, dtype=torch.float64,
                                                                                            device="cuda")

@@ -101,6 +101,23 @@ def test_ensemble_step_budget_reports_status(cuda):
     assert (res.nsteps.cpu().numpy() == 3).all()
 
 
+def test_ensemble_default_step_budget(cuda):
+    """max_steps = 0 is the finite default budget (1e5 steps per instance): a solve that
+    would need far more steps ends with ND_ERR_MAXITERS instead of occupying the GPU."""
+    import torch
+    g = nd.cycle_graph(4)
+    # injections far above what the lines carry (|P| = 5 > K = 1): no steady state, the
+    # phases keep oscillating with periods of O(1), so a horizon of 1e9 needs ~1e10 steps
+    P = np.array([5.0, -5.0, 5.0, -5.0])
+    p = torch.from_numpy(np.concatenate([np.stack([np.ones(4), np.full(4, 0.1), P], 1).ravel(),
+                                         np.full(4, 1.0)])).to(cuda)
+    ens = Ensemble([g], nd.kuramoto_second(), nd.static_line(), torch.float64)
+    u0 = torch.from_numpy(np.array([0.3, 0.0, -0.2, 0.0, 0.1, 0.0, 0.0, 0.0])).to(cuda)
+    res = ens.solve_tsit5(u0, p, (0.0, 1e9), reltol=1e-8, abstol=1e-10, max_steps=0)
+    assert int(res.status.cpu()[0]) == nd.capi.ND_ERR_MAXITERS
+    assert int(res.nsteps.cpu()[0]) == nd.capi.ND_ENSEMBLE_DEFAULT_MAX_STEPS
+
+
 def test_fixpoint_known_answer_and_oracle(cuda):
     import torch
     # 4-node swing of test/initialization_test.jl:15-38 (asin(1/12) phase steps)

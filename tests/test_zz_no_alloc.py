@@ -1,10 +1,11 @@
 """The allocation-free RHS entry point (nd_rhs_static_scratch) against the regular one.
 
 nd_rhs_static_scratch serves callers that cannot allocate device memory while they run
-the RHS (a step being recorded into a CUDA graph, a process whose device memory belongs
-to a caching allocator).  It takes the topology as device arrays and keeps its edge
-values in a fixed file-scope device array.  Here it must reproduce nd_rhs on the same
-network, on two calls in a row (the second call reuses the scratch the first one left).
+the RHS (a process whose device memory belongs to a caching allocator such as CUDA.jl's
+or PyTorch's pool, or one that budgets its device memory up front).  It takes the
+topology as device arrays and keeps its edge values in a fixed file-scope device array.
+Here it must reproduce nd_rhs on the same network, on two calls in a row (the second call
+reuses the scratch the first one left), and leave the device's free memory unchanged.
 This file runs last so a failure here never hides the other tests.
 """
 import ctypes as C
@@ -64,8 +65,12 @@ def test_static_scratch_rhs_matches_nd_rhs(cuda, vk, ek, make_vm, make_em):
         ref = torch.empty_like(u)
         nw(ref, u, p, 0.0)
         got = torch.full_like(u, float("nan"))
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         capi.check(static_rhs(lib, vk, ek, g, dev_arrays, got, u, p, capi.ND_F64))
         torch.cuda.synchronize()
+        if call == 1:  # after the first call (module and scratch loaded) nothing is allocated
+            assert torch.cuda.mem_get_info()[0] == free_before
         # same operations in the same order as nd_rhs: identical bits
         np.testing.assert_array_equal(got.cpu().numpy(), ref.cpu().numpy())
     # FP32: within the FP32 tolerance of the parity tests (the regular path adds long rows
@@ -89,3 +94,31 @@ def test_static_scratch_rejects_oversized_networks(cuda):
                                      None, None, None, None, None, None, None, None, None)
     assert code == capi.ND_ERR_ARG
     assert "exceed the static scratch" in capi.last_error()
+
+
+@pytest.mark.gpu
+def test_static_scratch_with_a_non_canonical_order(cuda):
+    """Arrays that are not the canonical sort are not detected (they live on the device);
+    the result is still the network's RHS, summed in the arrays' order: equal to nd_rhs
+    within the rounding of a reordered FP64 sum, not bit for bit."""
+    import torch
+    lib = capi.load()
+    g = nd.barabasi_albert(50_000, 4, seed=43)
+    src_ptr, dst_ptr, dst_eid = csr_arrays(g)
+    rng = np.random.default_rng(2)
+    for v in range(g.nv):  # reverse each vertex's destination-side order
+        a, b = int(dst_ptr[v]), int(dst_ptr[v + 1])
+        dst_eid[a:b] = dst_eid[a:b][::-1]
+    dev_arrays = [torch.from_numpy(np.ascontiguousarray(x)).to(cuda) for x in
+                  (g.src.astype(np.int32), g.dst.astype(np.int32), src_ptr.view(np.int32), dst_ptr.view(np.int32),
+                   dst_eid)]
+    on = O.OracleNetwork.from_graph(g, O.V_DIFFUSION, O.E_DIFFUSION)
+    u_h, p_h = random_inputs(on, O.V_DIFFUSION, rng)
+    u = torch.from_numpy(u_h).to(cuda)
+    p = torch.from_numpy(p_h).to(cuda)
+    ref = torch.empty_like(u)
+    nd.adapt(nd.Network(g, nd.diffusion_vertex(), nd.diffusion_edge()), torch.float64)(ref, u, p, 0.0)
+    got = torch.empty_like(u)
+    capi.check(static_rhs(lib, O.V_DIFFUSION, O.E_DIFFUSION, g, dev_arrays, got, u, p, capi.ND_F64))
+    d = np.abs(got.cpu().numpy() - ref.cpu().numpy())
+    assert np.all(d <= 1e-13 * on.abs_terms(u_h, p_h))
