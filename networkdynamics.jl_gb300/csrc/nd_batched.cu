@@ -493,13 +493,25 @@ int validate_batched(const nd_batched_network_desc* d) {
         const int32_t b = d->vertex_batch[v];
         if (b < 0 || b >= nvb) return fail(ND_ERR_ARG, "vertex " + std::to_string(v) + " has no valid batch");
     }
+    int64_t states = 0, params = 0;
+    for (int64_t v = 0; v < nv; ++v) {
+        const int k = d->vertex_batches[d->vertex_batch[v]].kind;
+        states += vertex_dim(k);
+        params += vertex_pdim(k);
+    }
     for (int64_t e = 0; e < ne; ++e) {
         const int32_t b = d->edge_batch[e];
         if (b < 0 || b >= neb) return fail(ND_ERR_ARG, "edge " + std::to_string(e) + " has no valid batch");
         const int64_t s = d->src[e], t = d->dst[e];
         if (s < 0 || s >= nv || t < 0 || t >= nv)
             return fail(ND_ERR_ARG, "edge " + std::to_string(e) + " has endpoint out of range");
+        states += edge_dim(d->edge_batches[b].kind);
+        params += edge_pdim(d->edge_batches[b].kind);
     }
+    // the kernels index states and parameters with 32-bit offsets
+    if (states > (int64_t)INT32_MAX) return fail(ND_ERR_UNSUPPORTED, "more than 2^31-1 states in a batched network");
+    if (params > (int64_t)INT32_MAX)
+        return fail(ND_ERR_UNSUPPORTED, "more than 2^31-1 parameters in a batched network");
     return ND_OK;
 }
 
@@ -558,8 +570,7 @@ int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out) {
         par += ecount[b] * edge_pdim(k);
     }
     eb.pos0[neb] = pos;
-    if (st > (int64_t)INT32_MAX) return fail(ND_ERR_UNSUPPORTED, "more than 2^31-1 states in a batched network");
-    (void)vdim_total;
+    (void)vdim_total;  // states and parameters fit 32-bit offsets: checked by validate_batched
 
     // vertex positions and the u index of every vertex output (its first state)
     std::vector<int64_t> fill(vb.pos0.begin(), vb.pos0.begin() + nvb);
