@@ -123,6 +123,13 @@ function edge_batch_kind(batch)
 end
 
 function GB300Aggregator(im, batches, f)
+    # External inputs (the ExtMap gather, src/external_inputs.jl:51-80) and loopback edges
+    # (the injector copy, src/post_utils.jl:213-248) are rejected by name, before any
+    # component lookup: no library component reads external inputs or is an injector.
+    NetworkDynamics.has_external_input(im) &&
+        throw(ArgumentError("GB300Execution supports networks without external inputs only"))
+    any(NetworkDynamics.is_loopback, im.edgem) &&
+        throw(ArgumentError("GB300Execution supports networks without LoopbackConnection edges only"))
     # vertex batches exactly as the Network formed them (src/construction.jl:155-160)
     vidxs = NetworkDynamics._find_identical_components(im.vertexm)
     vbatches = map(vidxs) do idxs

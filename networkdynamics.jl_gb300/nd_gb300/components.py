@@ -29,6 +29,7 @@ class VertexModel:
     outdim: int = 1                     # StateMask(1:outdim)
     mass_matrix: Optional[float] = None  # 0: algebraic states (the PQ bus); None: identity
     constants: tuple = ()               # values the component function closes over
+    extin: Optional[Sequence] = None    # external inputs (VIndex / EIndex of other components' states)
 
 
 @dataclass
@@ -43,6 +44,8 @@ class EdgeModel:
     f: Optional[Callable] = None
     g: Optional[Callable] = None
     outdim: int = 1                     # per side
+    extin: Optional[Sequence] = None    # external inputs (VIndex / EIndex of other components' states)
+    loopback: bool = False              # a LoopbackConnection: copies the dst output into the src input
 
 
 # --- vertices (test/ComponentLibrary.jl) -------------------------------------------------

@@ -82,6 +82,23 @@ def _check_library(models, what):
             "GB300Execution has no CPU fallback")
 
 
+def _check_no_external_inputs(vms, ems):
+    """Networks with external inputs (the ExtMap gather of src/external_inputs.jl:51-80) or
+    loopback edges (the injector copy of src/post_utils.jl:213-248, applied at
+    src/coreloop.jl:47) are rejected by name: no library component reads external inputs or
+    has a feed-forward output, so neither map can be built for a GB300 network."""
+    bad = next((m for m in list(vms) + list(ems) if m.extin), None)
+    if bad is not None:
+        raise capi.ArgumentError(capi.ND_ERR_ARG,
+                                 f"{bad.name!r} has external inputs; GB300Execution supports networks without "
+                                 "external inputs only (no library component reads them)")
+    bad = next((m for m in ems if m.loopback), None)
+    if bad is not None:
+        raise capi.ArgumentError(capi.ND_ERR_ARG,
+                                 f"{bad.name!r} is a LoopbackConnection; GB300Execution supports networks without "
+                                 "loopback edges only (no library vertex is an injector with a feed-forward output)")
+
+
 def _batches(models, key):
     """Batches of identical components in order of first appearance, as find_identical
     groups them (src/utils.jl:197-216, src/construction.jl:155-168): the model of every
@@ -126,6 +143,7 @@ class Network:
         if not ems:
             raise capi.ArgumentError(capi.ND_ERR_ARG,
                                      "a graph without edges needs the edge model passed as a single EdgeModel")
+        _check_no_external_inputs(vms, ems)
         _check_library(vms, "vertex")
         _check_library(ems, "edge")
         # src/construction.jl:98-106

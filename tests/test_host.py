@@ -37,6 +37,27 @@ def test_unsupported_component_raises_no_fallback():
         nd.Symmetric(nd.diffusion_odeedge())  # the wrappers take a static single-sided g
 
 
+def test_external_inputs_and_loopback_edges_are_rejected_by_name():
+    """A network with external inputs (src/external_inputs.jl:51-80) or loopback edges
+    (src/post_utils.jl:213-248) raises ArgumentError naming the feature, before any
+    component lookup, also when the component would otherwise be a library one."""
+    import dataclasses
+    g = nd.cycle_graph(4)
+    v_ext = dataclasses.replace(nd.kuramoto_first(), extin=[("VIndex", 2, "θ")])
+    with pytest.raises(nd.ArgumentError, match="external inputs"):
+        nd.Network(g, v_ext, nd.kuramoto_edge())
+    user_ext = nd.VertexModel("fvext", dim=1, pdim=0, f=lambda *a: None, extin=[("VIndex", 2, "a")])
+    with pytest.raises(nd.ArgumentError, match="external inputs") as err:
+        nd.Network(g, user_ext, nd.diffusion_edge())
+    assert not isinstance(err.value, nd.UnsupportedComponentError)
+    e_ext = dataclasses.replace(nd.diffusion_edge(), extin=[("EIndex", 2, "a")])
+    with pytest.raises(nd.ArgumentError, match="external inputs"):
+        nd.Network(g, nd.diffusion_vertex(), e_ext)
+    loop = dataclasses.replace(nd.diffusion_edge(), loopback=True)
+    with pytest.raises(nd.ArgumentError, match="LoopbackConnection"):
+        nd.Network(g, nd.diffusion_vertex(), [nd.diffusion_edge()] * (g.ne - 1) + [loop])
+
+
 def test_heterogeneous_network_layout():
     """Batches in order of first appearance, laid out batch by batch; edge states after
     every vertex state (src/construction.jl:155-195, src/network_structure.jl:224-258)."""
