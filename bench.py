@@ -479,13 +479,24 @@ def run_gb300(args, rank, world, local):
         torch.cuda.empty_cache()
         if not args.no_ensemble:
             ens = NB.ensemble(4096)
+            keys = ("synchronised_median", "synchronised_p95", "synchronised_max", "synchronised_within_1e-6",
+                    "median_instance", "instances_within_1e-6", "desynchronised_median", "sync_verdict_agreement")
             line["ensemble"] = {
                 "metric": "ensemble solves/s FP32 vs FP64 @1e-6", "workload": ens["workload"],
+                "instances": 4096, "sync_fraction_f64": ens["sync_fraction_f64"],
                 "solves_per_s_f32_batched": ens["f32"]["solves_per_s"],
+                "solves_per_s_f32x2_batched": ens["f32x2"]["solves_per_s"],
                 "solves_per_s_f64_batched": ens["f64"]["solves_per_s"],
                 "solves_per_s_plain_f64": ens["plain_f64_per_instance"]["solves_per_s"],
                 "f32_batched_vs_plain_f64": ens["f32_batched_vs_plain_f64"],
+                "f32x2_batched_vs_plain_f64": ens["f32x2_batched_vs_plain_f64"],
                 "f32_batched_vs_f64_batched": ens["f32"]["solves_per_s"] / ens["f64"]["solves_per_s"],
+                "final_state_err_vs_f64": {k: {x: ens[f"{k}_final_state_err_vs_f64"][x] for x in keys}
+                                           for k in ("f32", "f32x2", "f64_1ulp", "f64_f32params")},
+                "note": "f32: FP32 RHS on FP32 parameters; f32x2: double-float RHS (pairs of floats on the FP32 "
+                        "pipe) on FP64 parameters; f64_1ulp / f64_f32params: FP64 solves with the parameters "
+                        "perturbed by one ulp / rounded to FP32 (the sensitivity floor); state, error norm and "
+                        "step control are FP64 in every run",
                 "details": ens}
             torch.cuda.empty_cache()
         if not args.no_warmstart:

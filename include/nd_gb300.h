@@ -42,8 +42,10 @@ enum nd_status {
 };
 
 /* Element type of caller buffers.  A handle is built for one of them, like
- * adapt(CuArray{Float32}/CuArray{Float64}, nw) (ext/NetworkDynamicsCUDAExt.jl:16-45). */
-enum nd_dtype { ND_F32 = 1, ND_F64 = 2 };
+ * adapt(CuArray{Float32}/CuArray{Float64}, nw) (ext/NetworkDynamicsCUDAExt.jl:16-45).
+ * ND_F32X2 (ensembles only; no counterpart in the reference): FP64 buffers, RHS arithmetic
+ * in double-float (pairs of floats, ~48-bit significands) on the FP32 pipe. */
+enum nd_dtype { ND_F32 = 1, ND_F64 = 2, ND_F32X2 = 3 };
 
 /* Hand-written component library.  Anything else is rejected with
  * ND_ERR_UNSUPPORTED_COMPONENT: there is no CPU fallback. */

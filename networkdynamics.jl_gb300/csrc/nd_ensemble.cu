@@ -16,9 +16,11 @@
 #include <cmath>
 #include <cstring>
 #include <numeric>
+#include <type_traits>
 #include <vector>
 
 #include "nd_components.cuh"
+#include "nd_df.cuh"
 #include "nd_internal.h"
 
 struct nd_ensemble {
@@ -84,6 +86,18 @@ struct EnsArgs {
     const int32_t* nbr;
     const int32_t* eid;
     int* counter;
+};
+
+// Tag of the double-float RHS (ND_F32X2): FP64 state and parameters, arithmetic in pairs
+// of floats on the FP32 pipe (nd_df.cuh).
+struct F32x2 {};
+template <typename T>
+struct Elem {
+    using type = T;  // element type of p and of the RHS's caller buffers
+};
+template <>
+struct Elem<F32x2> {
+    using type = double;
 };
 
 // Instance views.
@@ -162,11 +176,61 @@ __device__ void instance_rhs(const EnsArgs& a, const Inst& s, const TU* __restri
     }
 }
 
+// The same RHS in double-float: each incidence's phase difference is taken in FP64 (one
+// subtraction, exact up to the state's rounding) and split into floats; the sine, the
+// products, the row sum and the vertex function run in double-float; du is rounded to FP64.
+// Errors stay near 1e-14 relative where the FP32 RHS has ~1e-7.
+template <int VK, int EK>
+__device__ void instance_rhs_df(const EnsArgs& a, const Inst& s, const double* __restrict__ y,
+                                const double* __restrict__ p, double* __restrict__ du_d) {
+    using namespace df;
+    constexpr int DV = VertexDims<VK>::dim;
+    const double* pv = p + s.pbase;
+    const double* pe = pv + s.nvi * VertexDims<VK>::pdim;
+    const double* yi = y + s.ubase;
+    for (int64_t v = threadIdx.x; v < s.nvi; v += blockDim.x) {
+        const uint32_t beg = a.row_ptr[s.vbase + v], end = a.row_ptr[s.vbase + v + 1];
+        const double uvd = yi[v * DV];
+        Df acc{0.f, 0.f};
+        for (uint32_t k = beg; k < end; ++k) {
+            const int32_t nb = a.nbr[k], e = a.eid[k] & 0x7fffffff;
+            const double dd = __dsub_rn(yi[(int64_t)nb * DV], uvd);
+            Df term;
+            if constexpr (EK == ND_E_DIFFUSION) term = mul(from_double(pe[e]), from_double(dd));
+            else if constexpr (EK == ND_E_DIFFUSION_UNIT) term = from_double(dd);
+            else term = mul(from_double(pe[e]), df::sin(from_double3(dd)));
+            acc = add(acc, term);
+        }
+        double* out = du_d + s.ubase + v * DV;
+        if constexpr (VK == ND_V_DIFFUSION) {
+            out[0] = to_double(acc);
+        } else if constexpr (VK == ND_V_KURAMOTO) {
+            out[0] = to_double(add(from_double(pv[v]), acc));
+        } else {
+            // dv[2] = 1 / M * (Pm - D * v[2] + acc)
+            const double w = yi[v * DV + 1];
+            const Df inv = df::div(Df{1.f, 0.f}, from_double(pv[3 * v]));
+            const Df t = add(sub(from_double(pv[3 * v + 2]), mul(from_double(pv[3 * v + 1]), from_double(w))), acc);
+            out[0] = w;
+            out[1] = to_double(mul(inv, t));
+        }
+    }
+}
+
 template <typename T, int VK, int EK>
-__global__ void ens_rhs_kernel(EnsArgs a, const T* __restrict__ u, const T* __restrict__ p, T* __restrict__ du) {
+__device__ __forceinline__ void any_instance_rhs(const EnsArgs& a, const Inst& s, const double* __restrict__ y,
+                                                 const typename Elem<T>::type* __restrict__ p, double* __restrict__ du) {
+    if constexpr (std::is_same<T, F32x2>::value) instance_rhs_df<VK, EK>(a, s, y, p, du);
+    else instance_rhs<T, VK, EK, double>(a, s, y, p, du, nullptr);
+}
+
+template <typename T, int VK, int EK>
+__global__ void ens_rhs_kernel(EnsArgs a, const typename Elem<T>::type* __restrict__ u,
+                               const typename Elem<T>::type* __restrict__ p, typename Elem<T>::type* __restrict__ du) {
     for (int64_t i = blockIdx.x; i < a.n_inst; i += gridDim.x) {
         const Inst s = instance<VK, EK>(a, i);
-        instance_rhs<T, VK, EK, T>(a, s, u, p, nullptr, du);
+        if constexpr (std::is_same<T, F32x2>::value) instance_rhs_df<VK, EK>(a, s, u, p, du);
+        else instance_rhs<T, VK, EK, T>(a, s, u, p, nullptr, du);
     }
 }
 
@@ -197,7 +261,8 @@ struct SolveParams {
 };
 
 template <typename T, int VK, int EK>
-__global__ void ens_tsit5_kernel(EnsArgs a, SolveParams sp, double* __restrict__ U, const T* __restrict__ p,
+__global__ void ens_tsit5_kernel(EnsArgs a, SolveParams sp, double* __restrict__ U,
+                                 const typename Elem<T>::type* __restrict__ p,
                                  double* __restrict__ work, int32_t* __restrict__ status, int64_t* __restrict__ nsteps) {
     __shared__ double red[32];
     __shared__ int sh_inst;
@@ -216,7 +281,7 @@ __global__ void ens_tsit5_kernel(EnsArgs a, SolveParams sp, double* __restrict__
         const int64_t n = s.nvi * VertexDims<VK>::dim;
         double* u = U + s.ubase;
         // k0 = f(u); initial step (Hairer & Wanner)
-        instance_rhs<T, VK, EK, double>(a, s, U, p, K[0], nullptr);
+        any_instance_rhs<T, VK, EK>(a, s, U, p, K[0]);
         __syncthreads();
         double d0 = 0, d1 = 0;
         for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
@@ -231,7 +296,7 @@ __global__ void ens_tsit5_kernel(EnsArgs a, SolveParams sp, double* __restrict__
         h0 = fmin(h0, sp.t1 - sp.t0);
         for (int64_t j = threadIdx.x; j < n; j += blockDim.x) Y[s.ubase + j] = u[j] + h0 * K[0][s.ubase + j];
         __syncthreads();
-        instance_rhs<T, VK, EK, double>(a, s, Y, p, K[1], nullptr);
+        any_instance_rhs<T, VK, EK>(a, s, Y, p, K[1]);
         __syncthreads();
         double d2 = 0;
         for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
@@ -260,7 +325,7 @@ __global__ void ens_tsit5_kernel(EnsArgs a, SolveParams sp, double* __restrict__
                     Y[s.ubase + j] = __dadd_rn(u[j], __dmul_rn(h, acc));
                 }
                 __syncthreads();
-                instance_rhs<T, VK, EK, double>(a, s, Y, p, K[st], nullptr);
+                any_instance_rhs<T, VK, EK>(a, s, Y, p, K[st]);
                 __syncthreads();
             }
             double se = 0.0;
@@ -473,8 +538,9 @@ cudaError_t launch_ens_rhs(const nd_ensemble* e, const EnsArgs& a, const void* u
     const unsigned grid = (unsigned)std::min<int64_t>(e->n_inst, 152 * 16);
 #define ND_CASE(VK, EK)                                                                                       \
     if (e->vertex_kind == VK && e->edge_kind == EK) {                                                          \
-        ens_rhs_kernel<T, VK, EK><<<grid, 128, 0, s>>>(a, static_cast<const T*>(u), static_cast<const T*>(p),   \
-                                                       static_cast<T*>(du));                                    \
+        using E = typename Elem<T>::type;                                                                       \
+        ens_rhs_kernel<T, VK, EK><<<grid, 128, 0, s>>>(a, static_cast<const E*>(u), static_cast<const E*>(p),   \
+                                                       static_cast<E*>(du));                                    \
         return cudaGetLastError();                                                                             \
     }
     ND_CASE(ND_V_DIFFUSION, ND_E_DIFFUSION)
@@ -495,7 +561,8 @@ cudaError_t launch_ens_tsit5(const nd_ensemble* e, const EnsArgs& a, const Solve
                              int32_t* status, int64_t* nsteps, int threads, int blocks, cudaStream_t s) {
 #define ND_CASE(VK, EK)                                                                                       \
     if (e->vertex_kind == VK && e->edge_kind == EK) {                                                          \
-        ens_tsit5_kernel<T, VK, EK><<<blocks, threads, 0, s>>>(a, sp, u, static_cast<const T*>(p), e->work,    \
+        ens_tsit5_kernel<T, VK, EK><<<blocks, threads, 0, s>>>(a, sp, u,                                       \
+                                                               static_cast<const typename Elem<T>::type*>(p), e->work, \
                                                                status, nsteps);                                \
         return cudaGetLastError();                                                                             \
     }
@@ -558,7 +625,8 @@ int nd_ensemble_create(const nd_ensemble_desc* d, int dtype, nd_ensemble** out) 
     clear_error();
     if (!d || !out) return fail(ND_ERR_ARG, "nd_ensemble_create: NULL argument");
     *out = nullptr;
-    if (dtype != ND_F32 && dtype != ND_F64) return fail(ND_ERR_DTYPE, "nd_ensemble_create: dtype must be ND_F32 or ND_F64");
+    if (dtype != ND_F32 && dtype != ND_F64 && dtype != ND_F32X2)
+        return fail(ND_ERR_DTYPE, "nd_ensemble_create: dtype must be ND_F32, ND_F64 or ND_F32X2");
     if (d->vertex_kind < ND_V_DIFFUSION || d->vertex_kind > ND_V_SWING || d->edge_kind < ND_E_DIFFUSION ||
         d->edge_kind > ND_E_KURAMOTO || d->coupling != ND_ANTISYMMETRIC)
         return fail(ND_ERR_UNSUPPORTED_COMPONENT, "nd_ensemble_create: component not in the GB300 library");
@@ -655,8 +723,9 @@ int nd_ensemble_rhs(nd_ensemble* e, int dtype, void* du, const void* u, const vo
     if (dtype != e->dtype) return fail(ND_ERR_DTYPE, "nd_ensemble_rhs: element type differs from the ensemble's");
     if (e->pdim > 0 && !p) return fail(ND_ERR_ARG, "nd_ensemble_rhs: p is NULL");
     const EnsArgs a = args_of(e);
-    cudaError_t err = e->dtype == ND_F64 ? launch_ens_rhs<double>(e, a, u, p, du, (cudaStream_t)stream)
-                                         : launch_ens_rhs<float>(e, a, u, p, du, (cudaStream_t)stream);
+    cudaError_t err = e->dtype == ND_F64   ? launch_ens_rhs<double>(e, a, u, p, du, (cudaStream_t)stream)
+                      : e->dtype == ND_F32 ? launch_ens_rhs<float>(e, a, u, p, du, (cudaStream_t)stream)
+                                           : launch_ens_rhs<F32x2>(e, a, u, p, du, (cudaStream_t)stream);
     return err == cudaSuccess ? ND_OK : cuda_fail(err, "nd_ensemble_rhs");
 }
 
@@ -674,11 +743,12 @@ int nd_ensemble_solve_tsit5(nd_ensemble* e, double* u, const void* p, double t0,
     if (err != cudaSuccess) return cuda_fail(err, "tableau upload");
     if ((err = ensure_work(e, sizeof(double) * 8 * (size_t)e->dim)) != cudaSuccess) return cuda_fail(err, "workspace");
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm,
-                                                  e->dtype == ND_F64
-                                                      ? (const void*)ens_tsit5_kernel<double, ND_V_SWING, ND_E_KURAMOTO>
-                                                      : (const void*)ens_tsit5_kernel<float, ND_V_SWING, ND_E_KURAMOTO>,
-                                                  threads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm,
+        e->dtype == ND_F64   ? (const void*)ens_tsit5_kernel<double, ND_V_SWING, ND_E_KURAMOTO>
+        : e->dtype == ND_F32 ? (const void*)ens_tsit5_kernel<float, ND_V_SWING, ND_E_KURAMOTO>
+                             : (const void*)ens_tsit5_kernel<F32x2, ND_V_SWING, ND_E_KURAMOTO>,
+        threads, 0);
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device);
     const int blocks = (int)std::min<int64_t>(e->n_inst, (int64_t)sms * std::max(1, per_sm));
@@ -695,8 +765,9 @@ int nd_ensemble_solve_tsit5(nd_ensemble* e, double* u, const void* p, double t0,
     err = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (err == cudaSuccess) {
         cudaMemsetAsync(e->counter, 0, sizeof(int), cs);
-        err = e->dtype == ND_F64 ? launch_ens_tsit5<double>(e, a, sp, u, p, status, nsteps, threads, blocks, cs)
-                                 : launch_ens_tsit5<float>(e, a, sp, u, p, status, nsteps, threads, blocks, cs);
+        err = e->dtype == ND_F64   ? launch_ens_tsit5<double>(e, a, sp, u, p, status, nsteps, threads, blocks, cs)
+              : e->dtype == ND_F32 ? launch_ens_tsit5<float>(e, a, sp, u, p, status, nsteps, threads, blocks, cs)
+                                   : launch_ens_tsit5<F32x2>(e, a, sp, u, p, status, nsteps, threads, blocks, cs);
         cudaError_t e2 = cudaStreamEndCapture(cs, &g);
         if (err == cudaSuccess) err = e2;
     }

@@ -22,6 +22,7 @@ ND_ERR_NOT_CONVERGED = -8
 
 ND_F32 = 1
 ND_F64 = 2
+ND_F32X2 = 3  # ensembles: FP64 buffers, double-float RHS arithmetic on the FP32 pipe
 
 ND_V_DIFFUSION = 1
 ND_V_KURAMOTO = 2

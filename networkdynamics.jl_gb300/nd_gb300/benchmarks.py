@@ -126,9 +126,15 @@ def ensemble(n=4096, nv_lo=50, nv_hi=5000, t_end=50.0, reltol=1e-6, abstol=1e-6,
            "instances_redrawn": int((draw > 0).sum()), "instances_with_scaled_injections": int((scale < 1).sum()),
            "injection_scale_min": float(scale.min())}
     finals = {}
-    for name, dt in (("f64", torch.float64), ("f32", torch.float32)):
+    # f64: the FP64 RHS; f32: FP32 RHS on FP32-rounded parameters; f32x2: double-float RHS
+    # on the FP32 pipe with FP64 parameters.  Two more FP64 solves measure the floor that
+    # separates precision from sensitivity: parameters perturbed by one relative ulp
+    # (f64_1ulp), and rounded to FP32 (f64_f32params).
+    one_ulp = p64 * (1.0 + 2.0 ** -52)
+    runs = (("f64", torch.float64, p64), ("f32", torch.float32, p64.float()), ("f32x2", "f32x2", p64),
+            ("f64_1ulp", torch.float64, one_ulp), ("f64_f32params", torch.float64, p64.float().double()))
+    for name, dt, p in runs:
         ens = e64 if dt == torch.float64 else Ensemble(graphs, nd.kuramoto_second(), nd.static_line(), dt)
-        p = p64 if dt == torch.float64 else p64.float()
         threads = ens.autotune(u0, p, 0.0, 0.5, reltol, abstol)
         _log(f"{name}: autotuned {threads} threads per instance")
         ens.solve_tsit5(u0, p, (0.0, 0.5), reltol, abstol)  # warm-up (graph capture)
@@ -142,23 +148,31 @@ def ensemble(n=4096, nv_lo=50, nv_hi=5000, t_end=50.0, reltol=1e-6, abstol=1e-6,
         st = r.status.cpu().numpy()
         out[name] = {"seconds": el, "solves_per_s": n / el, "threads_per_instance": threads,
                      "steps_mean": float(r.nsteps.double().mean().item()), "ok": int((st == 0).sum())}
-    err = np.abs(finals["f32"] - finals["f64"])
-    per_inst = np.maximum.reduceat(err, e64.u_offset[:-1].astype(np.int64))
     # synchronised / desynchronised verdict per instance: max |ω| at T below 0.1
     verdict = {}
-    for name in ("f64", "f32"):
+    for name in finals:
         w = np.abs(finals[name][1::2])
         per = np.maximum.reduceat(w, (e64.u_offset[:-1] // 2).astype(np.int64))
         verdict[name] = per < 0.1
     out["sync_fraction_f64"] = float(verdict["f64"].mean())
-    out["sync_verdict_agreement_f32_vs_f64"] = float((verdict["f64"] == verdict["f32"]).mean())
     sync = verdict["f64"]
-    out["f32_final_state_err_vs_f64"] = {
-        "max": float(err.max()), "median_instance": float(np.median(per_inst)),
-        "instances_within_1e-6": int((per_inst <= 1e-6).sum()),
-        "synchronised_max": float(per_inst[sync].max()) if sync.any() else None,
-        "synchronised_median": float(np.median(per_inst[sync])) if sync.any() else None,
-        "desynchronised_median": float(np.median(per_inst[~sync])) if (~sync).any() else None}
+
+    def err_stats(name):
+        err = np.abs(finals[name] - finals["f64"])
+        per_inst = np.maximum.reduceat(err, e64.u_offset[:-1].astype(np.int64))
+        q = lambda m, x: float(np.percentile(per_inst[m], x)) if m.any() else None  # noqa: E731
+        return {"max": float(err.max()), "median_instance": float(np.median(per_inst)),
+                "instances_within_1e-6": int((per_inst <= 1e-6).sum()),
+                "synchronised_median": q(sync, 50), "synchronised_p95": q(sync, 95),
+                "synchronised_max": float(per_inst[sync].max()) if sync.any() else None,
+                "synchronised_within_1e-6": int((per_inst[sync] <= 1e-6).sum()),
+                "desynchronised_median": q(~sync, 50),
+                "sync_verdict_agreement": float((verdict[name] == verdict["f64"]).mean())}
+
+    for name in finals:
+        if name != "f64":
+            out[f"{name}_final_state_err_vs_f64"] = err_stats(name)
+    out["sync_verdict_agreement_f32_vs_f64"] = out["f32_final_state_err_vs_f64"]["sync_verdict_agreement"]
     # the plain per-instance FP64 GPU solve on a sample of the instances
     idx = rng.choice(n, size=min(baseline_sample, n), replace=False)
     t_plain = 0.0
@@ -177,15 +191,16 @@ def ensemble(n=4096, nv_lo=50, nv_hi=5000, t_end=50.0, reltol=1e-6, abstol=1e-6,
         ref = uT.cpu().numpy()
         sl = e64.u_slice(i)
         d64.append(float(np.abs(finals["f64"][sl] - ref).max()))
-        d32.append(float(np.abs(finals["f32"][sl] - ref).max()))
+        d32.append(float(np.abs(finals["f32x2"][sl] - ref).max()))
     plain = len(idx) / t_plain
     _log(f"plain per-instance FP64: {len(idx)} solves in {t_plain:.2f} s")
     out["plain_f64_per_instance"] = {
         "solves_per_s": plain, "sample": int(len(idx)),
         "note": "solve_tsit5 of one Network at a time, sampled instances",
         "final_state_diff_batched_f64_vs_plain": {"median": float(np.median(d64)), "max": float(np.max(d64))},
-        "final_state_diff_batched_f32_vs_plain": {"median": float(np.median(d32)), "max": float(np.max(d32))}}
+        "final_state_diff_batched_f32x2_vs_plain": {"median": float(np.median(d32)), "max": float(np.max(d32))}}
     out["f32_batched_vs_plain_f64"] = out["f32"]["solves_per_s"] / plain
+    out["f32x2_batched_vs_plain_f64"] = out["f32x2"]["solves_per_s"] / plain
     out["f64_batched_vs_plain_f64"] = out["f64"]["solves_per_s"] / plain
     return out
 

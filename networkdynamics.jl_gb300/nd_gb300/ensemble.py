@@ -13,7 +13,15 @@ import numpy as np
 
 from . import _capi as capi
 from .components import EdgeModel, VertexModel
-from .network import _dtype_code
+from .network import _dtype_code as _network_dtype_code
+
+
+def _dtype_code(dtype) -> int:
+    """torch.float64 / torch.float32 as for networks, or "f32x2": FP64 buffers with the
+    RHS computed in double-float on the FP32 pipe (ensembles only)."""
+    if isinstance(dtype, str) and dtype.lower() in ("f32x2", "float32x2", "double-float"):
+        return capi.ND_F32X2
+    return _network_dtype_code(dtype)
 
 
 @dataclass
@@ -56,7 +64,8 @@ class Ensemble:
         capi.check(self._lib.nd_ensemble_create(C.byref(desc), _dtype_code(dtype), C.byref(h)))
         self._h = h
         self.dtype_code = _dtype_code(dtype)
-        self.torch_dtype = torch.float64 if self.dtype_code == capi.ND_F64 else torch.float32
+        # element type of p and of the RHS buffers (the state is FP64 in every precision)
+        self.torch_dtype = torch.float32 if self.dtype_code == capi.ND_F32 else torch.float64
         dim, pdim = C.c_int64(), C.c_int64()
         capi.check(self._lib.nd_ensemble_get_info(h, C.byref(dim), C.byref(pdim)))
         self.dim, self.pdim = dim.value, pdim.value

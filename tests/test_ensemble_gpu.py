@@ -170,3 +170,63 @@ def test_find_fixpoint_known_answer_and_errors(cuda):
         nd.find_fixpoint(net, p_bad, max_newton=20)
     with pytest.raises(nd.ArgumentError):  # the swing solver takes swing networks only
         nd.find_fixpoint(nd.Network(g4, nd.kuramoto_first(), nd.kuramoto_edge()), np.zeros(8), alg="swing")
+
+
+@pytest.mark.parametrize("vm,em,vk,ek", [
+    (nd.kuramoto_second, nd.static_line, O.V_SWING, O.E_KURAMOTO),
+    (nd.kuramoto_first, nd.kuramoto_edge, O.V_KURAMOTO, O.E_KURAMOTO),
+    (nd.diffusion_vertex, nd.diffusion_edge, O.V_DIFFUSION, O.E_DIFFUSION),
+])
+def test_double_float_rhs_accuracy(cuda, vm, em, vk, ek):
+    """The double-float RHS (ND_F32X2: FP64 buffers, arithmetic in float pairs on the FP32
+    pipe) against the oracle's FP64 RHS, phases wound up to |θ| ~ 1e3 included: every
+    entry within 1e-13 (Σ|terms| + |du| + 1), where the FP32 RHS is ~1e-7 off."""
+    import torch
+    rng = np.random.default_rng(7)
+    gs = make_graphs(rng, 8, 50, 600)
+    ens = Ensemble(gs, vm(), em(), "f32x2")
+    us, ps, refs, scales = [], [], [], []
+    for i, g in enumerate(gs):
+        on = O.OracleNetwork.from_graph(g, vk, ek)
+        u = rng.normal(size=on.dim)
+        if vk == O.V_SWING:
+            u[0::2] = rng.uniform(-1e3, 1e3, g.nv) if i % 2 else rng.uniform(-np.pi, np.pi, g.nv)
+            p = swing_params(g, rng)
+        else:
+            p = rng.uniform(0.5, 1.5, size=on.pdim)
+        us.append(u)
+        ps.append(p)
+        refs.append(on.rhs(u, p))
+        scales.append(on.abs_terms(u, p))
+    u = torch.from_numpy(np.concatenate(us)).to(cuda)
+    p = torch.from_numpy(np.concatenate(ps)).to(cuda)
+    du = torch.empty_like(u)
+    ens.rhs(du, u, p)
+    got = du.cpu().numpy()
+    ref, sc = np.concatenate(refs), np.concatenate(scales)
+    d = np.abs(got - ref)
+    assert np.all(d <= 1e-13 * (sc + np.abs(ref) + 1.0)), d.max()
+
+
+def test_double_float_ensemble_solve_tracks_fp64(cuda):
+    """Tsit5 with the double-float RHS follows the FP64 ensemble's steps and final states
+    from perturbed steady states (contracting dynamics) to far below 1e-6."""
+    import torch
+    rng = np.random.default_rng(8)
+    gs = make_graphs(rng, 16, 30, 400)
+    p = torch.from_numpy(np.concatenate([swing_params(g, rng) for g in gs])).to(cuda)
+    e64 = Ensemble(gs, nd.kuramoto_second(), nd.static_line(), torch.float64)
+    fx = e64.fixpoint(torch.zeros(e64.dim, dtype=torch.float64, device=cuda), p, tol=1e-11)
+    ok = fx.status.cpu().numpy() == 0
+    assert ok.sum() >= 8
+    u0 = fx.u.clone()
+    u0[0::2] += torch.from_numpy(0.2 * rng.normal(size=e64.dim // 2)).to(cuda)
+    r64 = e64.solve_tsit5(u0, p, (0.0, 20.0), reltol=1e-6, abstol=1e-6)
+    edf = Ensemble(gs, nd.kuramoto_second(), nd.static_line(), "f32x2")
+    rdf = edf.solve_tsit5(u0, p, (0.0, 20.0), reltol=1e-6, abstol=1e-6)
+    a, b = r64.u.cpu().numpy(), rdf.u.cpu().numpy()
+    for i in np.nonzero(ok)[0]:  # instances with a steady state (the others start nowhere near one)
+        assert int(rdf.status[i]) == 0 and int(r64.status[i]) == 0
+        sl = e64.u_slice(i)
+        assert abs(int(r64.nsteps[i]) - int(rdf.nsteps[i])) <= 2
+        assert np.max(np.abs(a[sl] - b[sl])) <= 1e-9
