@@ -50,6 +50,13 @@ struct Arith<float> {
     static __device__ __forceinline__ float cos_phase(float x) { return cosf(wrap(x)); }
 };
 
+// Read-only load of a component parameter (a plain read for value types that are not
+// float / double, such as the dual numbers of nd_dual.cuh).
+template <typename T>
+__device__ __forceinline__ T ldv(const T* p) {
+    return __ldg(p);
+}
+
 // y_dst of the single-sided edge function g(vs, vd, p) for edge e.
 template <typename T, int EK>
 __device__ __forceinline__ T edge_g(T vs, T vd, const T* __restrict__ pe, int32_t e) {
@@ -231,14 +238,14 @@ __device__ __forceinline__ void vertex_f2_at(T* __restrict__ du, const T* __rest
                                              int64_t s, int64_t q, Cx<T> in) {
     using A = Arith<T>;
     if constexpr (VK == ND_V_PQ) {
-        const Cx<T> uc = cdiv<T>({__ldg(p + q), __ldg(p + q + 1)}, {in.r, -in.i});
+        const Cx<T> uc = cdiv<T>({ldv(p + q), ldv(p + q + 1)}, {in.r, -in.i});
         du[s] = uc.r;
         du[s + 1] = uc.i;
     } else {
-        const T H = __ldg(p + q), P = __ldg(p + q + 1), D = __ldg(p + q + 2), Om = __ldg(p + q + 3);
-        const T E_f = __ldg(p + q + 4), T_d_dash = __ldg(p + q + 5), T_q_dash = __ldg(p + q + 6);
-        const T X_q_dash = __ldg(p + q + 7), X_d_dash = __ldg(p + q + 8), X_d = __ldg(p + q + 9);
-        const T X_q = __ldg(p + q + 10);
+        const T H = ldv(p + q), P = ldv(p + q + 1), D = ldv(p + q + 2), Om = ldv(p + q + 3);
+        const T E_f = ldv(p + q + 4), T_d_dash = ldv(p + q + 5), T_q_dash = ldv(p + q + 6);
+        const T X_q_dash = ldv(p + q + 7), X_d_dash = ldv(p + q + 8), X_d = ldv(p + q + 9);
+        const T X_q = ldv(p + q + 10);
         const T Om_H = A::div(Om, A::mul(T(2), H));
         const Cx<T> uc = {u[s], u[s + 1]};
         const T th = u[s + 2], w = u[s + 3];

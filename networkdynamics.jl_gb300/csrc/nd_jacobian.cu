@@ -14,6 +14,10 @@
 // Columns are sorted and unique per row; a structural entry can be numerically zero (a
 // self loop, whose two derivatives cancel), as in a traced pattern.
 //
+// Power grids (complex outputs): a vertex's rows have its own states (generators) and the
+// voltage states of both endpoints of every incident line; the values come from dual
+// numbers carried through the component functions (jac_powergrid_kernel).
+//
 // Values: one thread per vertex row of up to 32 terms adds its terms' derivatives into its
 // row (found by binary search in the sorted columns), in the order of its terms; longer
 // rows take a warp each; one thread per ODE edge writes that edge's two rows.  For simple
@@ -24,6 +28,7 @@
 #include <vector>
 
 #include "nd_components.cuh"
+#include "nd_dual.cuh"
 #include "nd_internal.h"
 
 namespace nd {
@@ -251,6 +256,107 @@ __global__ void __launch_bounds__(kJacBlock) jac_ode_edge_kernel(JacArgs<T> a) {
     }
 }
 
+// ---- networks with complex outputs (power grids: PQ buses, generators, π-lines) ----------
+// A vertex thread differentiates its component with dual numbers: the generator with
+// respect to its four states and the two components of the aggregated current, the PQ bus
+// with respect to the current (its output does not depend on its own states).  Each
+// incident π-line side is differentiated with respect to the two endpoint voltages (four
+// partials); the chain rule ∂f/∂i · ∂i/∂V gives the voltage columns.
+template <typename T, int N>
+__device__ __forceinline__ Cx<Dual<T, N>> cx_seed(T re, T im, int k) {
+    return {Dual<T, N>::seed(re, k), Dual<T, N>::seed(im, k + 1)};
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kJacBlock) jac_powergrid_kernel(JacArgs<T> a) {
+    using A = Arith<T>;
+    using D4 = Dual<T, 4>;
+    using D6 = Dual<T, 6>;
+    const int64_t slot = (int64_t)blockIdx.x * kJacBlock + threadIdx.x;
+    if (slot >= a.nv) return;
+    const int64_t pos = __ldg(a.slot_vpos + slot);
+    const int b = find_batch(a.vb, pos);
+    const int vk = __ldg(a.vb.kind + b);
+    const int64_t r = pos - __ldg(a.vb.pos0 + b);
+    const int dim = vk == ND_V_GENERATOR ? 4 : 2;
+    const int pd = vk == ND_V_GENERATOR ? 11 : (vk == ND_V_PQ ? 2 : 0);
+    const int64_t s = __ldg(a.vb.s0 + b) + dim * r, q = __ldg(a.vb.p0 + b) + pd * r;
+    const uint32_t t0 = __ldg(a.tptr + slot), t1 = __ldg(a.tptr + slot + 1);
+    // the output of line side j at this vertex and its derivatives by (Vs_r, Vs_i, Vd_r, Vd_i)
+    auto side = [&](uint32_t j, int2& o, Cx<D4>& y) {
+        const int32_t t = __ldg(a.tidx + j);
+        const int64_t k = t >> 1;
+        const int eb = find_batch(a.eb, k);
+        const int64_t pe = __ldg(a.eb.p0 + eb) + 4 * (k - __ldg(a.eb.pos0 + eb));
+        o = __ldg(a.eu + k);
+        const Cx<D4> vs = cx_seed<T, 4>(__ldg(a.u + o.x), __ldg(a.u + o.x + 1), 0);
+        const Cx<D4> vd = cx_seed<T, 4>(__ldg(a.u + o.y), __ldg(a.u + o.y + 1), 2);
+        Cx<D4> ys, yd;
+        piline_g<D4>(vs, vd, D4(__ldg(a.p + pe)), D4(__ldg(a.p + pe + 1)), D4(__ldg(a.p + pe + 2)),
+                     D4(__ldg(a.p + pe + 3)), ys, yd);
+        y = (t & 1) ? yd : ys;
+    };
+    // the aggregated current (any order: only its value enters the derivatives)
+    T ir = T(0), ii = T(0);
+    for (uint32_t j = t0; j < t1; ++j) {
+        int2 o;
+        Cx<D4> y;
+        side(j, o, y);
+        ir = A::add(ir, y.r.v);
+        ii = A::add(ii, y.i.v);
+    }
+    // ∂f/∂(states) and ∂f/∂(current) for the rows f = 0..dim-1
+    T dfs[4][4] = {}, dfi[4][2] = {};
+    if (vk == ND_V_GENERATOR) {
+        D6 uu[4], pp[11], out[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) uu[c] = D6::seed(__ldg(a.u + s + c), c);
+#pragma unroll
+        for (int c = 0; c < 11; ++c) pp[c] = D6(__ldg(a.p + q + c));
+        vertex_f2_at<D6, ND_V_GENERATOR>(out, uu, pp, 0, 0, cx_seed<T, 6>(ir, ii, 4));
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) dfs[f][c] = out[f].d[c];
+            dfi[f][0] = out[f].d[4];
+            dfi[f][1] = out[f].d[5];
+        }
+    } else {
+        using D2 = Dual<T, 2>;
+        const Cx<D2> in = cx_seed<T, 2>(ir, ii, 0);
+        Cx<D2> uc;
+        if (vk == ND_V_PQ) {
+            uc = cdiv<D2>({D2(__ldg(a.p + q)), D2(__ldg(a.p + q + 1))}, {in.r, -in.i});
+        } else {  // ND_V_PQ_CONST: P, Q are the batch's constants
+            uc = cdiv<D2>({D2((T)__ldg(a.vb.consts + kBatchConstants * b)),
+                           D2((T)__ldg(a.vb.consts + kBatchConstants * b + 1))},
+                          {in.r, -in.i});
+        }
+        dfi[0][0] = uc.r.d[0];
+        dfi[0][1] = uc.r.d[1];
+        dfi[1][0] = uc.i.d[0];
+        dfi[1][1] = uc.i.d[1];
+    }
+    for (int f = 0; f < dim; ++f) {
+        const int32_t r0 = __ldg(a.rowptr + s + f);
+        const int n = __ldg(a.rowptr + s + f + 1) - r0;
+        T* vals = a.values + r0;
+        const int32_t* cols = a.colidx + r0;
+        if (vk == ND_V_GENERATOR)
+            for (int c = 0; c < 4; ++c) jadd<T>(vals, cols, n, (int32_t)(s + c), dfs[f][c]);
+        for (uint32_t j = t0; j < t1; ++j) {
+            int2 o;
+            Cx<D4> y;
+            side(j, o, y);
+#pragma unroll
+            for (int x = 0; x < 4; ++x) {
+                const T v = A::add(A::mul(dfi[f][0], y.r.d[x]), A::mul(dfi[f][1], y.i.d[x]));
+                jadd<T>(vals, cols, n, (x < 2 ? o.x : o.y) + (x & 1), v);
+            }
+        }
+    }
+}
+
 // The batched view of a homogeneous handle: its edge list recovered from the device CSR
 // (every edge appears once on its source side), one vertex and one edge batch.
 int build_view(nd_handle* h, BatchedNet* view) {
@@ -300,9 +406,6 @@ int build_plan(nd_handle* h) {
         if (rc != ND_OK) return rc;
     }
     const BatchedNet& b = h->batched.enabled ? h->batched : J.view;
-    if (b.depth != 1)
-        return fail(ND_ERR_UNSUPPORTED, "nd_jacobian: networks with complex (two-dimensional) outputs, the "
-                                        "power-grid components, have no analytic Jacobian here");
     const int64_t nv = b.nv, ne = b.ne, dim = b.dim;
     std::vector<uint32_t> tptr(nv + 1);
     std::vector<int32_t> tidx((size_t)2 * ne), slot_vpos(nv);
@@ -316,7 +419,27 @@ int build_plan(nd_handle* h) {
                     (err = cudaMemcpy(eu.data(), b.eu, eu.size() * sizeof(int2), cudaMemcpyDeviceToHost)) != cudaSuccess)))
         return cuda_fail(err, "nd_jacobian: structure download");
     std::vector<std::vector<int32_t>> rows(dim);
-    for (int64_t slot = 0; slot < nv; ++slot) {
+    // power grids: every state row of a vertex has its own states (generators) and both
+    // voltage states of both endpoints of each incident line side
+    for (int64_t slot = 0; b.depth == 2 && slot < nv; ++slot) {
+        const int64_t pos = slot_vpos[slot];
+        const int vbi = host_find_batch(b.vb, pos);
+        const int vk = b.vb.kind[vbi];
+        const int vdim = vertex_dim(vk);
+        const int64_t s = b.vb.s0[vbi] + vdim * (pos - b.vb.pos0[vbi]);
+        std::vector<int32_t> cols;
+        if (vk == ND_V_GENERATOR)
+            for (int c = 0; c < 4; ++c) cols.push_back((int32_t)(s + c));
+        for (uint32_t j = tptr[slot]; j < tptr[slot + 1]; ++j) {
+            const int2 o = eu[tidx[j] >> 1];
+            for (int c = 0; c < 2; ++c) {
+                cols.push_back(o.x + c);
+                cols.push_back(o.y + c);
+            }
+        }
+        for (int f = 0; f < vdim; ++f) rows[s + f] = cols;
+    }
+    for (int64_t slot = 0; b.depth == 1 && slot < nv; ++slot) {
         const int64_t pos = slot_vpos[slot];
         const int vbi = host_find_batch(b.vb, pos);
         const int vk = b.vb.kind[vbi];
@@ -340,7 +463,7 @@ int build_plan(nd_handle* h) {
             }
         }
     }
-    for (int64_t k = 0; k < ne; ++k) {
+    for (int64_t k = 0; b.depth == 1 && k < ne; ++k) {
         const int ebi = host_find_batch(b.eb, k);
         if (!is_ode(b.eb.kind[ebi])) continue;
         const int64_t es = b.eb.s0[ebi] + 2 * (k - b.eb.pos0[ebi]);
@@ -361,7 +484,7 @@ int build_plan(nd_handle* h) {
         J.rowptr_h[i + 1] = (int32_t)nnz;
     }
     std::vector<int32_t> long_slots;
-    for (int64_t slot = 0; slot < nv; ++slot)
+    for (int64_t slot = 0; b.depth == 1 && slot < nv; ++slot)
         if (tptr[slot + 1] - tptr[slot] > kJacLongRow) long_slots.push_back((int32_t)slot);
     J.n_long = (int64_t)long_slots.size();
     J.colidx_h.resize(nnz);
@@ -401,6 +524,10 @@ cudaError_t launch_values(nd_handle* h, void* values, const void* u, const void*
     a.slot_vpos = b.slot_vpos;
     cudaError_t err = cudaMemsetAsync(values, 0, std::max<int64_t>(J.nnz, 1) * sizeof(T), s);
     if (err != cudaSuccess) return err;
+    if (b.depth == 2) {
+        jac_powergrid_kernel<T><<<(unsigned)((b.nv + kJacBlock - 1) / kJacBlock), kJacBlock, 0, s>>>(a);
+        return cudaGetLastError();
+    }
     jac_vertex_kernel<T><<<(unsigned)((b.nv + kJacBlock - 1) / kJacBlock), kJacBlock, 0, s>>>(a);
     if (J.n_long > 0)
         jac_long_row_kernel<T><<<(unsigned)((J.n_long * 32 + kJacBlock - 1) / kJacBlock), kJacBlock, 0, s>>>(

@@ -1,6 +1,6 @@
 """Steady states of one network on the GPU: the counterpart of the reference's
 ``find_fixpoint(nw, x0, p)`` (src/initialization.jl:44-144).  Homogeneous swing networks
-use the batched swing Newton below; every other network of output dimension 1 uses
+use the batched swing Newton below; every other network of the library (power grids included) uses
 Newton-GMRES on the sparse Jacobian (nd_find_fixpoint).
 
 The swing solve is the batched Newton of ``Ensemble.fixpoint`` on an ensemble of one:
@@ -29,7 +29,7 @@ def find_fixpoint(nw, p, x0=None, tol=1e-10, max_newton=50, max_cg=0, alg=None, 
 
     alg: "swing" -- Newton-CG on the power balance of a homogeneous swing network at ω = 0
     (default for such networks); "newton_gmres" -- Newton with restarted GMRES on the sparse
-    Jacobian, for any network of the library whose outputs have dimension 1 (default for
+    Jacobian, for any network of the library (default for
     all others)."""
     import torch
     swing = nw.vertexm is not None and nw.edgem is not None and nw.vertexm.kind == capi.ND_V_SWING

@@ -328,17 +328,6 @@ def test_powergrid_parity(cuda, nv):
         check_f32_isapprox(got32, ref)
 
 
-def test_powergrid_has_no_jacobian(cuda):
-    import torch
-    g, net, _ = powergrid_network(50, 1)
-    nw = adapt(net, np.float64)
-    with pytest.raises(nd.ArgumentError):
-        nd.jacobian_pattern(nw)
-    u = torch.zeros(nw.dim, dtype=torch.float64, device=cuda)
-    with pytest.raises(nd.ArgumentError):
-        nd.jvp(nw, torch.empty_like(u), u, torch.ones(nw.pdim, dtype=torch.float64, device=cuda), u)
-
-
 def test_inhomogeneous_pq_parity(cuda):
     """powergrid_inhomogeneous_pq (benchmark/benchmark_cases.jl:82-102): half the buses are
     PQ buses closing over their own P, Q (one batch each, ~1500 batches), half generators."""

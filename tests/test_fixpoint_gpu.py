@@ -90,8 +90,7 @@ def test_batched_network_with_ode_edges(cuda):
 
 
 def test_failures_raise(cuda):
-    """No fixpoint (frequencies that do not sum to zero), NaN in the parameters, and the
-    power-grid networks (no Jacobian) raise."""
+    """No fixpoint (frequencies that do not sum to zero) and NaN in the parameters raise."""
     g = nd.cycle_graph(20)
     net = adapt(nd.Network(g, nd.kuramoto_first(), nd.kuramoto_edge()))
     p = np.concatenate([np.full(20, 0.3), np.full(20, 2.0)])
@@ -101,7 +100,3 @@ def test_failures_raise(cuda):
     p_nan[3] = np.nan
     with pytest.raises(nd.NotConvergedError, match="NaN"):
         nd.find_fixpoint(net, p_nan)
-    g4 = nd.cycle_graph(4)
-    pg = adapt(nd.Network(g4, nd.pqnode(), nd.piline()))
-    with pytest.raises(nd.ArgumentError):
-        nd.find_fixpoint(pg, np.ones(pg.pdim))
