@@ -299,6 +299,18 @@ typedef struct nd_solve_stats {
 int nd_solve_tsit5(nd_handle* h, double* u, const void* p, double t0, double t1, double reltol, double abstol,
                    int64_t max_steps, nd_solve_stats* stats, void* stream);
 
+/* Rosenbrock23 (Shampine & Reichelt 1997) for M u' = f(u) with a diagonal mass matrix:
+ * mass[dim] (device, FP64; NULL = identity), zero entries making states algebraic, as
+ * construct_mass_matrix builds it (src/construction.jl:409-467) for components with
+ * mass_matrix = 0 (the PQ bus, benchmark/benchmark_models.jl:66-74).  Each step uses the
+ * analytic sparse Jacobian (nd_jacobian) and solves its three linear systems with
+ * W = M - h d J by Jacobi-preconditioned GMRES.  u: FP64 device state, consistent for the
+ * algebraic rows (in: u0, out: u(t1)).  max_steps <= 0 means ND_ENSEMBLE_DEFAULT_MAX_STEPS.
+ * FP64 handles only.  Synchronous.  Replaces solve(ODEProblem(nw, u0, tspan, p),
+ * Rosenbrock23()) of SciML (src/post_utils.jl:43-100 builds that ODEFunction). */
+int nd_solve_rosenbrock23(nd_handle* h, double* u, const double* p, const double* mass, double t0, double t1,
+                          double reltol, double abstol, int64_t max_steps, nd_solve_stats* stats, void* stream);
+
 /* Allocation-free RHS.  This entry point has no counterpart in the reference.  It is for
  * callers that must not allocate device memory while they evaluate the RHS: a process
  * whose device memory belongs to a caching allocator (CUDA.jl's or PyTorch's pool), where a

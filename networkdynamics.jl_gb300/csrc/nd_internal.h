@@ -271,6 +271,23 @@ struct Tracer {
     void release();       // destroy every pooled event
 };
 
+// Restarted GMRES on a CSR matrix (nd_newton.cu), shared by the Newton fixpoint and the
+// Rosenbrock solver.  attach() lays its workspace out in `buf` (doubles(n, m) doubles).
+struct GmresSolver {
+    int64_t n = 0;
+    int m = 0;
+    cudaStream_t s = nullptr;
+    double *w = nullptr, *dinv = nullptr, *z = nullptr, *V = nullptr, *partial = nullptr, *dscal = nullptr;
+    static size_t doubles(int64_t n, int m);
+    void attach(double* buf, int64_t n, int m, cudaStream_t s);
+    void jacobi(const int32_t* rowptr, const int32_t* col, const double* vals);  // D^-1 from the diagonal
+    int solve(const int32_t* rowptr, const int32_t* col, const double* vals, const double* b, double* x, double rtol,
+              int restarts, double* rel_res);
+    int multidot(const double* V, int nv, const double* x, double* dots);
+    int sync(const char* what);
+};
+void vec_axpby(int64_t n, double a, const double* x, double b, double* y, cudaStream_t s);  // y = a x + b y
+
 cudaError_t launch_exact_selftest(const double* a, const double* b, double* out, int64_t n, cudaStream_t s);
 cudaError_t launch_scan_selftest(const double* terms, const int64_t* seg, const double* s0, double* out,
                                  int64_t nseg, cudaStream_t s);

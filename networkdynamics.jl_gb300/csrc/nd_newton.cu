@@ -1,4 +1,4 @@
-// Steady states of any network of the library (output dimension 1): Newton's method with
+// Steady states of any network of the library: Newton's method with
 // restarted GMRES on the assembled sparse Jacobian, the GPU counterpart of
 // find_fixpoint(nw, x0, p) (src/initialization.jl:44-144), which solves a
 // SteadyStateProblem with NonlinearSolve's Newton-type root finders.
@@ -153,6 +153,121 @@ struct Workspace {
 
 }  // namespace
 
+size_t GmresSolver::doubles(int64_t n, int m) { return (size_t)n * (3 + m + 1) + (size_t)kDotBlocks * (m + 1) + 2 * (kMaxKrylov + 2); }
+
+void GmresSolver::attach(double* buf, int64_t n_, int m_, cudaStream_t s_) {
+    n = n_;
+    m = std::max(2, std::min(m_, kMaxKrylov));
+    s = s_;
+    w = buf;
+    dinv = w + n;
+    z = dinv + n;
+    V = z + n;
+    partial = V + (size_t)n * (m + 1);
+    dscal = partial + (size_t)kDotBlocks * (m + 1);
+}
+
+int GmresSolver::sync(const char* what) {
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    return e == cudaSuccess ? ND_OK : cuda_fail(e, what);
+}
+
+int GmresSolver::multidot(const double* Vb, int nv, const double* x, double* dots) {
+    multidot_partial<<<kDotBlocks, kNB, 0, s>>>(n, nv, Vb, n, x, partial);
+    multidot_final<<<1, 64, 0, s>>>(kDotBlocks, nv, partial, dscal);
+    cudaMemcpyAsync(dots, dscal, nv * sizeof(double), cudaMemcpyDeviceToHost, s);
+    return sync("gmres: dot");
+}
+
+void GmresSolver::jacobi(const int32_t* rowptr, const int32_t* col, const double* vals) {
+    diag_inverse_kernel<<<grid_for(n), kNB, 0, s>>>(n, rowptr, col, vals, dinv);
+}
+
+// Restarted GMRES(m) for A x = b, x updated in place, right-preconditioned by the Jacobi
+// scaling set by jacobi(); Arnoldi by classical Gram-Schmidt applied twice, Givens
+// rotations on the host; stops at ||b - A x|| <= rtol ||b||.
+int GmresSolver::solve(const int32_t* rowptr, const int32_t* col, const double* vals, const double* b, double* x,
+                       double rtol, int restarts, double* rel_res) {
+    const unsigned G = grid_for(n);
+    const int64_t ldv = n;
+    int rc;
+    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m), dots(m + 1);
+    double bnorm2 = 0.0;
+    if ((rc = multidot(b, 1, b, &bnorm2)) != ND_OK) return rc;
+    const double bnorm = std::sqrt(bnorm2);
+    double res = 0.0;
+    for (int cycle = 0; cycle < restarts; ++cycle) {
+        // r = b - A x  (in V[0])
+        spmv_kernel<<<G, kNB, 0, s>>>(n, rowptr, col, vals, x, V);
+        axpby_kernel<<<G, kNB, 0, s>>>(n, 1.0, b, -1.0, V);
+        double beta2 = 0.0;
+        if ((rc = multidot(V, 1, V, &beta2)) != ND_OK) return rc;
+        const double beta = std::sqrt(beta2);
+        res = beta;
+        if (beta <= rtol * bnorm || beta == 0.0) break;
+        axpby_kernel<<<G, kNB, 0, s>>>(n, 0.0, V, 1.0 / beta, V);
+        std::fill(g.begin(), g.end(), 0.0);
+        g[0] = beta;
+        int k = 0;
+        for (; k < m; ++k) {
+            double* vk1 = V + (size_t)(k + 1) * ldv;
+            // right preconditioning: w = A D^-1 v_k
+            scale_kernel<<<G, kNB, 0, s>>>(n, dinv, V + (size_t)k * ldv, z);
+            spmv_kernel<<<G, kNB, 0, s>>>(n, rowptr, col, vals, z, vk1);
+            for (int pass = 0; pass < 2; ++pass) {
+                if ((rc = multidot(V, k + 1, vk1, dots.data())) != ND_OK) return rc;
+                cudaMemcpyAsync(dscal, dots.data(), (k + 1) * sizeof(double), cudaMemcpyHostToDevice, s);
+                orth_update<<<G, kNB, 0, s>>>(n, k + 1, V, ldv, dscal, vk1);
+                for (int j = 0; j <= k; ++j) H[(size_t)j * m + k] = (pass ? H[(size_t)j * m + k] : 0.0) + dots[j];
+            }
+            double hn2 = 0.0;
+            if ((rc = multidot(vk1, 1, vk1, &hn2)) != ND_OK) return rc;
+            const double hn = std::sqrt(hn2);
+            H[(size_t)(k + 1) * m + k] = hn;
+            if (hn > 0) axpby_kernel<<<G, kNB, 0, s>>>(n, 0.0, vk1, 1.0 / hn, vk1);
+            for (int j = 0; j < k; ++j) {
+                const double a = H[(size_t)j * m + k], bb = H[(size_t)(j + 1) * m + k];
+                H[(size_t)j * m + k] = cs[j] * a + sn[j] * bb;
+                H[(size_t)(j + 1) * m + k] = -sn[j] * a + cs[j] * bb;
+            }
+            const double a = H[(size_t)k * m + k], bb = H[(size_t)(k + 1) * m + k];
+            const double r = std::hypot(a, bb);
+            cs[k] = r > 0 ? a / r : 1.0;
+            sn[k] = r > 0 ? bb / r : 0.0;
+            H[(size_t)k * m + k] = r;
+            H[(size_t)(k + 1) * m + k] = 0.0;
+            g[k + 1] = -sn[k] * g[k];
+            g[k] = cs[k] * g[k];
+            res = std::fabs(g[k + 1]);
+            if (res <= rtol * bnorm || hn == 0.0) {
+                ++k;
+                break;
+            }
+        }
+        for (int i = k - 1; i >= 0; --i) {
+            double sacc = g[i];
+            for (int j = i + 1; j < k; ++j) sacc -= H[(size_t)i * m + j] * y[j];
+            const double d = H[(size_t)i * m + i];
+            y[i] = d != 0.0 ? sacc / d : 0.0;
+        }
+        // x += D^-1 V y
+        cudaMemcpyAsync(dscal, y.data(), k * sizeof(double), cudaMemcpyHostToDevice, s);
+        cudaMemsetAsync(z, 0, n * sizeof(double), s);
+        combine_kernel<<<G, kNB, 0, s>>>(n, k, V, ldv, dscal, z);
+        scale_kernel<<<G, kNB, 0, s>>>(n, dinv, z, z);
+        axpby_kernel<<<G, kNB, 0, s>>>(n, 1.0, z, 1.0, x);
+        if ((rc = sync("gmres")) != ND_OK) return rc;
+        if (res <= rtol * bnorm) break;
+    }
+    if (rel_res) *rel_res = bnorm > 0 ? res / bnorm : 0.0;
+    return ND_OK;
+}
+
+void vec_axpby(int64_t n, double a, const double* x, double b, double* y, cudaStream_t s) {
+    axpby_kernel<<<grid_for(n), kNB, 0, s>>>(n, a, x, b, y);
+}
+
 }  // namespace nd
 
 using namespace nd;
@@ -174,11 +289,9 @@ extern "C" int nd_find_fixpoint(nd_handle* h, double* u, const double* p, double
     if (rc != ND_OK) return rc;
     const int64_t n = h->dim;
     const JacPlan& J = h->jac;
-    // device workspace: F, Fnew, trial u, δ, w, Krylov basis V[m+1][n], Jacobian values,
-    // dot partials, scalars
-    const int64_t ldv = n;
-    const size_t doubles = (size_t)n * (7 + m + 1) + (size_t)std::max<int64_t>(nnz, 1) +
-                           (size_t)kDotBlocks * (m + 1) + 2 * (kMaxKrylov + 2);
+    // device workspace: F, Fnew, trial u, δ, -F, the Jacobian values, the GMRES workspace
+    // (w, D^-1, z, Krylov basis V[m+1][n], dot partials, scalars), the NaN flag
+    const size_t doubles = (size_t)n * 5 + (size_t)std::max<int64_t>(nnz, 1) + GmresSolver::doubles(n, m);
     Workspace ws;
     cudaError_t err = cudaMalloc(&ws.buf, doubles * sizeof(double) + 64);
     if (err != cudaSuccess) return cuda_fail(err, "nd_find_fixpoint: workspace");
@@ -186,14 +299,11 @@ extern "C" int nd_find_fixpoint(nd_handle* h, double* u, const double* p, double
     double* Fn = F + n;
     double* ut = Fn + n;
     double* dlt = ut + n;
-    double* w = dlt + n;
-    double* dinv = w + n;
-    double* z = dinv + n;
-    double* V = z + n;
-    double* vals = V + (size_t)n * (m + 1);
-    double* partial = vals + std::max<int64_t>(nnz, 1);
-    double* dscal = partial + (size_t)kDotBlocks * (m + 1);
-    int* nan_flag = reinterpret_cast<int*>(dscal + 2 * (kMaxKrylov + 2));
+    double* negF = dlt + n;
+    double* vals = negF + n;
+    GmresSolver gm;
+    gm.attach(vals + std::max<int64_t>(nnz, 1), n, m, s);
+    int* nan_flag = reinterpret_cast<int*>(gm.dscal + 2 * (kMaxKrylov + 2));
     const unsigned G = grid_for(n);
 
     auto sync_err = [&](const char* what) -> int {
@@ -205,21 +315,14 @@ extern "C" int nd_find_fixpoint(nd_handle* h, double* u, const double* p, double
     // max |x| and a NaN flag, on the host
     auto absmax = [&](const double* x, double* val, bool* nan) -> int {
         cudaMemsetAsync(nan_flag, 0, sizeof(int), s);
-        absmax_partial<<<kDotBlocks, kNB, 0, s>>>(n, x, partial, nan_flag);
-        absmax_final<<<1, 32, 0, s>>>(kDotBlocks, partial, dscal);
+        absmax_partial<<<kDotBlocks, kNB, 0, s>>>(n, x, gm.partial, nan_flag);
+        absmax_final<<<1, 32, 0, s>>>(kDotBlocks, gm.partial, gm.dscal);
         int flag = 0;
-        cudaMemcpyAsync(val, dscal, sizeof(double), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(val, gm.dscal, sizeof(double), cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(&flag, nan_flag, sizeof(int), cudaMemcpyDeviceToHost, s);
         const int r = sync_err("nd_find_fixpoint: norm");
         *nan = flag != 0;
         return r;
-    };
-    // dots[j] = V[j] . x for j < nv (host)
-    auto multidot = [&](const double* Vb, int nv, const double* x, double* dots) -> int {
-        multidot_partial<<<kDotBlocks, kNB, 0, s>>>(n, nv, Vb, ldv, x, partial);
-        multidot_final<<<1, 64, 0, s>>>(kDotBlocks, nv, partial, dscal);
-        cudaMemcpyAsync(dots, dscal, nv * sizeof(double), cudaMemcpyDeviceToHost, s);
-        return sync_err("nd_find_fixpoint: dot");
     };
 
     if ((rc = rhs(F, u)) != ND_OK) return rc;
@@ -231,83 +334,16 @@ extern "C" int nd_find_fixpoint(nd_handle* h, double* u, const double* p, double
         return fail(ND_ERR_NOT_CONVERGED, "Evaluation of network rhs resulted in NaNs (check u and p for NaN)");
     }
     int it = 0;
-    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m), dots(m + 1);
     while (fmax > tol && it < max_newton) {
         ++it;
         // Jacobian at u, then GMRES for J δ = -F from δ = 0
         if ((rc = nd_jacobian(h, ND_F64, vals, u, p, t, s)) != ND_OK) return rc;
-        diag_inverse_kernel<<<G, kNB, 0, s>>>(n, J.rowptr, J.colidx, vals, dinv);
+        gm.jacobi(J.rowptr, J.colidx, vals);
         cudaMemsetAsync(dlt, 0, n * sizeof(double), s);
-        double bnorm2 = 0.0;
-        if ((rc = multidot(F, 1, F, &bnorm2)) != ND_OK) return rc;
-        const double bnorm = std::sqrt(bnorm2);
-        const double eta = std::min(1e-2, fmax);
-        for (int cycle = 0; cycle < restarts; ++cycle) {
-            // r = -F - J δ  (in V[0])
-            spmv_kernel<<<G, kNB, 0, s>>>(n, J.rowptr, J.colidx, vals, dlt, V);
-            axpby_kernel<<<G, kNB, 0, s>>>(n, -1.0, F, -1.0, V);
-            double beta2 = 0.0;
-            if ((rc = multidot(V, 1, V, &beta2)) != ND_OK) return rc;
-            const double beta = std::sqrt(beta2);
-            if (beta <= eta * bnorm || beta == 0.0) break;
-            axpby_kernel<<<G, kNB, 0, s>>>(n, 0.0, V, 1.0 / beta, V);
-            std::fill(g.begin(), g.end(), 0.0);
-            g[0] = beta;
-            int k = 0;
-            double res = beta;
-            for (; k < m; ++k) {
-                double* vk1 = V + (size_t)(k + 1) * ldv;
-                // right preconditioning: w = J D^-1 v_k
-                scale_kernel<<<G, kNB, 0, s>>>(n, dinv, V + (size_t)k * ldv, z);
-                spmv_kernel<<<G, kNB, 0, s>>>(n, J.rowptr, J.colidx, vals, z, vk1);
-                // classical Gram-Schmidt, applied twice (reorthogonalisation)
-                for (int pass = 0; pass < 2; ++pass) {
-                    if ((rc = multidot(V, k + 1, vk1, dots.data())) != ND_OK) return rc;
-                    cudaMemcpyAsync(dscal, dots.data(), (k + 1) * sizeof(double), cudaMemcpyHostToDevice, s);
-                    orth_update<<<G, kNB, 0, s>>>(n, k + 1, V, ldv, dscal, vk1);
-                    for (int j = 0; j <= k; ++j) H[(size_t)j * m + k] = (pass ? H[(size_t)j * m + k] : 0.0) + dots[j];
-                }
-                double hn2 = 0.0;
-                if ((rc = multidot(vk1, 1, vk1, &hn2)) != ND_OK) return rc;
-                const double hn = std::sqrt(hn2);
-                H[(size_t)(k + 1) * m + k] = hn;
-                if (hn > 0) axpby_kernel<<<G, kNB, 0, s>>>(n, 0.0, vk1, 1.0 / hn, vk1);
-                // apply the previous rotations to column k, then a new one
-                for (int j = 0; j < k; ++j) {
-                    const double a = H[(size_t)j * m + k], b = H[(size_t)(j + 1) * m + k];
-                    H[(size_t)j * m + k] = cs[j] * a + sn[j] * b;
-                    H[(size_t)(j + 1) * m + k] = -sn[j] * a + cs[j] * b;
-                }
-                const double a = H[(size_t)k * m + k], b = H[(size_t)(k + 1) * m + k];
-                const double r = std::hypot(a, b);
-                cs[k] = r > 0 ? a / r : 1.0;
-                sn[k] = r > 0 ? b / r : 0.0;
-                H[(size_t)k * m + k] = r;
-                H[(size_t)(k + 1) * m + k] = 0.0;
-                g[k + 1] = -sn[k] * g[k];
-                g[k] = cs[k] * g[k];
-                res = std::fabs(g[k + 1]);
-                if (res <= eta * bnorm || hn == 0.0) {
-                    ++k;
-                    break;
-                }
-            }
-            // back substitution for y, then δ += V y
-            for (int i = k - 1; i >= 0; --i) {
-                double sacc = g[i];
-                for (int j = i + 1; j < k; ++j) sacc -= H[(size_t)i * m + j] * y[j];
-                const double d = H[(size_t)i * m + i];
-                y[i] = d != 0.0 ? sacc / d : 0.0;
-            }
-            // δ += D^-1 V y
-            cudaMemcpyAsync(dscal, y.data(), k * sizeof(double), cudaMemcpyHostToDevice, s);
-            cudaMemsetAsync(z, 0, n * sizeof(double), s);
-            combine_kernel<<<G, kNB, 0, s>>>(n, k, V, ldv, dscal, z);
-            scale_kernel<<<G, kNB, 0, s>>>(n, dinv, z, z);
-            axpby_kernel<<<G, kNB, 0, s>>>(n, 1.0, z, 1.0, dlt);
-            if ((rc = sync_err("nd_find_fixpoint: gmres")) != ND_OK) return rc;
-            if (res <= eta * bnorm) break;
-        }
+        cudaMemsetAsync(negF, 0, n * sizeof(double), s);  // 0 * (uninitialised) could be NaN
+        axpby_kernel<<<G, kNB, 0, s>>>(n, -1.0, F, 0.0, negF);
+        if ((rc = gm.solve(J.rowptr, J.colidx, vals, negF, dlt, std::min(1e-2, fmax), restarts, nullptr)) != ND_OK)
+            return rc;
         // backtracking line search on max|F|
         double lam = 1.0, fnew = 0.0;
         bool accepted = false;

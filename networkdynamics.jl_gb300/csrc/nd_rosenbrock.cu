@@ -1,0 +1,247 @@
+// Rosenbrock23 with a mass matrix: the linearly implicit method of Shampine & Reichelt
+// ("The MATLAB ODE Suite", SIAM J. Sci. Comput. 18, 1997; ode23s) for M u' = f(u) with a
+// diagonal M, zero entries making states algebraic -- the DAE form the reference hands to
+// SciML for networks whose components carry mass matrices (construct_mass_matrix,
+// src/construction.jl:409-467; the PQ bus of benchmark/benchmark_models.jl:66-74).
+//
+// With d = 1 / (2 + √2), e32 = 6 + √2 and W = M - h d J (J = ∂f/∂u at the step's start):
+//   k1 = W⁻¹ f(u)
+//   f1 = f(u + h/2 k1),            k2 = W⁻¹ (f1 - M k1) + k1
+//   u1 = u + h k2,  f2 = f(u1),    k3 = W⁻¹ (f2 - e32 (M k2 - f1) - 2 (M k1 - f0))
+//   error estimate h/6 (k1 - 2 k2 + k3), scaled RMS norm as for Tsit5; f2 is the next
+//   step's f0.  Step control: h ← h · min(5, max(0.2, 0.9 err^(-1/3))).
+// J is the analytic sparse Jacobian of nd_jacobian; W has J's pattern plus the diagonal;
+// each solve is GMRES right-preconditioned by W's diagonal.  FP64 handles only.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "nd_internal.h"
+
+namespace nd {
+
+namespace {
+
+constexpr int kB = 256;
+constexpr int kErrBlocks = 304;
+
+unsigned grid_of(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + kB - 1) / kB, 152 * 8)); }
+
+// W = -c J on W's pattern (jmap: the W position of every J entry) ...
+__global__ void form_w_kernel(int64_t nnz_j, const int32_t* __restrict__ jmap, const double* __restrict__ jv, double c,
+                              double* __restrict__ wv) {
+    for (int64_t k = (int64_t)blockIdx.x * kB + threadIdx.x; k < nnz_j; k += (int64_t)gridDim.x * kB)
+        wv[jmap[k]] = -__dmul_rn(c, jv[k]);
+}
+// ... plus M on the diagonal (wdiag: the W position of every row's diagonal)
+__global__ void add_mass_kernel(int64_t n, const int32_t* __restrict__ wdiag, const double* __restrict__ mass,
+                                double* __restrict__ wv) {
+    for (int64_t i = (int64_t)blockIdx.x * kB + threadIdx.x; i < n; i += (int64_t)gridDim.x * kB)
+        wv[wdiag[i]] = __dadd_rn(wv[wdiag[i]], mass ? mass[i] : 1.0);
+}
+
+// out = a x + b (M y), with M = diag(mass) (identity when mass is null)
+__global__ void axpmy_kernel(int64_t n, double a, const double* __restrict__ x, double b,
+                             const double* __restrict__ mass, const double* __restrict__ y, double* __restrict__ out) {
+    for (int64_t i = (int64_t)blockIdx.x * kB + threadIdx.x; i < n; i += (int64_t)gridDim.x * kB) {
+        const double my = mass ? __dmul_rn(mass[i], y[i]) : y[i];
+        out[i] = __dadd_rn(__dmul_rn(a, x[i]), __dmul_rn(b, my));
+    }
+}
+
+// the k3 right-hand side: f2 - e32 (M k2 - f1) - 2 (M k1 - f0)
+__global__ void k3_rhs_kernel(int64_t n, double e32, const double* __restrict__ mass, const double* __restrict__ f0,
+                              const double* __restrict__ f1, const double* __restrict__ f2,
+                              const double* __restrict__ k1, const double* __restrict__ k2, double* __restrict__ out) {
+    for (int64_t i = (int64_t)blockIdx.x * kB + threadIdx.x; i < n; i += (int64_t)gridDim.x * kB) {
+        const double mi = mass ? mass[i] : 1.0;
+        const double a = __dsub_rn(__dmul_rn(mi, k2[i]), f1[i]);
+        const double b = __dsub_rn(__dmul_rn(mi, k1[i]), f0[i]);
+        out[i] = __dsub_rn(__dsub_rn(f2[i], __dmul_rn(e32, a)), __dmul_rn(2.0, b));
+    }
+}
+
+// Σ (err_i / (abstol + reltol max(|u_i|, |u1_i|)))² per block, err = h/6 (k1 - 2 k2 + k3)
+__global__ void err_partial_kernel(int64_t n, double h6, const double* __restrict__ k1, const double* __restrict__ k2,
+                                   const double* __restrict__ k3, const double* __restrict__ u,
+                                   const double* __restrict__ u1, double abstol, double reltol,
+                                   double* __restrict__ partial) {
+    __shared__ double red[kB / 32];
+    double acc = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * kB + threadIdx.x; i < n; i += (int64_t)gridDim.x * kB) {
+        const double e = __dmul_rn(h6, __dadd_rn(__dsub_rn(k1[i], __dmul_rn(2.0, k2[i])), k3[i]));
+        const double sc = abstol + reltol * fmax(fabs(u[i]), fabs(u1[i]));
+        const double r = e / sc;
+        acc = __dadd_rn(acc, __dmul_rn(r, r));
+    }
+    for (int off = 16; off > 0; off >>= 1) acc = __dadd_rn(acc, __shfl_xor_sync(0xffffffffu, acc, off));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < kB / 32; ++k) t = __dadd_rn(t, red[k]);
+        partial[blockIdx.x] = t;
+    }
+}
+
+struct Buf {
+    void* p = nullptr;
+    ~Buf() { cudaFree(p); }
+};
+
+}  // namespace
+
+}  // namespace nd
+
+using namespace nd;
+
+extern "C" int nd_solve_rosenbrock23(nd_handle* h, double* u, const double* p, const double* mass, double t0,
+                                     double t1, double reltol, double abstol, int64_t max_steps, nd_solve_stats* st,
+                                     void* stream) {
+    clear_error();
+    if (!h || !u || !st) return fail(ND_ERR_ARG, "nd_solve_rosenbrock23: NULL argument");
+    if (h->dtype != ND_F64) return fail(ND_ERR_DTYPE, "nd_solve_rosenbrock23: FP64 handles only");
+    if (h->pdim > 0 && !p) return fail(ND_ERR_ARG, "nd_solve_rosenbrock23: p is NULL");
+    if (!(t1 > t0)) return fail(ND_ERR_ARG, "nd_solve_rosenbrock23: t1 must be greater than t0");
+    if (!(reltol > 0) || !(abstol > 0)) return fail(ND_ERR_ARG, "nd_solve_rosenbrock23: tolerances must be > 0");
+    const int64_t budget = max_steps > 0 ? max_steps : (int64_t)ND_ENSEMBLE_DEFAULT_MAX_STEPS;
+    *st = nd_solve_stats{};
+    cudaStream_t s = (cudaStream_t)stream;
+    int64_t nnz = 0;
+    int rc = nd_jacobian_pattern(h, &nnz, nullptr, nullptr);
+    if (rc != ND_OK) return rc;
+    const int64_t n = h->dim;
+    const JacPlan& J = h->jac;
+    // W's pattern: J's columns plus the diagonal, sorted per row
+    std::vector<int32_t> wrow(n + 1, 0), wcol, jmap((size_t)std::max<int64_t>(nnz, 1)), wdiag(n);
+    wcol.reserve((size_t)nnz + n);
+    for (int64_t i = 0; i < n; ++i) {
+        const int32_t b = J.rowptr_h[i], e = J.rowptr_h[i + 1];
+        bool diag_done = false;
+        for (int32_t k = b; k <= e; ++k) {
+            const bool end = k == e;
+            const int32_t c = end ? INT32_MAX : J.colidx_h[k];
+            if (!diag_done && c >= (int32_t)i) {
+                if (c != (int32_t)i) wcol.push_back((int32_t)i);  // a diagonal the pattern lacks
+                wdiag[i] = (int32_t)wcol.size() - (c == (int32_t)i ? 0 : 1);
+                diag_done = true;
+            }
+            if (end) break;
+            jmap[k] = (int32_t)wcol.size();
+            wcol.push_back(c);
+        }
+        wrow[i + 1] = (int32_t)wcol.size();
+    }
+    const int64_t wnnz = (int64_t)wcol.size();
+    const int m = 30;
+    // device: W pattern (rowptr, col, jmap, wdiag), J values, W values, 8 vectors
+    // (f0 f1 f2 k1 k2 k3 u1 rhs), error partials, GMRES workspace
+    const size_t ints = (size_t)(n + 1) + wnnz + jmap.size() + n;
+    const size_t dbl = (size_t)std::max<int64_t>(nnz, 1) + wnnz + 8 * (size_t)n + kErrBlocks + GmresSolver::doubles(n, m);
+    Buf buf;
+    cudaError_t err = cudaMalloc(&buf.p, ints * sizeof(int32_t) + 16 + dbl * sizeof(double));
+    if (err != cudaSuccess) return cuda_fail(err, "nd_solve_rosenbrock23: workspace");
+    int32_t* d_wrow = static_cast<int32_t*>(buf.p);
+    int32_t* d_wcol = d_wrow + (n + 1);
+    int32_t* d_jmap = d_wcol + wnnz;
+    int32_t* d_wdiag = d_jmap + jmap.size();
+    double* jv = reinterpret_cast<double*>((reinterpret_cast<uintptr_t>(d_wdiag + n) + 15) & ~uintptr_t(15));
+    double* wv = jv + std::max<int64_t>(nnz, 1);
+    double* f0 = wv + wnnz;
+    double* f1 = f0 + n;
+    double* f2 = f1 + n;
+    double* k1 = f2 + n;
+    double* k2 = k1 + n;
+    double* k3 = k2 + n;
+    double* u1 = k3 + n;
+    double* rb = u1 + n;
+    double* partial = rb + n;
+    GmresSolver gm;
+    gm.attach(partial + kErrBlocks, n, m, s);
+    if ((err = cudaMemcpyAsync(d_wrow, wrow.data(), (n + 1) * sizeof(int32_t), cudaMemcpyHostToDevice, s)) !=
+            cudaSuccess ||
+        (err = cudaMemcpyAsync(d_wcol, wcol.data(), wnnz * sizeof(int32_t), cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (err = cudaMemcpyAsync(d_jmap, jmap.data(), jmap.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s)) !=
+            cudaSuccess ||
+        (err = cudaMemcpyAsync(d_wdiag, wdiag.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return cuda_fail(err, "nd_solve_rosenbrock23: pattern upload");
+    const unsigned G = grid_of(n);
+    const double d = 1.0 / (2.0 + std::sqrt(2.0)), e32 = 6.0 + std::sqrt(2.0);
+    auto rhs = [&](double* out, const double* x) { return nd_rhs(h, ND_F64, out, n, x, n, p, h->pdim, NAN, s); };
+    // the linear systems are solved well below the step's own error scale
+    const double lin_tol = std::min(1e-3, 1e-2 * reltol);
+    auto wsolve = [&](const double* bvec, double* x) -> int {
+        cudaMemsetAsync(x, 0, n * sizeof(double), s);
+        return gm.solve(d_wrow, d_wcol, wv, bvec, x, lin_tol, 50, nullptr);
+    };
+    if ((rc = rhs(f0, u)) != ND_OK) return rc;
+    double dt = std::min(1e-3 * (t1 - t0), 1e-2);
+    double t = t0;
+    int64_t steps = 0;
+    int status = ND_OK;
+    std::vector<double> hpart(kErrBlocks);
+    while (t < t1) {
+        if (steps >= budget) {
+            status = ND_ERR_MAXITERS;
+            break;
+        }
+        ++steps;
+        if (t + dt * (1 + 1e-12) > t1) dt = t1 - t;
+        // W = M - h d J at u
+        if ((rc = nd_jacobian(h, ND_F64, jv, u, p, t, s)) != ND_OK) return rc;
+        cudaMemsetAsync(wv, 0, wnnz * sizeof(double), s);
+        form_w_kernel<<<grid_of(std::max<int64_t>(nnz, 1)), kB, 0, s>>>(nnz, d_jmap, jv, dt * d, wv);
+        add_mass_kernel<<<G, kB, 0, s>>>(n, d_wdiag, mass, wv);
+        gm.jacobi(d_wrow, d_wcol, wv);
+        // k1
+        if ((rc = wsolve(f0, k1)) != ND_OK) return rc;
+        // f1 = f(u + h/2 k1); k2 = W⁻¹ (f1 - M k1) + k1
+        cudaMemcpyAsync(u1, u, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+        vec_axpby(n, 0.5 * dt, k1, 1.0, u1, s);
+        if ((rc = rhs(f1, u1)) != ND_OK) return rc;
+        axpmy_kernel<<<G, kB, 0, s>>>(n, 1.0, f1, -1.0, mass, k1, rb);
+        if ((rc = wsolve(rb, k2)) != ND_OK) return rc;
+        vec_axpby(n, 1.0, k1, 1.0, k2, s);
+        // u1 = u + h k2, f2 = f(u1); k3
+        cudaMemcpyAsync(u1, u, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+        vec_axpby(n, dt, k2, 1.0, u1, s);
+        if ((rc = rhs(f2, u1)) != ND_OK) return rc;
+        k3_rhs_kernel<<<G, kB, 0, s>>>(n, e32, mass, f0, f1, f2, k1, k2, rb);
+        if ((rc = wsolve(rb, k3)) != ND_OK) return rc;
+        // error norm
+        err_partial_kernel<<<kErrBlocks, kB, 0, s>>>(n, dt / 6.0, k1, k2, k3, u, u1, abstol, reltol, partial);
+        cudaMemcpyAsync(hpart.data(), partial, kErrBlocks * sizeof(double), cudaMemcpyDeviceToHost, s);
+        if ((rc = gm.sync("nd_solve_rosenbrock23")) != ND_OK) return rc;
+        double e2 = 0.0;
+        for (double x : hpart) e2 += x;
+        double EEst = std::sqrt(e2 / (double)(n ? n : 1));
+        if (!(EEst == EEst)) EEst = 1e10;
+        const double fac = std::min(5.0, std::max(0.2, 0.9 * std::pow(std::max(EEst, 1e-10), -1.0 / 3.0)));
+        if (EEst <= 1.0) {
+            t = (std::fabs(t1 - (t + dt)) <= 1e-14 * std::max(1.0, std::fabs(t1))) ? t1 : t + dt;
+            cudaMemcpyAsync(u, u1, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+            cudaMemcpyAsync(f0, f2, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+            st->naccept++;
+        } else {
+            st->nreject++;
+        }
+        st->nf += 2;
+        st->dt_last = dt * fac;
+        dt *= fac;
+        if (t < t1 && dt < 1e-14 * std::max(1.0, std::fabs(t))) {
+            status = ND_ERR_NOT_CONVERGED;
+            break;
+        }
+    }
+    if ((rc = gm.sync("nd_solve_rosenbrock23")) != ND_OK) return rc;
+    st->t_final = t;
+    st->status = status;
+    if (status == ND_ERR_MAXITERS) return fail(ND_ERR_MAXITERS, "nd_solve_rosenbrock23: step budget exhausted before t1");
+    if (status == ND_ERR_NOT_CONVERGED) {
+        char msg[160];
+        snprintf(msg, sizeof msg, "nd_solve_rosenbrock23: step size underflow at t = %.6g", t);
+        return fail(ND_ERR_NOT_CONVERGED, msg);
+    }
+    return ND_OK;
+}

@@ -27,7 +27,9 @@ class VertexModel:
     f: Optional[Callable] = None
     g: object = 1                       # StateMask(1): the first state is the output
     outdim: int = 1                     # StateMask(1:outdim)
-    mass_matrix: Optional[float] = None  # 0: algebraic states (the PQ bus); None: identity
+    # diagonal mass matrix: None (the identity), a scalar for every state (0: algebraic, as the
+    # PQ bus) or one entry per state
+    mass_matrix: Optional[object] = None
     constants: tuple = ()               # values the component function closes over
     extin: Optional[Sequence] = None    # external inputs (VIndex / EIndex of other components' states)
 
@@ -46,6 +48,7 @@ class EdgeModel:
     outdim: int = 1                     # per side
     extin: Optional[Sequence] = None    # external inputs (VIndex / EIndex of other components' states)
     loopback: bool = False              # a LoopbackConnection: copies the dst output into the src input
+    mass_matrix: Optional[object] = None  # diagonal mass matrix of the edge's states, as for vertices
 
 
 # --- vertices (test/ComponentLibrary.jl) -------------------------------------------------

@@ -99,6 +99,15 @@ def _check_no_external_inputs(vms, ems):
                                  "loopback edges only (no library vertex is an injector with a feed-forward output)")
 
 
+def _mm_key(mm):
+    """A hashable form of a component's mass matrix (components with different mass
+    matrices are different components, in batches of their own)."""
+    if mm is None:
+        return None
+    a = np.asarray(mm, dtype=np.float64)
+    return (a.shape, tuple(a.ravel().tolist()))
+
+
 def _batches(models, key):
     """Batches of identical components in order of first appearance, as find_identical
     groups them (src/utils.jl:197-216, src/construction.jl:155-168): the model of every
@@ -159,11 +168,12 @@ class Network:
         if isinstance(vertexm, VertexModel):
             self.vertex_batches, self.vertex_batch = [vertexm], np.zeros(g.nv, dtype=np.int32)
         else:
-            self.vertex_batches, self.vertex_batch = _batches(vms, lambda m: (m.kind, m.constants))
+            self.vertex_batches, self.vertex_batch = _batches(vms, lambda m: (m.kind, m.constants,
+                                                                              _mm_key(m.mass_matrix)))
         if isinstance(edgem, EdgeModel):
             self.edge_batches, self.edge_batch = [edgem], np.zeros(g.ne, dtype=np.int32)
         else:
-            self.edge_batches, self.edge_batch = _batches(ems, lambda m: (m.kind, m.coupling))
+            self.edge_batches, self.edge_batch = _batches(ems, lambda m: (m.kind, m.coupling, _mm_key(m.mass_matrix)))
         # the single model of a one-batch network (None when there are several)
         self.vertexm = self.vertex_batches[0] if len(self.vertex_batches) == 1 else None
         self.edgem = self.edge_batches[0] if len(self.edge_batches) == 1 else None
@@ -231,6 +241,29 @@ class Network:
                     val = np.asarray(val, dtype=np.float64)
                     p[first[idx] + k] = val if val.ndim == 0 else val[idx]
         return p
+
+    def mass_matrix(self):
+        """The network's mass matrix as construct_mass_matrix builds it
+        (src/construction.jl:409-467): None when every component has the identity (the
+        reference's `I`), else its diagonal over the flat state vector, each component's own
+        diagonal placed at its state range (v_data / e_data).  A component's mass matrix is a
+        scalar for all its states or one entry per state; full matrices are not supported."""
+        if all(m.mass_matrix is None for m in list(self.vertex_batches) + list(self.edge_batches)):
+            return None
+        diag = np.ones(self.dim)
+        for models, batch, first in ((self.vertex_batches, self.vertex_batch, self.v_data),
+                                     (self.edge_batches, self.edge_batch, self.e_data)):
+            for b, m in enumerate(models):
+                if m.mass_matrix is None or m.dim == 0:
+                    continue
+                mm = np.asarray(m.mass_matrix, dtype=np.float64)
+                if mm.ndim > 1 or (mm.ndim == 1 and mm.shape[0] != m.dim):
+                    raise capi.ArgumentError(capi.ND_ERR_ARG,
+                                             f"Mass matrix must be a scalar or one entry per state (a diagonal); "
+                                             f"got shape {mm.shape} in component :{m.name}.")
+                idx = np.flatnonzero(batch == b)
+                diag[first[idx][:, None] + np.arange(m.dim)] = np.broadcast_to(mm, (m.dim,))
+        return diag
 
     # --- device handle -------------------------------------------------------------------
     def _create(self, dtype):

@@ -269,6 +269,46 @@ class OracleNetwork:
         return out
 
 
+def rosenbrock23(rhs, jac, u0, t0, t1, reltol, abstol, mass=None, max_steps=100_000):
+    """Rosenbrock23 (Shampine & Reichelt 1997, ode23s) for M u' = rhs(u) with a diagonal mass
+    matrix (None: identity), dense: W = M - h d J, d = 1/(2+√2), e32 = 6+√2;
+    k1 = W⁻¹ f0, k2 = W⁻¹ (f(u + h/2 k1) - M k1) + k1, u1 = u + h k2,
+    k3 = W⁻¹ (f(u1) - e32 (M k2 - f1) - 2 (M k1 - f0)), error h/6 (k1 - 2 k2 + k3) in the
+    scaled RMS norm, step factor min(5, max(0.2, 0.9 err^(-1/3))), first step
+    min(1e-3 (t1 - t0), 1e-2).  The restatement the GPU solver is checked against.
+    Returns (u(t1), accepted steps, rejected steps)."""
+    u = np.array(u0, dtype=np.float64, copy=True)
+    n = u.size
+    M = np.ones(n) if mass is None else np.broadcast_to(np.asarray(mass, dtype=np.float64), (n,))
+    d, e32 = 1.0 / (2.0 + np.sqrt(2.0)), 6.0 + np.sqrt(2.0)
+    f0 = rhs(u)
+    t, dt = t0, min(1e-3 * (t1 - t0), 1e-2)
+    na = nr = 0
+    while t < t1 and na + nr < max_steps:
+        if t + dt * (1 + 1e-12) > t1:
+            dt = t1 - t
+        W = np.diag(M) - dt * d * jac(u)
+        k1 = np.linalg.solve(W, f0)
+        f1 = rhs(u + 0.5 * dt * k1)
+        k2 = np.linalg.solve(W, f1 - M * k1) + k1
+        u1 = u + dt * k2
+        f2 = rhs(u1)
+        k3 = np.linalg.solve(W, f2 - e32 * (M * k2 - f1) - 2.0 * (M * k1 - f0))
+        err = dt / 6.0 * (k1 - 2.0 * k2 + k3)
+        E = np.sqrt(np.mean((err / (abstol + reltol * np.maximum(np.abs(u), np.abs(u1)))) ** 2))
+        if not E == E:
+            E = 1e10
+        fac = min(5.0, max(0.2, 0.9 * max(E, 1e-10) ** (-1.0 / 3.0)))
+        if E <= 1.0:
+            t = t1 if abs(t1 - (t + dt)) <= 1e-14 * max(1.0, abs(t1)) else t + dt
+            u, f0 = u1, f2
+            na += 1
+        else:
+            nr += 1
+        dt *= fac
+    return u, na, nr
+
+
 def rhs_numpy(nv, src, dst, vk, ek, u, p, dtype=np.float64):
     """Independent numpy restatement of the sequential RHS for one homogeneous batch."""
     src = np.asarray(src, dtype=np.int64)

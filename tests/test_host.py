@@ -174,3 +174,34 @@ def test_python_layout_matches_oracle_layout(seed):
     assert [lib.nd_oracle_e_para(on.L, e) for e in range(g.ne)] == net.e_para.tolist()
     ode = [e for e in range(g.ne) if net.edge_batches[net.edge_batch[e]].dim == 2]
     assert [lib.nd_oracle_e_data(on.L, e) for e in ode] == net.e_data[ode].tolist()
+
+
+def test_mass_matrix_like_construct_mass_matrix():
+    """construct_mass_matrix (src/construction.jl:409-467): the identity (None) when no
+    component has a mass matrix; otherwise each component's diagonal at its state range.
+    The PQ bus is algebraic (mass matrix 0, benchmark/benchmark_models.jl:74)."""
+    import dataclasses
+    g = nd.watts_strogatz(12, 2, 0.3, seed=3)
+    assert nd.Network(g, nd.kuramoto_second(), nd.static_line()).mass_matrix() is None
+    vm = [nd.pqnode() if v % 3 == 0 else nd.generator() for v in range(g.nv)]
+    net = nd.Network(g, vm, nd.piline())
+    mm = net.mass_matrix()
+    assert mm.shape == (net.dim,)
+    for v in range(g.nv):
+        s = net.vertex_state_index(v)
+        want = [0.0, 0.0] if v % 3 == 0 else [1.0] * 4
+        np.testing.assert_array_equal(mm[s:s + len(want)], want)
+    # any library vertex can be made algebraic; it then forms a batch of its own
+    alg = dataclasses.replace(nd.diffusion_vertex(), mass_matrix=0)
+    vms = [alg if v in (2, 5) else nd.diffusion_vertex() for v in range(g.nv)]
+    net = nd.Network(g, vms, nd.diffusion_edge())
+    assert len(net.vertex_batches) == 2
+    mm = net.mass_matrix()
+    assert mm[net.vertex_state_index(2)] == 0 and mm[net.vertex_state_index(5)] == 0 and mm.sum() == g.nv - 2
+    # per-state diagonals; a full matrix is rejected
+    sw = dataclasses.replace(nd.kuramoto_second(), mass_matrix=[1.0, 0.5])
+    net = nd.Network(g, sw, nd.static_line())
+    np.testing.assert_array_equal(net.mass_matrix(), np.tile([1.0, 0.5], g.nv))
+    bad = dataclasses.replace(nd.kuramoto_second(), mass_matrix=np.eye(2))
+    with pytest.raises(nd.ArgumentError):
+        nd.Network(g, bad, nd.static_line()).mass_matrix()

@@ -147,3 +147,22 @@ def test_oracle_barabasi_albert_equals_package_generator(n, m, seed):
     assert a.nv == b.nv
     np.testing.assert_array_equal(a.src, b.src)
     np.testing.assert_array_equal(a.dst, b.dst)
+
+
+def test_oracle_rosenbrock23_known_answer():
+    """The oracle's dense Rosenbrock23 (the restatement the GPU solver is checked against)
+    reproduces exp(-tL) x0 for diffusion (test/diffusion_test.jl:119-129), and with a zero
+    mass-matrix entry keeps that vertex on its algebraic constraint."""
+    import scipy.linalg
+    g = nd.barabasi_albert(20, 3, seed=4)
+    L = g.laplacian()
+    on = O.OracleNetwork.from_graph(g, O.V_DIFFUSION, O.E_DIFFUSION_UNIT)
+    x0 = np.random.default_rng(1).normal(size=g.nv)
+    rhs, jac = (lambda x: on.rhs(x, None)), (lambda x: -L)
+    u, na, nr = O.rosenbrock23(rhs, jac, x0, 0.0, 1.0, 1e-6, 1e-9)
+    assert na > 0 and np.max(np.abs(u - scipy.linalg.expm(-L) @ x0)) < 1e-5
+    mass = np.ones(g.nv)
+    mass[0] = 0.0
+    x0[0] = -L[0, 1:] @ x0[1:] / L[0, 0]  # consistent: (L x)_0 = 0
+    u, _, _ = O.rosenbrock23(rhs, jac, x0, 0.0, 1.0, 1e-6, 1e-9, mass=mass)
+    assert abs(L[0] @ u) < 1e-10
