@@ -73,9 +73,9 @@ def peaks():
 def kernel_bytes(g, s):
     """Algorithmic bytes (and FP64 lane operations) of one launch of each RHS kernel for
     diffusion edges with s-byte values.
-      edge phase  per edge: src, dst, bucket slot (4 B each); u_src, u_dst, w, y, ybkt (s each)
-      row phase   per row: slot vertex, slot pointer, dptr pair, sptr (20 B) and du (s);
-                  per destination-side incidence loc (4 B) + ybkt (s); per source-side y (s)
+      edge phase  per edge: src, dst (4 B each), staging slot (2 B); u_src, u_dst, w, y, ybkt (s each)
+      row phase   per row: its 16-byte record and du (s); per destination-side incidence its
+                  ybkt position (4 B) + ybkt (s); per source-side y (s)
       heavy rows  per row: slot vertex, slot pointer pair (12 B), u_v and du (s each);
                   per incidence the (nbr, eid) pair (8 B), u_nbr and w (s each)
       fused       the whole RHS (algorithmic_bytes)
@@ -86,9 +86,9 @@ def kernel_bytes(g, s):
     heavy = (ndst + nsrc) > HEAVY_MIN_DEGREE - 1
     light = ~heavy
     nh, inc_h = int(heavy.sum()), int((ndst + nsrc)[heavy].sum())
-    rows = int(light.sum()) * (20 + s) + int(ndst[light].sum()) * (4 + s) + int(nsrc[light].sum()) * s
+    rows = int(light.sum()) * (16 + s) + int(ndst[light].sum()) * (4 + s) + int(nsrc[light].sum()) * s
     return {
-        "edge_phase": (ne * (12 + 5 * s), 2 * ne),
+        "edge_phase": (ne * (10 + 5 * s), 2 * ne),
         "row_phase": (rows, int((ndst + nsrc)[light].sum())),
         "heavy_rows": (nh * (12 + 2 * s) + inc_h * (8 + 2 * s), 3 * inc_h),
         "fused": (algorithmic_bytes(nv, ne, s), 3 * 2 * ne),

@@ -41,9 +41,8 @@ void free_topology(Topology* t) {
     cudaFree(el.lslot);
     cudaFree(el.run_start);
     cudaFree(el.run_base);
-    cudaFree(el.dptr);
-    cudaFree(el.loc);
-    cudaFree(el.sptr);
+    cudaFree(el.rmeta);
+    cudaFree(el.locp);
     cudaFree(el.y);
     cudaFree(el.ybkt);
     *t = Topology{};
@@ -247,6 +246,22 @@ int build_topology(int64_t nv, int64_t ne, const int64_t* src, const int64_t* ds
     if (edge_elem > 0 && ne > 0 && is_canonical(ne, src, dst)) {
         EdgeLayoutHost h;
         build_edge_layout(nv, ne, src, dst, h);
+        // the row records and the padded loc array, in slot order of the rows
+        std::vector<int64_t> lstart(nv + 1, 0);
+        for (int64_t v = 0; v < nv; ++v) lstart[v + 1] = lstart[v] + ((h.dptr[v + 1] - h.dptr[v] + 3) & ~3u);
+        if (lstart[nv] > (int64_t)INT32_MAX) {
+            free_topology(&t);
+            return fail(ND_ERR_UNSUPPORTED, "padded destination-side index array above 2^31-1 entries");
+        }
+        std::vector<int32_t> locp((size_t)std::max<int64_t>(lstart[nv], 4), 0);
+        for (int64_t v = 0; v < nv; ++v)
+            for (uint32_t k = h.dptr[v]; k < h.dptr[v + 1]; ++k) locp[lstart[v] + (k - h.dptr[v])] = h.loc[k];
+        std::vector<int4> rmeta(nv, int4{0, 0, 0, 0});
+        for (int64_t sl = t.n_heavy; sl < nv; ++sl) {
+            const int32_t v = slot_vertex[sl];
+            const uint32_t nd = h.dptr[v + 1] - h.dptr[v], ns = h.sptr[v + 1] - h.sptr[v];
+            rmeta[sl] = int4{v, (int32_t)lstart[v], (int32_t)h.sptr[v], (int32_t)(nd | (ns << 16))};
+        }
         EdgeLayout& el = t.edge;
         el.n_chunks = h.n_chunks;
         if ((err = upload((void**)&el.esrc, h.esrc.data(), h.esrc.size() * sizeof(int32_t))) != cudaSuccess ||
@@ -256,10 +271,10 @@ int build_topology(int64_t nv, int64_t ne, const int64_t* src, const int64_t* ds
                 cudaSuccess ||
             (err = upload((void**)&el.run_base, h.run_base.data(), h.run_base.size() * sizeof(int32_t))) !=
                 cudaSuccess ||
-            (err = upload((void**)&el.dptr, h.dptr.data(), h.dptr.size() * sizeof(uint32_t))) != cudaSuccess ||
-            (err = upload((void**)&el.loc, h.loc.data(), h.loc.size() * sizeof(int32_t))) != cudaSuccess ||
-            (err = upload((void**)&el.sptr, h.sptr.data(), h.sptr.size() * sizeof(uint32_t))) != cudaSuccess ||
-            (err = cudaMalloc(&el.y, (size_t)ne * edge_elem)) != cudaSuccess ||
+            (err = upload((void**)&el.rmeta, rmeta.data(), rmeta.size() * sizeof(int4))) != cudaSuccess ||
+            (err = upload((void**)&el.locp, locp.data(), locp.size() * sizeof(int32_t))) != cudaSuccess ||
+            (err = cudaMalloc(&el.y, (size_t)(ne + 2) * edge_elem)) != cudaSuccess ||
+            (err = cudaMemset(el.y, 0, (size_t)(ne + 2) * edge_elem)) != cudaSuccess ||
             (err = cudaMalloc(&el.ybkt, (size_t)ne * edge_elem)) != cudaSuccess) {
             free_topology(&t);
             return cuda_fail(err, "upload of the edge-centric layout");
@@ -561,9 +576,8 @@ int nd_rhs(nd_handle* h, int dtype, void* du, int64_t n_du, const void* u, int64
     a.lslot = el.lslot;
     a.run_start = el.run_start;
     a.run_base = el.run_base;
-    a.dptr = el.dptr;
-    a.loc = el.loc;
-    a.sptr = el.sptr;
+    a.rmeta = el.rmeta;
+    a.locp = el.locp;
     a.y = el.y;
     a.ybkt = el.ybkt;
     a.heavy_only = 0;

@@ -64,7 +64,7 @@ inline int edge_outdim(int ek) { return ek == ND_E_PILINE ? 2 : 1; }
 constexpr int kLightMaxDeg = 32;
 constexpr int kMediumMaxDeg = 2048;
 constexpr int kWindow = 256;
-constexpr int kLightRun = 8192;
+constexpr int kLightRun = 128;
 
 // Device-resident topology of one network.
 // Rows are stored in processing order ("slots"): heavy rows (by degree, descending), then
@@ -81,7 +81,8 @@ constexpr int kWindowIncidences = 2048;  // light window: at most this many inci
 //      destination-CSR positions: a block stages its chunk's values in shared memory in
 //      (bucket, edge) order and writes each bucket's run of them as one contiguous piece;
 //   R: each row sums its dst-side values (gathered from one bucket, which stays in L2
-//      while the rows of that range run) and then -y over its source block.
+//      while the rows of that range run) and then -y over its source block; its position
+//      in locp, its source block and both lengths come in one 16-byte record per slot.
 // Each edge's function is evaluated once instead of twice, and the edge parameters and
 // the incidence stream are read in order instead of gathered.
 constexpr int kEdgeChunk = 2048;  // edges per phase-E block
@@ -95,10 +96,13 @@ struct EdgeLayout {
     uint16_t* lslot = nullptr;     // [ne] slot of edge e in its chunk's (bucket, edge)-ordered staging
     uint16_t* run_start = nullptr;  // [n_chunks][kBuckets+1] first staging slot of each bucket's run
     int32_t* run_base = nullptr;    // [n_chunks][kBuckets] ybkt position of each bucket's run
-    uint32_t* dptr = nullptr;  // [nv+1] each vertex's range in destination-CSR order
-    int32_t* loc = nullptr;    // [ne] ybkt position of destination-CSR entry k
-    uint32_t* sptr = nullptr;  // [nv+1] each vertex's source block (edge ids)
-    void* y = nullptr;         // [ne] scratch, element type of the handle
+    // per row slot (rows of degree <= kMediumMaxDeg; zero for the heavy slots): the vertex,
+    // the row's first entry in locp, its source block's first edge, nd | ns << 16
+    int4* rmeta = nullptr;
+    // ybkt positions of every row's destination-side values, each row's run starting on a
+    // multiple of 4 entries (padding entries hold 0), so they load as 16-byte vectors
+    int32_t* locp = nullptr;
+    void* y = nullptr;         // [ne + 2] scratch, element type of the handle (+2: pair loads)
     void* ybkt = nullptr;      // [ne] scratch
 };
 
@@ -148,9 +152,8 @@ struct RhsArgs {
     const uint16_t* lslot;
     const uint16_t* run_start;
     const int32_t* run_base;
-    const uint32_t* dptr;
-    const int32_t* loc;
-    const uint32_t* sptr;
+    const int4* rmeta;
+    const int32_t* locp;
     void* y;
     void* ybkt;
 };

@@ -124,7 +124,9 @@ __global__ void __launch_bounds__(kBlock) edge_phase_kernel(RhsArgs a) {
 //         start folded into the first term (0 + t is t, and both zeros give +0);
 //   FP32  the same order with Kahan compensation on rows longer than kLightMaxDeg.
 template <typename T, int VK>
-__global__ void __launch_bounds__(kBlock) row_phase_kernel(RhsArgs a) {
+// FP32 rows run best with 5 blocks per SM (registers capped at 48), FP64 rows with the 52
+// registers they take at 4 blocks (A/B on BA(1e7, 4): 256 / 288 µs FP32, 346 / 327 µs FP64).
+__global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 5 : 1) row_phase_kernel(RhsArgs a) {
     using A = Arith<T>;
     constexpr int kBatch = 12;
     const int64_t slot = (int64_t)a.n_heavy + (int64_t)blockIdx.x * kBlock + threadIdx.x;
@@ -132,10 +134,12 @@ __global__ void __launch_bounds__(kBlock) row_phase_kernel(RhsArgs a) {
     const T* __restrict__ y = static_cast<const T*>(a.y);
     const T* __restrict__ ybkt = static_cast<const T*>(a.ybkt);
     const uint64_t stream = policy_evict_first();
-    const int64_t v = __ldg(a.slot_vertex + slot);
-    const uint32_t dp = __ldg(a.dptr + v), sp = __ldg(a.sptr + v);
-    const int nd = (int)(__ldg(a.dptr + v + 1) - dp);
-    const int ns = (int)(__ldg(a.sptr + v + 1) - sp);
+    const int4 rm = ld_hint(a.rmeta + slot, stream);
+    const int64_t v = rm.x;
+    const int32_t lp = rm.y;  // multiple of 4
+    const uint32_t sp = (uint32_t)rm.z;
+    const int nd = rm.w & 0xffff;
+    const int ns = (int)((uint32_t)rm.w >> 16);
     const bool kahan = sizeof(T) == 4 && nd + ns > kLightMaxDeg;
     T acc = T(0), comp = T(0);
     auto add = [&](T t, bool src) {
@@ -156,10 +160,20 @@ __global__ void __launch_bounds__(kBlock) row_phase_kernel(RhsArgs a) {
     // The adds of a batch stop at the longest remaining run in the warp (a warp-uniform
     // bound), so a warp issues no add for batch slots that none of its rows has.
     for (int j0 = 0; j0 < nd; j0 += kBatch) {
+        // the batch's positions as 16-byte vectors (the row's run starts on a multiple of 4)
+        int li[kBatch];
+#pragma unroll
+        for (int k4 = 0; k4 < kBatch / 4; ++k4) {
+            const int4 q = j0 + 4 * k4 < nd ? ld_hint(reinterpret_cast<const int4*>(a.locp + lp + j0) + k4, stream)
+                                            : int4{0, 0, 0, 0};
+            li[4 * k4] = q.x;
+            li[4 * k4 + 1] = q.y;
+            li[4 * k4 + 2] = q.z;
+            li[4 * k4 + 3] = q.w;
+        }
         T t[kBatch];
 #pragma unroll
-        for (int k = 0; k < kBatch; ++k)
-            t[k] = j0 + k < nd ? ld_hint(ybkt + ld_hint(a.loc + dp + j0 + k, stream), stream) : T(0);
+        for (int k = 0; k < kBatch; ++k) t[k] = j0 + k < nd ? ld_hint(ybkt + li[k], stream) : T(0);
         const int lim = __reduce_max_sync(__activemask(), (unsigned)min(kBatch, nd - j0));
 #pragma unroll
         for (int k = 0; k < kBatch; ++k) {

@@ -48,6 +48,13 @@ __device__ __forceinline__ uint32_t ld_hint(const uint32_t* ptr, uint64_t pol) {
     asm("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(r) : "l"(ptr), "l"(pol));
     return r;
 }
+__device__ __forceinline__ int4 ld_hint(const int4* ptr, uint64_t pol) {
+    int4 r;
+    asm("ld.global.nc.L2::cache_hint.v4.s32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+        : "l"(ptr), "l"(pol));
+    return r;
+}
 __device__ __forceinline__ double2 ld_hint(const double2* ptr, uint64_t pol) {
     double2 r;
     asm("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(r.x), "=d"(r.y) : "l"(ptr), "l"(pol));
