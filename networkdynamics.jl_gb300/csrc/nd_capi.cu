@@ -396,6 +396,7 @@ extern "C" {
 
 int nd_create(const nd_network_desc* desc, int dtype, nd_handle** out) {
     clear_error();
+    ND_NVTX("nd_create");
     if (!desc || !out) return fail(ND_ERR_ARG, "nd_create: NULL descriptor or output pointer");
     *out = nullptr;
     if (dtype != ND_F32 && dtype != ND_F64)
@@ -447,6 +448,7 @@ int nd_create(const nd_network_desc* desc, int dtype, nd_handle** out) {
 
 int nd_create_batched(const nd_batched_network_desc* desc, int dtype, nd_handle** out) {
     clear_error();
+    ND_NVTX("nd_create_batched");
     if (!desc || !out) return fail(ND_ERR_ARG, "nd_create_batched: NULL descriptor or output pointer");
     *out = nullptr;
     if (dtype != ND_F32 && dtype != ND_F64)
@@ -524,6 +526,7 @@ int nd_set_layout(nd_handle* h, int layout) {
 
 int nd_rhs(nd_handle* h, int dtype, void* du, int64_t n_du, const void* u, int64_t n_u, const void* p,
            int64_t n_p, double t, void* stream) {
+    ND_NVTX("nd_rhs");
     (void)t;
     clear_error();
     if (!h) return fail(ND_ERR_ARG, "nd_rhs: NULL handle");

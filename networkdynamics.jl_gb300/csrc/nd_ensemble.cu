@@ -719,6 +719,7 @@ int nd_ensemble_get_info(const nd_ensemble* e, int64_t* dim, int64_t* pdim) {
 
 int nd_ensemble_rhs(nd_ensemble* e, int dtype, void* du, const void* u, const void* p, void* stream) {
     clear_error();
+    ND_NVTX("nd_ensemble_rhs");
     if (!e || !du || !u) return fail(ND_ERR_ARG, "nd_ensemble_rhs: NULL argument");
     if (dtype != e->dtype) return fail(ND_ERR_DTYPE, "nd_ensemble_rhs: element type differs from the ensemble's");
     if (e->pdim > 0 && !p) return fail(ND_ERR_ARG, "nd_ensemble_rhs: p is NULL");
@@ -733,6 +734,7 @@ int nd_ensemble_solve_tsit5(nd_ensemble* e, double* u, const void* p, double t0,
                             double abstol, int64_t max_steps, int threads, int32_t* status, int64_t* nsteps,
                             void* stream) {
     clear_error();
+    ND_NVTX("nd_ensemble_solve_tsit5");
     if (!e || !u || !status || !nsteps) return fail(ND_ERR_ARG, "nd_ensemble_solve_tsit5: NULL argument");
     if (!(t1 > t0) || !(reltol > 0) || !(abstol > 0)) return fail(ND_ERR_ARG, "nd_ensemble_solve_tsit5: bad time span or tolerances");
     if (e->pdim > 0 && !p) return fail(ND_ERR_ARG, "nd_ensemble_solve_tsit5: p is NULL");
@@ -796,6 +798,7 @@ int nd_ensemble_set_threads(nd_ensemble* e, int threads) {
 int nd_ensemble_fixpoint(nd_ensemble* e, double* u, const double* p, double tol, int max_newton, int max_cg,
                          int32_t* iters, double* resid, int32_t* status, int32_t* cg_iters, void* stream) {
     clear_error();
+    ND_NVTX("nd_ensemble_fixpoint");
     if (!e || !u || !p || !iters || !resid || !status) return fail(ND_ERR_ARG, "nd_ensemble_fixpoint: NULL argument");
     if (e->vertex_kind != ND_V_SWING)
         return fail(ND_ERR_UNSUPPORTED, "nd_ensemble_fixpoint: steady states are implemented for swing vertices");
@@ -833,6 +836,7 @@ int nd_ensemble_fixpoint(nd_ensemble* e, double* u, const double* p, double tol,
 extern "C" int nd_ensemble_autotune(nd_ensemble* e, const double* u, const void* p, double t0, double t_probe,
                                     double reltol, double abstol, int* chosen, void* stream) {
     clear_error();
+    ND_NVTX("nd_ensemble_autotune");
     if (!e || !u || !chosen) return fail(ND_ERR_ARG, "nd_ensemble_autotune: NULL argument");
     cudaStream_t s = (cudaStream_t)stream;
     double* uc = nullptr;

@@ -7,9 +7,22 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "nd_gb300.h"
 
 namespace nd {
+
+// NVTX range around a C-ABI call: the call shows up by name on a profiler's timeline
+// (Nsight Systems / Compute); without a tool attached a push / pop is a branch on a null
+// function pointer.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+#define ND_NVTX(name) ::nd::NvtxRange nd_nvtx_range_(name)
 
 // Thread-local error message behind nd_last_error().
 void set_error(const std::string& msg);

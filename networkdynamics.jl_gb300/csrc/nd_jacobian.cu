@@ -609,6 +609,7 @@ extern "C" int nd_jacobian_pattern(nd_handle* h, int64_t* nnz, int32_t* rowptr, 
 
 extern "C" int nd_jacobian(nd_handle* h, int dtype, void* values, const void* u, const void* p, double t,
                            void* stream) {
+    ND_NVTX("nd_jacobian");
     (void)t;
     clear_error();
     if (!h || !values || !u) return fail(ND_ERR_ARG, "nd_jacobian: NULL argument");

@@ -133,6 +133,7 @@ using namespace nd;
 
 extern "C" int nd_jvp(nd_handle* h, int dtype, void* jv, const void* u, const void* p, const void* v, double t,
                       void* stream) {
+    ND_NVTX("nd_jvp");
     (void)t;
     clear_error();
     if (!h || !jv || !u || !v) return fail(ND_ERR_ARG, "nd_jvp: NULL argument");

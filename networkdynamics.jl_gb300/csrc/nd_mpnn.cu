@@ -748,6 +748,7 @@ int nd_mpnn_get_grads(const nd_mpnn* m, float* dst, void* stream) {
 }
 
 int nd_mpnn_forward(nd_mpnn* m, int64_t batch, const float* P, const float* K, float* theta, void* stream) {
+    ND_NVTX("nd_mpnn_forward");
     nd::clear_error();
     if (!m || batch <= 0 || !P || (m->ne > 0 && !K) || !theta)
         return nd::fail(ND_ERR_ARG, "nd_mpnn_forward: bad arguments");
@@ -759,6 +760,7 @@ int nd_mpnn_forward(nd_mpnn* m, int64_t batch, const float* P, const float* K, f
 
 int nd_mpnn_loss_grad(nd_mpnn* m, int64_t batch, const float* P, const float* K, const float* theta_star, float* loss,
                       void* stream) {
+    ND_NVTX("nd_mpnn_loss_grad");
     nd::clear_error();
     if (!m || batch <= 0 || !P || (m->ne > 0 && !K) || !theta_star || !loss)
         return nd::fail(ND_ERR_ARG, "nd_mpnn_loss_grad: bad arguments");
@@ -774,6 +776,7 @@ int nd_mpnn_loss_grad(nd_mpnn* m, int64_t batch, const float* P, const float* K,
 }
 
 int nd_mpnn_adam(nd_mpnn* m, double lr, double beta1, double beta2, double eps, void* stream) {
+    ND_NVTX("nd_mpnn_adam");
     nd::clear_error();
     if (!m || !(lr > 0) || !(beta1 >= 0 && beta1 < 1) || !(beta2 >= 0 && beta2 < 1) || !(eps > 0))
         return nd::fail(ND_ERR_ARG, "nd_mpnn_adam: bad arguments");

@@ -275,6 +275,7 @@ using namespace nd;
 extern "C" int nd_find_fixpoint(nd_handle* h, double* u, const double* p, double t, double tol, int max_newton,
                                 int krylov_dim, int max_restarts, int32_t* iters, double* resid, void* stream) {
     clear_error();
+    ND_NVTX("nd_find_fixpoint");
     if (!h || !u || !iters || !resid) return fail(ND_ERR_ARG, "nd_find_fixpoint: NULL argument");
     if (h->dtype != ND_F64) return fail(ND_ERR_DTYPE, "nd_find_fixpoint: FP64 handles only");
     if (h->pdim > 0 && !p) return fail(ND_ERR_ARG, "nd_find_fixpoint: p is NULL");

@@ -100,6 +100,7 @@ extern "C" int nd_solve_rosenbrock23(nd_handle* h, double* u, const double* p, c
                                      double t1, double reltol, double abstol, int64_t max_steps, nd_solve_stats* st,
                                      void* stream) {
     clear_error();
+    ND_NVTX("nd_solve_rosenbrock23");
     if (!h || !u || !st) return fail(ND_ERR_ARG, "nd_solve_rosenbrock23: NULL argument");
     if (h->dtype != ND_F64) return fail(ND_ERR_DTYPE, "nd_solve_rosenbrock23: FP64 handles only");
     if (h->pdim > 0 && !p) return fail(ND_ERR_ARG, "nd_solve_rosenbrock23: p is NULL");

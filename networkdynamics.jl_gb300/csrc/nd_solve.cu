@@ -199,6 +199,7 @@ using namespace nd;
 extern "C" int nd_solve_tsit5(nd_handle* h, double* u, const void* p, double t0, double t1, double reltol,
                               double abstol, int64_t max_steps, nd_solve_stats* stats, void* stream) {
     clear_error();
+    ND_NVTX("nd_solve_tsit5");
     if (!h || !u || !stats) return fail(ND_ERR_ARG, "nd_solve_tsit5: NULL argument");
     if (!(t1 > t0)) return fail(ND_ERR_ARG, "nd_solve_tsit5: t1 must be greater than t0");
     if (!(reltol > 0) || !(abstol > 0)) return fail(ND_ERR_ARG, "nd_solve_tsit5: tolerances must be positive");
