@@ -188,9 +188,22 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 5 : 1) row_phase_kern
         }
     }
     for (int j0 = 0; j0 < ns; j0 += kBatch) {
+        // the source block's values as aligned pairs (y has two padding entries at its end;
+        // a pair may hold the neighbouring row's value, which is not used)
+        using P2 = typename Pair<T>::type;
+        const uint32_t b0 = sp + (uint32_t)j0, off = b0 & 1u;
+        const P2* __restrict__ yp = reinterpret_cast<const P2*>(y + (b0 - off));
+        const int avail = (int)off + ns - j0;  // entries from the pair base to the block end
+        T e[kBatch + 2];
+#pragma unroll
+        for (int k2 = 0; k2 < kBatch / 2 + 1; ++k2) {
+            const P2 v = 2 * k2 < avail ? ld_hint(yp + k2, stream) : P2{T(0), T(0)};
+            e[2 * k2] = v.x;
+            e[2 * k2 + 1] = v.y;
+        }
         T t[kBatch];
 #pragma unroll
-        for (int k = 0; k < kBatch; ++k) t[k] = j0 + k < ns ? ld_hint(y + sp + j0 + k, stream) : T(0);
+        for (int k = 0; k < kBatch; ++k) t[k] = off ? e[k + 1] : e[k];
         const int lim = __reduce_max_sync(__activemask(), (unsigned)min(kBatch, ns - j0));
 #pragma unroll
         for (int k = 0; k < kBatch; ++k) {
