@@ -336,6 +336,26 @@ int nd_rhs_static_scratch(int dtype, int vertex_kind, int edge_kind, int64_t nv,
                           const int32_t* dst, const uint32_t* src_ptr, const uint32_t* dst_ptr,
                           const int32_t* dst_eid, void* du, const void* u, const void* p, void* stream);
 
+/* ---------------------------------------------------------------------------------
+ * External inputs and loopback edges.  No library component reads external inputs or is
+ * an injector with a feed-forward output, so nd_create rejects networks that use them;
+ * a host that keeps its own components calls these two gathers between its component
+ * passes, where the reference's core loop makes the same copies.  Every pointer is a
+ * device pointer; indices are 0-based and must lie inside the buffers (not checked on
+ * the device).  n = 0 launches nothing.  dtype ND_F32 or ND_F64 for all value buffers.
+ * ------------------------------------------------------------------------------- */
+/* extbuf[k] = from_state[k] ? u[idx[k]] : o[idx[k]] for k < n: the ExtMap gather
+ * collect_externals! (src/external_inputs.jl:51-80), one entry per StateBufIdx /
+ * OutBufIdx of the map with the index shifted to 0-based. */
+int nd_collect_externals(int dtype, int64_t n, const int64_t* idx, const uint8_t* from_state, void* extbuf,
+                         const void* u, const void* o, void* stream);
+/* aggbuf[agg_idx[k]] = obuf[out_idx[k]] for k < n: apply_loopback! (src/post_utils.jl:230-248)
+ * on the map of gen_loopback_map (src/post_utils.jl:213-224), the destination vertex's
+ * outputs copied into its source vertex's aggregated inputs.  Repeated agg_idx entries
+ * race (the reference's GPU kernel has the same rule). */
+int nd_apply_loopback(int dtype, int64_t n, const int64_t* out_idx, const int64_t* agg_idx, void* aggbuf,
+                      const void* obuf, void* stream);
+
 
 /* ---------------------------------------------------------------------------------
  * Ensembles: many instances of one vertex / edge model pair on different graphs (the

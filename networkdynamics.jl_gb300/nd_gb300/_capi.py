@@ -234,4 +234,6 @@ SIGNATURES.update({
     "nd_mpnn_adam": (C.c_int, [_vp, _d, _d, _d, _d, _vp]),
     "nd_mpnn_reset_optimizer": (C.c_int, [_vp, _vp]),
     "nd_mpnn_set_hops": (C.c_int, [_vp, C.c_int]),
+    "nd_collect_externals": (C.c_int, [C.c_int, _i64, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "nd_apply_loopback": (C.c_int, [C.c_int, _i64, _vp, _vp, _vp, _vp, _vp]),
 })

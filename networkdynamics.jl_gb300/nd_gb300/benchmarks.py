@@ -1,5 +1,6 @@
 """Secondary GPU benchmarks of the package (the headline RHS benchmark is bench.py).
 
+    python -m nd_gb300.benchmarks rhs       [--nv 10000000 --dtype f64 --calls 8]
     python -m nd_gb300.benchmarks warmstart [--train 20000 --test 2000 --nv 2000]
     python -m nd_gb300.benchmarks ensemble  [--instances 4096]
     python -m nd_gb300.benchmarks swing     [--nv 100000]
@@ -29,6 +30,31 @@ _T0 = time.perf_counter()
 
 def _log(msg):
     print(f"[{time.perf_counter() - _T0:8.1f} s] {msg}", file=sys.stderr, flush=True)
+
+
+def rhs(nv=10_000_000, m=4, dtype="f64", calls=8, seed=1):
+    """A few calls of the diffusion RHS on Barabasi-Albert(nv, m) with the headline
+    benchmark's seeded inputs (u ~ N(0, 1), w ~ U(0, 1)): the short program that per-kernel
+    profiler captures run.  Reports the mean wall time of the calls and a checksum of du."""
+    import torch
+    import nd_gb300 as nd
+    td = {"f64": torch.float64, "f32": torch.float32}[dtype]
+    g = nd.barabasi_albert(nv, m, seed=seed)
+    rng = np.random.default_rng(seed)
+    u_h, w_h = rng.normal(size=g.nv), rng.uniform(0.0, 1.0, size=g.ne)
+    nw = nd.adapt(nd.Network(g, nd.diffusion_vertex(), nd.diffusion_edge()), td)
+    u = torch.from_numpy(u_h).to("cuda", td)
+    p = torch.from_numpy(w_h).to("cuda", td)
+    du = torch.empty_like(u)
+    nw(du, u, p, 0.0)
+    _sync()
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        nw(du, u, p, 0.0)
+    _sync()
+    return {"workload": f"diffusion on Barabasi-Albert N={g.nv}, m={m}, {dtype.upper()} RHS", "ne": g.ne,
+            "calls": calls, "ms_per_call_wall": 1e3 * (time.perf_counter() - t0) / calls,
+            "checksum": float(du.double().sum().item())}
 
 
 def warmstart(n_train=20000, n_test=2000, nv=2000, m=2, layers=4, epochs=80, batch=64, lr=2e-3, lr_final=5e-5,
@@ -326,7 +352,9 @@ def fixpoint(nv=1_000_000, m=2, seed=0):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("which", choices=["warmstart", "ensemble", "swing", "jacobian", "fixpoint"])
+    ap.add_argument("which", choices=["rhs", "warmstart", "ensemble", "swing", "jacobian", "fixpoint"])
+    ap.add_argument("--dtype", choices=["f64", "f32"], default="f64")
+    ap.add_argument("--calls", type=int, default=8)
     ap.add_argument("--train", type=int, default=20000)
     ap.add_argument("--test", type=int, default=2000)
     ap.add_argument("--nv", type=int, default=None)
@@ -335,7 +363,9 @@ def main():
     ap.add_argument("--sample", type=int, default=16)
     ap.add_argument("--t-end", type=float, default=50.0)
     a = ap.parse_args()
-    if a.which == "warmstart":
+    if a.which == "rhs":
+        r = rhs(a.nv or 10_000_000, dtype=a.dtype, calls=a.calls)
+    elif a.which == "warmstart":
         r = warmstart(a.train, a.test, a.nv or 2000, epochs=a.epochs)
     elif a.which == "ensemble":
         r = ensemble(a.instances, baseline_sample=a.sample, t_end=a.t_end)

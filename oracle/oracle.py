@@ -10,6 +10,8 @@ Python side of the CPU oracle:
   SequentialAggregator's order.
 * ``newton_fixpoint`` — dense Newton on the swing/Kuramoto steady state, the restated
   find_fixpoint (src/initialization.jl:44-144) for small networks.
+* ``collect_externals`` / ``gen_loopback_map`` / ``apply_loopback`` — the external-input
+  and loopback copies of the core loop (src/external_inputs.jl, src/post_utils.jl).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline use this module.
 """
@@ -525,3 +527,34 @@ def newton_fixpoint(nv, src, dst, K, P, theta0=None, tol=1e-10, maxiter=50):
         it += 1
         res = np.max(np.abs(swing_residual_theta(th, src, dst, K, P)))
     return th, it, res
+
+
+def collect_externals(from_state, idx, u, o):
+    """The ExtMap gather collect_externals! (src/external_inputs.jl:51-64, CPU loop):
+    entry k reads u[idx[k]] for a StateBufIdx, o[idx[k]] for an OutBufIdx.  0-based."""
+    ext = np.empty(len(idx), dtype=np.result_type(u, o))
+    for k, (st, i) in enumerate(zip(from_state, idx)):
+        ext[k] = u[i] if st else o[i]
+    return ext
+
+
+def gen_loopback_map(src, dst, loopback, v_out, v_aggr):
+    """gen_loopback_map (src/post_utils.jl:213-224): for each loopback edge in edge order,
+    the destination vertex's output indices and the source vertex's aggregation indices,
+    appended range by range.  v_out[v] / v_aggr[v] are index sequences (0-based)."""
+    out_idx, agg_idx = [], []
+    for e in range(len(src)):
+        if not loopback[e]:
+            continue
+        out_idx.extend(v_out[dst[e]])
+        agg_idx.extend(v_aggr[src[e]])
+    return np.asarray(out_idx, dtype=np.int64), np.asarray(agg_idx, dtype=np.int64)
+
+
+def apply_loopback(aggbuf, obuf, out_idx, agg_idx):
+    """_apply_loopback! on the CPU (src/post_utils.jl:230-236): aggbuf[agg] = obuf[out] in
+    map order (a later entry wins where agg repeats)."""
+    agg = np.array(aggbuf, copy=True)
+    for oi, ai in zip(out_idx, agg_idx):
+        agg[ai] = obuf[oi]
+    return agg

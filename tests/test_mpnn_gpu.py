@@ -105,10 +105,13 @@ def test_bad_arguments_raise(cuda):
 
 def test_warm_start_gain(cuda):
     """What the trained network gains over the plain cold start θ = 0 on held-out
-    instances: a much closer initial guess, every warm-started Newton solve converging to
-    1e-10 without the cold-start fallback, no more Newton iterations and fewer conjugate-
-    gradient iterations.  (The cold start already needs only ~3 Newton iterations on these
-    lightly loaded networks, so the iteration count itself cannot drop much.)"""
+    instances of this small training run (BA(300, 2), 1536 instances, 40 epochs; measured
+    on a GB300: prediction error 0.05 rad, Newton iterations 3.0 -> 3.0, CG iterations
+    185 -> 168): a much closer initial guess, every warm-started Newton solve converging to
+    1e-10 without the cold-start fallback, no more Newton iterations and at least 5 % fewer
+    conjugate-gradient iterations.  The full benchmark (BA(2000, 2), 20,000 instances,
+    80 epochs) reaches 3.00 -> 2.04 Newton iterations; one Newton iteration would need a
+    prediction within ~1e-5 rad, which a 4-hop network cannot give."""
     g = nd.barabasi_albert(300, 2, seed=5)
     P, K = W.swing_instances(g, 1536 + 128, 5)
     train = W.fixpoints(g, P[:1536], K[:1536], tol=1e-10)
@@ -123,4 +126,4 @@ def test_warm_start_gain(cuda):
     zero_err = np.abs(cold_th - cold_th.mean(axis=1, keepdims=True)).max(axis=1).mean()
     assert res["prediction_max_abs_err"]["mean"] < 0.5 * zero_err
     assert res["warm"]["newton_iters_mean"] <= res["cold"]["newton_iters_mean"]
-    assert res["warm"]["cg_iters_mean"] < res["cold"]["cg_iters_mean"]
+    assert res["cg_iter_ratio"] >= 1.05

@@ -297,3 +297,25 @@ def test_non_canonical_edge_list_uses_fused_path(cuda):
         on = O.OracleNetwork.from_graph(g, vk, ek)
         u, p = random_inputs(on, vk, rng)
         check_f64(gpu_rhs(nw, u, p, cuda, np.float64), on.rhs(u, p), on.abs_terms(u, p), exact=ek != O.E_KURAMOTO)
+
+
+def test_edge_phase_sources_of_sparse_and_dense_chunks(cuda):
+    """Edge chunks of very different shape: one 2048-edge chunk whose sources lie 12
+    vertices apart (spanning ~18,000 vertices, one edge each) and dense chunks of 2-4 edges
+    per source with empty source blocks in between.  Both give the oracle's bits."""
+    rng = np.random.default_rng(23)
+    nv = 40_000
+    pairs = set()
+    for i in range(1500):  # sources 0, 12, 24, ...: one chunk spans ~18,000 vertices
+        pairs.add((12 * i, 39_000 + (i % 1000)))
+    for s in range(20_000, 24_000):  # dense region: 2-4 edges per source, some sources empty
+        if s % 7 == 0:
+            continue
+        for d in rng.choice(np.arange(s + 1, nv), size=rng.integers(2, 5), replace=False):
+            pairs.add((s, int(d)))
+    arr = np.array(sorted(pairs), dtype=np.int64)
+    g = nd.Graph(nv, np.ascontiguousarray(arr[:, 0]), np.ascontiguousarray(arr[:, 1]))
+    nw = make(g, O.V_DIFFUSION, O.E_DIFFUSION, np.float64)
+    on = O.OracleNetwork.from_graph(g, O.V_DIFFUSION, O.E_DIFFUSION)
+    u, p = random_inputs(on, O.V_DIFFUSION, rng)
+    np.testing.assert_array_equal(gpu_rhs(nw, u, p, cuda, np.float64), on.rhs(u, p))
