@@ -414,6 +414,10 @@ def run_gb300(args, rank, world, local):
                        "achieved_gbs": B32 / (t32 / args.steps) / 1e9,
                        "frac": B32 / (t32 / args.steps) / 1e9 / hbm, "max_abs_err_vs_f64": err,
                        "kernels_avg_ms": {k: tot / n for k, (n, tot) in kt32.items() if n}}
+        traffic32 = profiled_traffic("f32", nv)
+        if traffic32:
+            line["f32"].update({"traffic": traffic32["total"], "traffic_per_kernel": traffic32["kernels"],
+                                "traffic_source": traffic32["source"]})
         del nw32, u32, p32, du32
     # end to end through the public API with pinned host buffers: every step copies its
     # inputs (u, p) host->device and its result du device->host.  Two buffer sets and
