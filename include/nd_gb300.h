@@ -38,7 +38,8 @@ enum nd_status {
     ND_ERR_MAXITERS = -5,              /* a solver hit its step / iteration budget         */
     ND_ERR_UNSUPPORTED = -6,           /* feature outside the GB300 path (perturb, RET...) */
     ND_ERR_NOMEM = -7,                 /* device allocation failed                         */
-    ND_ERR_NOT_CONVERGED = -8          /* Newton / fixpoint did not reach the tolerance    */
+    ND_ERR_NOT_CONVERGED = -8,         /* Newton / fixpoint did not reach the tolerance    */
+    ND_ERR_DEVICE_CHECK = -9           /* a device-side check found a bad index (checks on) */
 };
 
 /* Element type of caller buffers.  A handle is built for one of them, like
@@ -335,6 +336,18 @@ int nd_solve_rosenbrock23(nd_handle* h, double* u, const double* p, const double
 int nd_rhs_static_scratch(int dtype, int vertex_kind, int edge_kind, int64_t nv, int64_t ne, const int32_t* src,
                           const int32_t* dst, const uint32_t* src_ptr, const uint32_t* dst_ptr,
                           const int32_t* dst_eid, void* du, const void* u, const void* p, void* stream);
+/* Device-side checks of the topology arrays that nd_rhs_static_scratch reads (the entry
+ * point whose device indices no host code validates; nd_create checks its input on the
+ * host).  With checks on (process-wide; default off), its kernels test every index they
+ * read from src, dst, src_ptr, dst_ptr and dst_eid before using it, and the list's
+ * canonical order (src ascending, src < dst, each source block holding its vertex's
+ * edges, each destination list ascending and holding its vertex's edges).  An index out of
+ * range is not dereferenced (its term counts as zero).  The first finding is kept on the
+ * device; the call then synchronises its stream, reads it back and returns
+ * ND_ERR_DEVICE_CHECK, with the array, position and value in nd_last_error().  Nothing
+ * traps, and the context stays usable.  A checked call synchronises, so it cannot be
+ * captured into a graph. */
+int nd_set_device_checks(int on);
 
 /* ---------------------------------------------------------------------------------
  * External inputs and loopback edges.  No library component reads external inputs or is

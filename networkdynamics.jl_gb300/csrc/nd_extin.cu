@@ -47,6 +47,7 @@ using namespace nd;
 extern "C" int nd_collect_externals(int dtype, int64_t n, const int64_t* idx, const uint8_t* from_state, void* extbuf,
                                     const void* u, const void* o, void* stream) {
     clear_error();
+    ND_NVTX("nd_collect_externals");
     if (dtype != ND_F32 && dtype != ND_F64) return fail(ND_ERR_DTYPE, "nd_collect_externals: dtype must be ND_F32 or ND_F64");
     if (n < 0) return fail(ND_ERR_ARG, "nd_collect_externals: negative length");
     if (n == 0) return ND_OK;
@@ -65,6 +66,7 @@ extern "C" int nd_collect_externals(int dtype, int64_t n, const int64_t* idx, co
 extern "C" int nd_apply_loopback(int dtype, int64_t n, const int64_t* out_idx, const int64_t* agg_idx, void* aggbuf,
                                  const void* obuf, void* stream) {
     clear_error();
+    ND_NVTX("nd_apply_loopback");
     if (dtype != ND_F32 && dtype != ND_F64) return fail(ND_ERR_DTYPE, "nd_apply_loopback: dtype must be ND_F32 or ND_F64");
     if (n < 0) return fail(ND_ERR_ARG, "nd_apply_loopback: negative length");
     if (n == 0) return ND_OK;

@@ -19,6 +19,7 @@ ND_ERR_MAXITERS = -5
 ND_ERR_UNSUPPORTED = -6
 ND_ERR_NOMEM = -7
 ND_ERR_NOT_CONVERGED = -8
+ND_ERR_DEVICE_CHECK = -9
 
 ND_F32 = 1
 ND_F64 = 2
@@ -163,7 +164,7 @@ def check(code: int) -> int:
     msg = last_error()
     if code == ND_ERR_UNSUPPORTED_COMPONENT:
         raise UnsupportedComponentError(code, msg)
-    if code in (ND_ERR_ARG, ND_ERR_DTYPE, ND_ERR_UNSUPPORTED):
+    if code in (ND_ERR_ARG, ND_ERR_DTYPE, ND_ERR_UNSUPPORTED, ND_ERR_DEVICE_CHECK):
         raise ArgumentError(code, msg)
     if code in (ND_ERR_NOT_CONVERGED, ND_ERR_MAXITERS):
         raise NotConvergedError(code, msg)
@@ -234,6 +235,7 @@ SIGNATURES.update({
     "nd_mpnn_adam": (C.c_int, [_vp, _d, _d, _d, _d, _vp]),
     "nd_mpnn_reset_optimizer": (C.c_int, [_vp, _vp]),
     "nd_mpnn_set_hops": (C.c_int, [_vp, C.c_int]),
+    "nd_set_device_checks": (C.c_int, [C.c_int]),
     "nd_collect_externals": (C.c_int, [C.c_int, _i64, _vp, _vp, _vp, _vp, _vp, _vp]),
     "nd_apply_loopback": (C.c_int, [C.c_int, _i64, _vp, _vp, _vp, _vp, _vp]),
 })

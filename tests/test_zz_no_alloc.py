@@ -98,9 +98,10 @@ def test_static_scratch_rejects_oversized_networks(cuda):
 
 @pytest.mark.gpu
 def test_static_scratch_with_a_non_canonical_order(cuda):
-    """Arrays that are not the canonical sort are not detected (they live on the device);
-    the result is still the network's RHS, summed in the arrays' order: equal to nd_rhs
-    within the rounding of a reordered FP64 sum, not bit for bit."""
+    """With device checks off (the default), arrays that are not the canonical sort are not
+    detected (they live on the device); the result is still the network's RHS, summed in
+    the arrays' order: equal to nd_rhs within the rounding of a reordered FP64 sum, not bit
+    for bit."""
     import torch
     lib = capi.load()
     g = nd.barabasi_albert(50_000, 4, seed=43)
@@ -122,3 +123,62 @@ def test_static_scratch_with_a_non_canonical_order(cuda):
     capi.check(static_rhs(lib, O.V_DIFFUSION, O.E_DIFFUSION, g, dev_arrays, got, u, p, capi.ND_F64))
     d = np.abs(got.cpu().numpy() - ref.cpu().numpy())
     assert np.all(d <= 1e-13 * on.abs_terms(u_h, p_h))
+
+
+@pytest.mark.gpu
+def test_device_checks_report_non_canonical_arrays(cuda):
+    """nd_set_device_checks(1): a canonical list gives the bits of the unchecked call; the
+    reversed destination lists above, and an edge whose endpoints are swapped (src > dst),
+    come back as ND_ERR_DEVICE_CHECK naming the finding and its position, and the next
+    call on the same context succeeds.  Every input here is in range: the checks' range
+    tests (an out-of-range index is skipped and reported) are not exercised on the GPU."""
+    import torch
+    lib = capi.load()
+    assert lib.nd_set_device_checks(2) == capi.ND_ERR_ARG
+    g = nd.barabasi_albert(20_000, 3, seed=44)
+    on = O.OracleNetwork.from_graph(g, O.V_DIFFUSION, O.E_DIFFUSION)
+    u_h, p_h = random_inputs(on, O.V_DIFFUSION, np.random.default_rng(3))
+    u = torch.from_numpy(u_h).to(cuda)
+    p = torch.from_numpy(p_h).to(cuda)
+
+    def arrays(src, dst, dst_eid=None):
+        gg = nd.Graph(g.nv, src, dst) if dst_eid is None else g
+        sp, dp, de = csr_arrays(gg)
+        if dst_eid is not None:
+            de = dst_eid
+        return [torch.from_numpy(np.ascontiguousarray(x)).to(cuda) for x in
+                (src.astype(np.int32), dst.astype(np.int32), sp.view(np.int32), dp.view(np.int32), de)]
+
+    def run(dev_arrays):
+        out = torch.empty_like(u)
+        return static_rhs(lib, O.V_DIFFUSION, O.E_DIFFUSION, g, dev_arrays, out, u, p, capi.ND_F64), out
+
+    canonical = arrays(g.src, g.dst)
+    code, plain = run(canonical)
+    assert code == capi.ND_OK
+    _, dp, de = csr_arrays(g)
+    for v in range(g.nv):
+        a, b = int(dp[v]), int(dp[v + 1])
+        de[a:b] = de[a:b][::-1]
+    src_sw, dst_sw = g.src.copy(), g.dst.copy()
+    k = int(np.nonzero(np.diff(g.src) > 0)[0][100]) + 1  # first edge of a source block
+    src_sw[k], dst_sw[k] = g.dst[k], g.src[k]
+    lib.nd_set_device_checks(1)
+    try:
+        code, got = run(canonical)
+        assert code == capi.ND_OK
+        np.testing.assert_array_equal(got.cpu().numpy(), plain.cpu().numpy())
+        code, _ = run(arrays(g.src, g.dst, de))
+        assert code == capi.ND_ERR_DEVICE_CHECK
+        assert "dst_eid not ascending" in capi.last_error()
+        code, _ = run(arrays(src_sw, dst_sw))
+        assert code == capi.ND_ERR_DEVICE_CHECK
+        msg = capi.last_error()
+        assert "device check" in msg and ("not canonical" in msg or "source block" in msg), msg
+        code, got = run(canonical)
+        assert code == capi.ND_OK
+        np.testing.assert_array_equal(got.cpu().numpy(), plain.cpu().numpy())
+    finally:
+        lib.nd_set_device_checks(0)
+    with pytest.raises(nd.ArgumentError):
+        capi.check(capi.ND_ERR_DEVICE_CHECK)
