@@ -124,9 +124,11 @@ __global__ void __launch_bounds__(kBlock) edge_phase_kernel(RhsArgs a) {
 //         start folded into the first term (0 + t is t, and both zeros give +0);
 //   FP32  the same order with Kahan compensation on rows longer than kLightMaxDeg.
 template <typename T, int VK>
-// FP32 rows run best with 5 blocks per SM (registers capped at 48), FP64 rows with the 52
-// registers they take at 4 blocks (A/B on BA(1e7, 4): 256 / 288 µs FP32, 346 / 327 µs FP64).
-__global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 5 : 1) row_phase_kernel(RhsArgs a) {
+// 5 blocks per SM (registers capped at 48) in both precisions.  A/B on BA(1e7, 4), FP64:
+// 327 µs against 349 µs at the 64 registers the kernel takes uncapped (4 blocks), 374-390 µs
+// with 8-term batches at 5-6 blocks, 351 µs with 16-term batches at 4; FP32: 252 µs against
+// 309-451 µs with 8-term batches at 6-8 blocks.
+__global__ void __launch_bounds__(kBlock, 5) row_phase_kernel(RhsArgs a) {
     using A = Arith<T>;
     constexpr int kBatch = 12;
     const int64_t slot = (int64_t)a.n_heavy + (int64_t)blockIdx.x * kBlock + threadIdx.x;
