@@ -337,7 +337,12 @@ static int new_handle(int dtype, nd_handle** out) {
     h->sum_order = ND_ORDER_SEQUENTIAL;
     h->rhs_mode = kModeExact;
     h->edge_path = 1;
-    if (cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess ||
+    // FP64 heavy rows run on a high-priority side stream, so that their blocks take the first
+    // SM slots that edge-phase blocks free (see launch_heavy_solo in nd_rhs.cu)
+    int prio_lo = 0, prio_hi = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    if (cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, dtype == ND_F64 ? prio_hi : prio_lo) !=
+            cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess) {
         cudaError_t err = cudaGetLastError();

@@ -196,18 +196,18 @@ __global__ void __launch_bounds__(kBlock, 8) rhs_kernel(RhsArgs a) {
     }
 }
 
-// Heavy rows alone, a block per row on an SM of its own (the dynamic shared memory request
-// keeps other blocks off the SM): the row's summation chain is serial, and on an SM
-// shared with other blocks each of its steps waits for their instructions.
+// Heavy rows alone, a block per row.  The FP32 and tree rows ask for most of an SM's shared
+// memory, which keeps all but four other blocks off the SM: the row's summation chain is
+// serial, and on a crowded SM each of its steps waits for other blocks' instructions.
 constexpr int kHeavySoloSmem = 160 * 1024;
 
-// FP64 sequential sum of a heavy row in the solo kernel: warp 0 adds tile k of the row's
-// terms (exact scan, or the hardware DADD chain in the native mode) while warps 1..7
-// evaluate tile k + 1 into the other half of a double buffer, so the serial chain never
-// waits for its terms after the first tile.
+// FP64 sequential sum of a heavy row in the solo kernel, in tiles of TILE terms: warp 0
+// adds tile k of the row's terms (exact scan, or the hardware DADD chain in the native
+// mode) while warps 1..7 evaluate tile k + 1 into the other half of a double buffer, so the
+// serial chain never waits for its terms after the first tile.
 constexpr int kSoloTile = 8192;
 
-template <int VK, int EK, int MODE>
+template <int VK, int EK, int MODE, int TILE>
 __device__ __forceinline__ void solo_row_fp64(const RhsArgs& a, int slot, double* buf) {
     constexpr int DV = VertexDims<VK>::dim;
     const double* __restrict__ u = static_cast<const double*>(a.u);
@@ -219,11 +219,11 @@ __device__ __forceinline__ void solo_row_fp64(const RhsArgs& a, int slot, double
     const uint32_t beg = __ldg(a.slot_ptr + slot), end = __ldg(a.slot_ptr + slot + 1);
     const double uv = __ldg(u + v * DV);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int ntiles = (int)((end - beg + kSoloTile - 1) / kSoloTile);
+    const int ntiles = (int)((end - beg + TILE - 1) / TILE);
     auto load = [&](int k, int first, int stride) {
-        const uint32_t base = beg + (uint32_t)k * kSoloTile;
-        const int n = (int)min((uint32_t)kSoloTile, end - base);
-        double* dst = buf + (k & 1) * kSoloTile;
+        const uint32_t base = beg + (uint32_t)k * TILE;
+        const int n = (int)min((uint32_t)TILE, end - base);
+        double* dst = buf + (k & 1) * TILE;
 #pragma unroll 4
         for (int i = first; i < n; i += stride) {
             const int2 inc = ld_hint(incid + base + i, stream);
@@ -237,8 +237,8 @@ __device__ __forceinline__ void solo_row_fp64(const RhsArgs& a, int slot, double
     double S = 0.0;
     for (int k = 0; k < ntiles; ++k) {
         if (warp == 0) {
-            const double* cur = buf + (k & 1) * kSoloTile;
-            const int n = (int)min((uint32_t)kSoloTile, end - (beg + (uint32_t)k * kSoloTile));
+            const double* cur = buf + (k & 1) * TILE;
+            const int n = (int)min((uint32_t)TILE, end - (beg + (uint32_t)k * TILE));
             if constexpr (MODE == kModeNative) {
                 if (lane == 0)
                     for (int i = 0; i < n; ++i) S = __dadd_rn(S, cur[i]);
@@ -253,28 +253,48 @@ __device__ __forceinline__ void solo_row_fp64(const RhsArgs& a, int slot, double
     if (tid == 0) vertex_f<double, VK>(static_cast<double*>(a.du), u, p, v, S);
 }
 
-template <typename T, int VK, int EK, int MODE>
+template <typename T, int VK, int EK, int MODE, int TILE>
 __global__ void __launch_bounds__(kBlock, 1) heavy_solo_kernel(RhsArgs a) {
     extern __shared__ __align__(16) unsigned char smem_dyn[];
     if constexpr (sizeof(T) == 8 && MODE != kModeTree) {
-        static_assert(2 * kSoloTile * sizeof(double) <= kHeavySoloSmem, "solo double buffer");
-        solo_row_fp64<VK, EK, MODE>(a, blockIdx.x, reinterpret_cast<double*>(smem_dyn));
+        static_assert(2 * TILE * sizeof(double) <= kHeavySoloSmem, "solo double buffer");
+        solo_row_fp64<VK, EK, MODE, TILE>(a, blockIdx.x, reinterpret_cast<double*>(smem_dyn));
     } else {
         block_row<T, VK, EK, MODE>(a, blockIdx.x, smem_dyn);
     }
 }
 
+template <typename T, int VK, int EK, int MODE, int TILE>
+cudaError_t launch_heavy_solo_t(const RhsArgs& a, cudaStream_t s, int smem) {
+    static int attr_set = 0;  // per instantiation; the attribute is per function
+    if (attr_set < smem) {
+        cudaError_t err = cudaFuncSetAttribute(heavy_solo_kernel<T, VK, EK, MODE, TILE>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (err != cudaSuccess) return err;
+        attr_set = smem;
+    }
+    heavy_solo_kernel<T, VK, EK, MODE, TILE><<<a.n_heavy, kBlock, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+// The FP64 sequential sums (exact scan and hardware chains) use tiles of kSoloTileShared
+// terms: 32 KB of shared memory, so that a heavy-row block also fits on an SM that already
+// holds seven edge-phase blocks.  With the whole-SM request a heavy block could start only
+// on an SM holding at most four, and when the edge phase had filled the GPU first the heavy
+// rows waited for its end and outlasted the row phase: stretches of calls at 776-793 µs
+// instead of 755 µs on BA(1e7, 4).  With the small tiles and the handle's high-priority
+// side stream (FP64 handles) the step took 747-753 µs in every stretch.  The FP32 and tree
+// heavy rows keep the whole-SM request: with small tiles they took 515 µs against 476 µs.
+constexpr int kSoloTileShared = 2048;
+
 template <typename T, int VK, int EK, int MODE>
 cudaError_t launch_heavy_solo(const RhsArgs& a, cudaStream_t s) {
-    static bool attr_set = false;  // per instantiation; the attribute is per function
-    if (!attr_set) {
-        cudaError_t err = cudaFuncSetAttribute(heavy_solo_kernel<T, VK, EK, MODE>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, kHeavySoloSmem);
-        if (err != cudaSuccess) return err;
-        attr_set = true;
+    if constexpr (sizeof(T) == 8 && MODE != kModeTree) {
+        constexpr int smem = (int)(2 * kSoloTileShared * sizeof(double));
+        return launch_heavy_solo_t<T, VK, EK, MODE, kSoloTileShared>(a, s, smem);
+    } else {
+        return launch_heavy_solo_t<T, VK, EK, MODE, kSoloTile>(a, s, kHeavySoloSmem);
     }
-    heavy_solo_kernel<T, VK, EK, MODE><<<a.n_heavy, kBlock, kHeavySoloSmem, s>>>(a);
-    return cudaGetLastError();
 }
 
 template <typename T, int VK, int EK>
