@@ -410,6 +410,19 @@ int nd_ensemble_solve_tsit5(nd_ensemble* e, double* u, const void* p, double t0,
                             double abstol, int64_t max_steps, int threads, int32_t* status, int64_t* nsteps,
                             void* stream);
 
+/* nd_ensemble_solve_tsit5 with a snapshot of the step control (no reference counterpart:
+ * the reference hands the integrator to OrdinaryDiffEq, whose integrator state is
+ * serialised with Julia's Serialization, benchmark/benchmarks.jl:162-167).  control: NULL,
+ * or a device array of 3 doubles per instance, (t, dt, qold) = the time reached, the next
+ * step size the controller proposed and its error history, written when each instance
+ * ends.  resume != 0 starts every instance from the control array's dt and qold (dt
+ * clipped to t1 - t0) instead of the initial-step heuristic, so that a long solve can be
+ * split at a snapshot time t_s: solve to t_s, save u and control, and later solve from
+ * t_s with resume = 1.  Stream-ordered like nd_ensemble_solve_tsit5. */
+int nd_ensemble_solve_tsit5_ex(nd_ensemble* e, double* u, const void* p, double t0, double t1, double reltol,
+                               double abstol, int64_t max_steps, int threads, int32_t* status, int64_t* nsteps,
+                               double* control, int resume, void* stream);
+
 /* Autotuner: times a short solve (t0 .. t0 + t_probe) with each block size on a copy of
  * u and keeps the fastest for threads = 0.  Synchronous. */
 int nd_ensemble_autotune(nd_ensemble* e, const double* u, const void* p, double t0, double t_probe, double reltol,

@@ -258,6 +258,10 @@ struct SolveParams {
     double t0, t1, reltol, abstol;
     int64_t max_steps;
     int64_t dim;  // packed dim (stride of the stage vectors)
+    // per instance (t, dt, qold) written at the end of the solve (NULL: none); with resume,
+    // read at the start instead of the initial-step heuristic
+    double* control;
+    int resume;
 };
 
 template <typename T, int VK, int EK>
@@ -311,6 +315,11 @@ __global__ void ens_tsit5_kernel(EnsArgs a, SolveParams sp, double* __restrict__
             sh_dt = fmin(fmin(100 * h0, h1), sp.t1 - sp.t0);
             sh_t = sp.t0;
             sh_qold = 1e-4;
+            if (sp.control && sp.resume) {  // continue with the step size and error history of a snapshot
+                const double dt = sp.control[3 * i + 1], qold = sp.control[3 * i + 2];
+                if (dt > 0.0 && dt < INFINITY) sh_dt = fmin(dt, sp.t1 - sp.t0);
+                if (qold > 0.0 && qold < INFINITY) sh_qold = qold;
+            }
             sh_done = 0;
             sh_status = ND_OK;
             sh_steps = 0;
@@ -380,6 +389,11 @@ __global__ void ens_tsit5_kernel(EnsArgs a, SolveParams sp, double* __restrict__
         if (threadIdx.x == 0) {
             status[i] = sh_status;
             nsteps[i] = sh_steps;
+            if (sp.control) {
+                sp.control[3 * i] = sh_t;
+                sp.control[3 * i + 1] = sh_dt;
+                sp.control[3 * i + 2] = sh_qold;
+            }
         }
     }
 }
@@ -733,8 +747,16 @@ int nd_ensemble_rhs(nd_ensemble* e, int dtype, void* du, const void* u, const vo
 int nd_ensemble_solve_tsit5(nd_ensemble* e, double* u, const void* p, double t0, double t1, double reltol,
                             double abstol, int64_t max_steps, int threads, int32_t* status, int64_t* nsteps,
                             void* stream) {
+    return nd_ensemble_solve_tsit5_ex(e, u, p, t0, t1, reltol, abstol, max_steps, threads, status, nsteps, nullptr, 0,
+                                      stream);
+}
+
+int nd_ensemble_solve_tsit5_ex(nd_ensemble* e, double* u, const void* p, double t0, double t1, double reltol,
+                               double abstol, int64_t max_steps, int threads, int32_t* status, int64_t* nsteps,
+                               double* control, int resume, void* stream) {
     clear_error();
     ND_NVTX("nd_ensemble_solve_tsit5");
+    if (resume && !control) return fail(ND_ERR_ARG, "nd_ensemble_solve_tsit5_ex: resume needs the control array");
     if (!e || !u || !status || !nsteps) return fail(ND_ERR_ARG, "nd_ensemble_solve_tsit5: NULL argument");
     if (!(t1 > t0) || !(reltol > 0) || !(abstol > 0)) return fail(ND_ERR_ARG, "nd_ensemble_solve_tsit5: bad time span or tolerances");
     if (e->pdim > 0 && !p) return fail(ND_ERR_ARG, "nd_ensemble_solve_tsit5: p is NULL");
@@ -754,7 +776,8 @@ int nd_ensemble_solve_tsit5(nd_ensemble* e, double* u, const void* p, double t0,
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device);
     const int blocks = (int)std::min<int64_t>(e->n_inst, (int64_t)sms * std::max(1, per_sm));
-    SolveParams sp{t0, t1, reltol, abstol, max_steps > 0 ? max_steps : (int64_t)ND_ENSEMBLE_DEFAULT_MAX_STEPS, e->dim};
+    SolveParams sp{t0,     t1,     reltol,   abstol, max_steps > 0 ? max_steps : (int64_t)ND_ENSEMBLE_DEFAULT_MAX_STEPS,
+                   e->dim, control, resume ? 1 : 0};
     const EnsArgs a = args_of(e);
     // The persistent kernel (and the reset of its work queue) run as one captured graph.
     cudaStream_t s = (cudaStream_t)stream;

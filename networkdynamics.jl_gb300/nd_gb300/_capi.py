@@ -220,6 +220,8 @@ SIGNATURES.update({
     "nd_ensemble_get_info": (C.c_int, [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "nd_ensemble_rhs": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp]),
     "nd_ensemble_solve_tsit5": (C.c_int, [_vp, _vp, _vp, _d, _d, _d, _d, _i64, C.c_int, _vp, _vp, _vp]),
+    "nd_ensemble_solve_tsit5_ex": (C.c_int, [_vp, _vp, _vp, _d, _d, _d, _d, _i64, C.c_int, _vp, _vp, _vp, C.c_int,
+                                             _vp]),
     "nd_ensemble_autotune": (C.c_int, [_vp, _vp, _vp, _d, _d, _d, _d, C.POINTER(C.c_int), _vp]),
     "nd_ensemble_set_threads": (C.c_int, [_vp, C.c_int]),
     "nd_ensemble_fixpoint": (C.c_int, [_vp, _vp, _vp, _d, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),

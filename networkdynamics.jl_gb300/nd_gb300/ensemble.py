@@ -29,6 +29,40 @@ class EnsembleSolveResult:
     u: object          # packed FP64 CUDA tensor
     status: np.ndarray  # per instance nd_status
     nsteps: np.ndarray  # per instance steps
+    control: object = None  # per instance (t, dt, qold), FP64 CUDA tensor [n, 3] (snapshot solves)
+
+    def save_snapshot(self, directory) -> None:
+        """Write the state and step control as .npy files (u, control, status, nsteps), to
+        continue the solve later with ``Ensemble.solve_tsit5(..., snapshot=load_snapshot(dir))``."""
+        from pathlib import Path
+        if self.control is None:
+            raise capi.ArgumentError(capi.ND_ERR_ARG, "solve with snapshot=True to record the step control")
+        d = Path(directory)
+        d.mkdir(parents=True, exist_ok=True)
+        np.save(d / "u.npy", self.u.cpu().numpy())
+        np.save(d / "control.npy", self.control.cpu().numpy())
+        np.save(d / "status.npy", _host(self.status))
+        np.save(d / "nsteps.npy", _host(self.nsteps))
+
+
+@dataclass
+class EnsembleSnapshot:
+    u: np.ndarray        # packed FP64 state at the snapshot time
+    control: np.ndarray  # [n, 3]: time reached, next step size, error history
+
+    @property
+    def t(self) -> float:
+        return float(self.control[:, 0].min()) if len(self.control) else 0.0
+
+
+def load_snapshot(directory) -> EnsembleSnapshot:
+    from pathlib import Path
+    d = Path(directory)
+    return EnsembleSnapshot(np.load(d / "u.npy"), np.load(d / "control.npy"))
+
+
+def _host(x):
+    return x.cpu().numpy() if hasattr(x, "cpu") else np.asarray(x)
 
 
 @dataclass
@@ -96,27 +130,62 @@ class Ensemble:
         capi.check(self._lib.nd_ensemble_rhs(self._h, self.dtype_code, du.data_ptr(), u.data_ptr(),
                                              p.data_ptr() if p is not None else None, self._stream(stream)))
 
-    def solve_tsit5(self, u0, p, tspan, reltol=1e-6, abstol=1e-8, max_steps=0, threads=0, stream=None):
+    def solve_tsit5(self, u0, p, tspan, reltol=1e-6, abstol=1e-8, max_steps=0, threads=0, stream=None,
+                    snapshot=False):
         """Tsit5 of every instance over tspan.  max_steps is the per-instance step budget;
         0 means capi.ND_ENSEMBLE_DEFAULT_MAX_STEPS (1e5, SciML's default maxiters).  An
-        instance that runs out gets status ND_ERR_MAXITERS."""
+        instance that runs out gets status ND_ERR_MAXITERS.
+
+        snapshot=True records each instance's step control (result.control) so that the
+        result can be saved and continued; snapshot=<EnsembleSnapshot> (from
+        load_snapshot) continues a saved solve: u0 defaults to the snapshot's state, and
+        every instance starts with the snapshot's step size and error history instead of
+        the initial-step heuristic."""
         import torch
+        resume = isinstance(snapshot, EnsembleSnapshot)
+        if resume and u0 is None:
+            u0 = snapshot.u
         u = u0.to(torch.float64).clone() if isinstance(u0, torch.Tensor) else torch.tensor(u0, dtype=torch.float64,
                                                                                            device="cuda")
         dev = u.device
         status = torch.zeros(self.n, dtype=torch.int32, device=dev)
         nsteps = torch.zeros(self.n, dtype=torch.int64, device=dev)
-        capi.check(self._lib.nd_ensemble_solve_tsit5(self._h, u.data_ptr(), p.data_ptr() if p is not None else None,
-                                                     float(tspan[0]), float(tspan[1]), float(reltol), float(abstol),
-                                                     int(max_steps), int(threads), status.data_ptr(),
-                                                     nsteps.data_ptr(), self._stream(stream)))
-        return EnsembleSolveResult(u, status, nsteps)
+        control = None
+        if resume:
+            if snapshot.control.shape != (self.n, 3):
+                raise capi.ArgumentError(capi.ND_ERR_ARG, f"snapshot control must have shape ({self.n}, 3)")
+            control = torch.from_numpy(np.ascontiguousarray(snapshot.control, dtype=np.float64)).to(dev)
+        elif snapshot:
+            control = torch.zeros((self.n, 3), dtype=torch.float64, device=dev)
+        capi.check(self._lib.nd_ensemble_solve_tsit5_ex(
+            self._h, u.data_ptr(), p.data_ptr() if p is not None else None, float(tspan[0]), float(tspan[1]),
+            float(reltol), float(abstol), int(max_steps), int(threads), status.data_ptr(), nsteps.data_ptr(),
+            control.data_ptr() if control is not None else None, int(resume), self._stream(stream)))
+        return EnsembleSolveResult(u, status, nsteps, control)
 
-    def autotune(self, u0, p, t0=0.0, t_probe=0.5, reltol=1e-6, abstol=1e-8, stream=None):
+    def autotune(self, u0, p, t0=0.0, t_probe=0.5, reltol=1e-6, abstol=1e-8, stream=None, cache=True):
+        """Pick the threads per instance of the solver by timing a short solve with each
+        candidate block size (synchronous), and use it for threads = 0.  With ``cache``,
+        a block size that an earlier process picked for the same workload on the same
+        device is taken from the autotuner cache file instead (nd_gb300.tuning)."""
+        import torch
+        from .tuning import AutotuneCache, workload_key
+        key = store = None
+        if cache:
+            key = workload_key(torch.cuda.get_device_name(u0.device), int(self._lib.nd_version()), self.vertexm.kind,
+                               self.edgem.kind, self.dtype_code, self.n, int(self.v_offset[-1]),
+                               int(self.e_offset[-1]), float(reltol), float(abstol), float(t_probe))
+            store = AutotuneCache()
+            hit = store.get(key)
+            if hit in (64, 128, 256, 512):  # the block sizes the solver takes
+                self.set_threads(hit)
+                return hit
         chosen = C.c_int()
         capi.check(self._lib.nd_ensemble_autotune(self._h, u0.data_ptr(), p.data_ptr() if p is not None else None,
                                                   float(t0), float(t_probe), float(reltol), float(abstol),
                                                   C.byref(chosen), self._stream(stream)))
+        if store is not None:
+            store.put(key, chosen.value)
         return chosen.value
 
     def set_threads(self, threads):

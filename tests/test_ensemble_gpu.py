@@ -56,8 +56,9 @@ def test_ensemble_rhs_equals_per_instance_rhs(cuda):
         np.testing.assert_array_equal(got[ens.u_slice(i)], ref.cpu().numpy())
 
 
-def test_ensemble_tsit5_matches_single_and_oracle(cuda):
+def test_ensemble_tsit5_matches_single_and_oracle(cuda, monkeypatch, tmp_path):
     import torch
+    monkeypatch.setenv("ND_GB300_CACHE_DIR", str(tmp_path))
     rng = np.random.default_rng(2)
     gs = make_graphs(rng, 10, 20, 200)
     us, ps = [], []
@@ -87,6 +88,16 @@ def test_ensemble_tsit5_matches_single_and_oracle(cuda):
     assert chosen in (64, 128, 256, 512)
     res2 = ens.solve_tsit5(u0, p, (0.0, 3.0), reltol=1e-6, abstol=1e-8)
     np.testing.assert_allclose(res2.u.cpu().numpy(), got, atol=1e-12, rtol=0)
+    # the choice is kept in the cache file; a later call (a new ensemble of the same
+    # workload) takes it from there, and a different probe is a different entry
+    from nd_gb300.tuning import AutotuneCache
+    cache = AutotuneCache()
+    assert cache.path.parent == tmp_path and list(cache._load().values()) == [{"threads": chosen}]
+    key = next(iter(cache._load()))
+    cache.put(key, 512 if chosen != 512 else 64)  # a planted entry is what the next call returns
+    ens_b = Ensemble(gs, nd.kuramoto_second(), nd.static_line(), torch.float64)
+    assert ens_b.autotune(u0, p, 0.0, 0.2) == (512 if chosen != 512 else 64)
+    assert ens_b.autotune(u0, p, 0.0, 0.3) in (64, 128, 256, 512) and len(cache._load()) == 2
 
 
 def test_ensemble_step_budget_reports_status(cuda):
@@ -230,3 +241,48 @@ def test_double_float_ensemble_solve_tracks_fp64(cuda):
         sl = e64.u_slice(i)
         assert abs(int(r64.nsteps[i]) - int(rdf.nsteps[i])) <= 2
         assert np.max(np.abs(a[sl] - b[sl])) <= 1e-9
+
+
+def test_snapshot_resume_continues_the_solve(cuda, tmp_path):
+    """A solve split at t = 2 with a saved snapshot (state and step control as .npy files)
+    continues the one-shot solve to t = 4; the resumed instances start from the snapshot's
+    step size, not from the initial-step heuristic."""
+    import torch
+    from nd_gb300.ensemble import load_snapshot
+    rng = np.random.default_rng(9)
+    gs = make_graphs(rng, 8, 20, 200)
+    us, ps = [], []
+    for g in gs:
+        u = np.zeros(2 * g.nv)
+        u[0::2] = rng.uniform(-0.5, 0.5, g.nv)
+        us.append(u)
+        ps.append(swing_params(g, rng))
+    u0 = torch.from_numpy(np.concatenate(us)).to(cuda)
+    p = torch.from_numpy(np.concatenate(ps)).to(cuda)
+    ens = Ensemble(gs, nd.kuramoto_second(), nd.static_line(), torch.float64)
+    tol = dict(reltol=1e-8, abstol=1e-10)
+    full = ens.solve_tsit5(u0, p, (0.0, 4.0), **tol)
+    first = ens.solve_tsit5(u0, p, (0.0, 2.0), snapshot=True, **tol)
+    ctrl = first.control.cpu().numpy()
+    assert (first.status.cpu().numpy() == 0).all()
+    assert np.all(ctrl[:, 0] == 2.0) and np.all(ctrl[:, 1] > 0) and np.all(ctrl[:, 2] > 0)
+    first.save_snapshot(tmp_path / "snap")
+    snap = load_snapshot(tmp_path / "snap")
+    assert snap.t == 2.0
+    np.testing.assert_array_equal(snap.u, first.u.cpu().numpy())
+    np.testing.assert_array_equal(snap.control, ctrl)
+    second = ens.solve_tsit5(None, p, (snap.t, 4.0), snapshot=snap, **tol)
+    assert (second.status.cpu().numpy() == 0).all()
+    np.testing.assert_allclose(second.u.cpu().numpy(), full.u.cpu().numpy(), atol=1e-6, rtol=0)
+    # the split adds the step clipped at t = 2 and a few while the controller grows the step
+    # from its clipped size again (measured: 1 to 4)
+    steps = first.nsteps.cpu().numpy() + second.nsteps.cpu().numpy()
+    assert np.all(np.abs(steps - full.nsteps.cpu().numpy()) <= 8)
+    again = ens.solve_tsit5(None, p, (snap.t, 4.0), snapshot=snap, **tol)
+    np.testing.assert_array_equal(again.u.cpu().numpy(), second.u.cpu().numpy())
+    # a snapshot with a tiny step size takes more steps: the control array is read
+    tiny = snap.control.copy()
+    tiny[:, 1] = 1e-7
+    from nd_gb300.ensemble import EnsembleSnapshot
+    slow = ens.solve_tsit5(None, p, (snap.t, 4.0), snapshot=EnsembleSnapshot(snap.u, tiny), **tol)
+    assert np.all(slow.nsteps.cpu().numpy() >= second.nsteps.cpu().numpy() + 2)
