@@ -69,11 +69,26 @@ struct nd_batched_network_desc
 end
 
 """
-    GB300Execution()
+    GB300Execution(; sum_order=:sequential, layout=:auto)
 
-Unbuffered execution style whose RHS is one call into libnd_b200.so.
+Unbuffered execution style whose RHS is one call into libnd_b200.so.  The options are type
+parameters, because a Network rebuilds its style from its type (`executionstyle(nw) = EX()`,
+src/network_structure.jl:83-116):
+
+- `sum_order`: `:sequential` (SequentialAggregator's bits), `:sequential_hw` (the same bits,
+  hardware adds at hubs) or `:tree` (deterministic warp tree at hubs, not bitwise);
+- `layout`: `:auto` (two-phase kernels for canonical edge lists) or `:fused`.
+
+They are applied to the device handle at adapt time.
 """
-struct GB300Execution <: ExecutionStyle{false} end
+struct GB300Execution{O,L} <: ExecutionStyle{false} end
+function GB300Execution(; sum_order::Symbol=:sequential, layout::Symbol=:auto)
+    sum_order in (:sequential, :sequential_hw, :tree) || throw(ArgumentError("unknown sum_order $sum_order"))
+    layout in (:auto, :fused) || throw(ArgumentError("unknown layout $layout"))
+    GB300Execution{sum_order,layout}()
+end
+const ND_ORDER_CODES = Dict(:sequential => Cint(0), :tree => Cint(1), :sequential_hw => Cint(2))
+const ND_LAYOUT_CODES = Dict(:auto => Cint(0), :fused => Cint(1))
 
 # Known component functions -> library kinds (nd_vertex_kind / nd_edge_kind).  Models
 # built from the component library register their functions here: vertex f, the
@@ -185,10 +200,17 @@ function Adapt.adapt_structure(::Type{<:CuArray{T}}, a::GB300Aggregator) where {
     out
 end
 
+# The execution style's options on the handle (host-side settings, no device work).
+function configure!(a::GB300Aggregator, ::GB300Execution{O,L}) where {O,L}
+    check(ccall((:nd_set_sum_order, libnd), Cint, (Ptr{Cvoid}, Cint), a.handle, ND_ORDER_CODES[O]))
+    check(ccall((:nd_set_layout, libnd), Cint, (Ptr{Cvoid}, Cint), a.handle, ND_LAYOUT_CODES[L]))
+end
+
 # The RHS: one stream-ordered call on CUDA.jl's task-local stream.
 function (nw::Network{<:GB300Execution})(du::CuArray{T}, u::CuArray{T}, p, t) where {T}
     a = nw.layer.aggregator
     a.handle == C_NULL && throw(ArgumentError("adapt the network with adapt(CuArray{$T}, nw) first"))
+    configure!(a, NetworkDynamics.executionstyle(nw))
     dtype = T === Float64 ? ND_F64 : T === Float32 ? ND_F32 : Cint(0)
     pp, np = p === nothing || isempty(p) ? (CuPtr{T}(0), 0) : (pointer(p), length(p))
     check(ccall((:nd_rhs, libnd), Cint,

@@ -27,13 +27,49 @@ class ExecutionStyle:
 
 
 class GB300Execution(ExecutionStyle):
-    """Fused single-kernel RHS on one GB300 GPU.  Unbuffered: edges read vertex outputs
-    straight from u (the lazy gather of src/gbufs.jl:37-65, done in registers)."""
+    """The RHS on one GB300 GPU.  Unbuffered: edges read vertex outputs straight from u
+    (the lazy gather of src/gbufs.jl:37-65, done in registers).
+
+    Keyword options, applied to the device handle when the network is adapted (the
+    reference configures its execution styles by keyword and type parameter,
+    src/executionstyles.jl:13-52):
+
+    - ``sum_order``: "sequential" (default; the bits of SequentialAggregator, with the exact
+      scan at hubs), "sequential_hw" (the same bits with hardware adds at hubs) or "tree"
+      (a deterministic warp tree at hubs; not bitwise);
+    - ``layout``: "auto" (two-phase edge-centric kernels for canonical edge lists, else the
+      fused kernel) or "fused";
+    - ``kernel_timing``: bracket every kernel with CUDA events for ``Network.kernel_times``.
+
+    The precision is the dtype given to ``adapt``.  The degree buckets (light rows up to 32,
+    heavy rows above 2048) and the FP32 Kahan threshold (rows longer than 32) are
+    compile-time constants of the kernels."""
 
     buffered = False
+    SUM_ORDERS = ("sequential", "sequential_hw", "tree")
+    LAYOUTS = ("auto", "fused")
+
+    def __init__(self, sum_order: str = "sequential", layout: str = "auto", kernel_timing: bool = False):
+        if sum_order not in self.SUM_ORDERS:
+            raise capi.ArgumentError(capi.ND_ERR_ARG, f"unknown sum_order {sum_order!r}: one of {self.SUM_ORDERS}")
+        if layout not in self.LAYOUTS:
+            raise capi.ArgumentError(capi.ND_ERR_ARG, f"unknown layout {layout!r}: one of {self.LAYOUTS}")
+        self.sum_order = sum_order
+        self.layout = layout
+        self.kernel_timing = bool(kernel_timing)
+
+    def __eq__(self, other):
+        return isinstance(other, GB300Execution) and (self.sum_order, self.layout, self.kernel_timing) == (
+            other.sum_order, other.layout, other.kernel_timing)
+
+    def __hash__(self):
+        return hash((self.sum_order, self.layout, self.kernel_timing))
 
     def __repr__(self):
-        return "GB300Execution()"
+        opts = [f"{k}={v!r}" for k, v, d in (("sum_order", self.sum_order, "sequential"),
+                                             ("layout", self.layout, "auto"),
+                                             ("kernel_timing", self.kernel_timing, False)) if v != d]
+        return f"GB300Execution({', '.join(opts)})"
 
 
 def iscudacompatible(x) -> bool:
@@ -414,4 +450,11 @@ def adapt(nw: Network, dtype) -> Network:
     out._handle = None
     out._dtype = None
     out._create(dtype)
+    ex = nw.execution
+    if ex.sum_order != "sequential":
+        out.set_sum_order(ex.sum_order)
+    if ex.layout != "auto":
+        out.set_layout(ex.layout)
+    if ex.kernel_timing:
+        out.set_kernel_timing(True)
     return out

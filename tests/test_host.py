@@ -205,3 +205,17 @@ def test_mass_matrix_like_construct_mass_matrix():
     bad = dataclasses.replace(nd.kuramoto_second(), mass_matrix=np.eye(2))
     with pytest.raises(nd.ArgumentError):
         nd.Network(g, bad, nd.static_line()).mass_matrix()
+
+
+def test_execution_options_are_checked_and_kept():
+    ex = nd.GB300Execution(sum_order="tree", layout="fused", kernel_timing=True)
+    assert (ex.sum_order, ex.layout, ex.kernel_timing) == ("tree", "fused", True)
+    assert repr(nd.GB300Execution()) == "GB300Execution()"
+    assert repr(ex) == "GB300Execution(sum_order='tree', layout='fused', kernel_timing=True)"
+    assert nd.GB300Execution() == nd.GB300Execution(sum_order="sequential")
+    with pytest.raises(nd.ArgumentError):
+        nd.GB300Execution(sum_order="pairwise")
+    with pytest.raises(nd.ArgumentError):
+        nd.GB300Execution(layout="blocked")
+    nw = nd.Network(nd.cycle_graph(5), nd.diffusion_vertex(), nd.diffusion_edge(), execution=ex)
+    assert nw.execution is ex

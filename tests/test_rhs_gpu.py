@@ -319,3 +319,28 @@ def test_edge_phase_sources_of_sparse_and_dense_chunks(cuda):
     on = O.OracleNetwork.from_graph(g, O.V_DIFFUSION, O.E_DIFFUSION)
     u, p = random_inputs(on, O.V_DIFFUSION, rng)
     np.testing.assert_array_equal(gpu_rhs(nw, u, p, cuda, np.float64), on.rhs(u, p))
+
+
+def test_execution_options_reach_the_handle(cuda):
+    """GB300Execution(sum_order=..., layout=..., kernel_timing=...) configures the handle
+    that adapt creates: the fused layout gives the two-phase bits, the tree order is
+    reported by nd_get_info, and the kernels are timed."""
+    import torch
+    g = nd.barabasi_albert(1_000_000, 4, seed=12)
+    assert g.degree().max() > 2048
+    on = O.OracleNetwork.from_graph(g, O.V_DIFFUSION, O.E_DIFFUSION)
+    u, p = random_inputs(on, O.V_DIFFUSION, np.random.default_rng(4))
+    plain = nd.adapt(nd.Network(g, nd.diffusion_vertex(), nd.diffusion_edge()), torch.float64)
+    ex = nd.GB300Execution(layout="fused", kernel_timing=True)
+    fused = nd.adapt(nd.Network(g, nd.diffusion_vertex(), nd.diffusion_edge(), execution=ex), torch.float64)
+    ref = gpu_rhs(plain, u, p, cuda, np.float64)
+    np.testing.assert_array_equal(ref, on.rhs(u, p))
+    np.testing.assert_array_equal(gpu_rhs(fused, u, p, cuda, np.float64), ref)
+    t = fused.kernel_times()
+    assert t["fused"][0] == 1 and t["fused"][1] > 0.0 and t["edge_phase"][0] == 0
+    tree = nd.adapt(nd.Network(g, nd.diffusion_vertex(), nd.diffusion_edge(),
+                               execution=nd.GB300Execution(sum_order="tree")), torch.float64)
+    assert tree.info().sum_order == nd.capi.ND_ORDER_TREE and plain.info().sum_order == nd.capi.ND_ORDER_SEQUENTIAL
+    got = gpu_rhs(tree, u, p, cuda, np.float64)
+    # a hub of n terms summed in two orders differs by at most about n·eps·Σ|terms| (n < 4500)
+    assert np.all(np.abs(got - ref) <= 1e-12 * on.abs_terms(u, p))
