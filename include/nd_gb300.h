@@ -312,6 +312,18 @@ int nd_solve_tsit5(nd_handle* h, double* u, const void* p, double t0, double t1,
 int nd_solve_rosenbrock23(nd_handle* h, double* u, const double* p, const double* mass, double t0, double t1,
                           double reltol, double abstol, int64_t max_steps, nd_solve_stats* stats, void* stream);
 
+/* Rodas4 (Hairer & Wanner, Solving ODEs II, section VI.4: the first method of RODAS; order
+ * 4, L-stable, stiffly accurate, embedded order 3) for M u' = f(u) with a diagonal mass
+ * matrix, on the same stage machinery as nd_solve_rosenbrock23: six linear systems per step
+ * with W = M - h γ J (γ = 1/4, J from nd_jacobian), each solved by Jacobi-preconditioned
+ * GMRES.  Step control h <- h min(6, max(0.2, 0.9 err^(-1/4))) on the scaled RMS norm of
+ * the embedded estimate.  Arguments, stats and errors as for nd_solve_rosenbrock23.  FP64
+ * handles only.  Synchronous.  Replaces solve(prob, Rodas4()) (the reference's tests solve
+ * its heterogeneous and ODE-edge networks with Rodas4 / Rodas5,
+ * test/inhomogeneous_test.jl:51, test/diffusion_test.jl:121). */
+int nd_solve_rodas4(nd_handle* h, double* u, const double* p, const double* mass, double t0, double t1, double reltol,
+                    double abstol, int64_t max_steps, nd_solve_stats* stats, void* stream);
+
 /* Allocation-free RHS.  This entry point has no counterpart in the reference.  It is for
  * callers that must not allocate device memory while they evaluate the RHS: a process
  * whose device memory belongs to a caching allocator (CUDA.jl's or PyTorch's pool), where a
@@ -327,7 +339,10 @@ int nd_solve_rosenbrock23(nd_handle* h, double* u, const double* p, const double
  * The arrays must describe a canonical list exactly as nd_create would sort it; they are
  * device arrays and are not checked.  Another order still gives the network's RHS, but its
  * sums run in that order, not the reference's.
- * Result: the same du as nd_rhs on the same network.  ne above the scratch size returns
+ * Result: the same du as nd_rhs on the same network: in FP64 bit for bit; in FP32 bit for
+ * bit on every row of degree <= 2048 (rows longer than 32 with Kahan compensation, as in
+ * nd_rhs), within the FP32 rounding on longer rows, which nd_rhs sums with a warp tree.
+ * ne above the scratch size returns
  * ND_ERR_ARG.  The first call on a device looks up the scratch array's device address
  * (cudaGetSymbolAddress, with that device current) and should come before any stream
  * capture; the lookup is repeated only after the device's context was reset.  All calls

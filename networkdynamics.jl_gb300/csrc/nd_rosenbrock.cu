@@ -90,6 +90,102 @@ struct Buf {
     ~Buf() { cudaFree(p); }
 };
 
+// W's pattern: J's columns plus the diagonal, sorted per row; jmap gives the W position of
+// every J entry and wdiag that of every row's diagonal.
+void w_pattern(const JacPlan& J, int64_t n, int64_t nnz, std::vector<int32_t>& wrow, std::vector<int32_t>& wcol,
+               std::vector<int32_t>& jmap, std::vector<int32_t>& wdiag) {
+    wrow.assign(n + 1, 0);
+    wcol.clear();
+    jmap.assign((size_t)std::max<int64_t>(nnz, 1), 0);
+    wdiag.assign(n, 0);
+    wcol.reserve((size_t)nnz + n);
+    for (int64_t i = 0; i < n; ++i) {
+        const int32_t b = J.rowptr_h[i], e = J.rowptr_h[i + 1];
+        bool diag_done = false;
+        for (int32_t k = b; k <= e; ++k) {
+            const bool end = k == e;
+            const int32_t c = end ? INT32_MAX : J.colidx_h[k];
+            if (!diag_done && c >= (int32_t)i) {
+                if (c != (int32_t)i) wcol.push_back((int32_t)i);  // a diagonal the pattern lacks
+                wdiag[i] = (int32_t)wcol.size() - (c == (int32_t)i ? 0 : 1);
+                diag_done = true;
+            }
+            if (end) break;
+            jmap[k] = (int32_t)wcol.size();
+            wcol.push_back(c);
+        }
+        wrow[i + 1] = (int32_t)wcol.size();
+    }
+}
+
+// ---- Rodas4 ---------------------------------------------------------------------------------
+// Hairer & Wanner, Solving ODEs II (section VI.4), the first method of their RODAS code, in
+// the transformed variables that need no product with J.  Stage i solves
+//   (M / (h γ) - J) k_i = f(U_i) + M Σ_{j<i} C_ij k_j / h,
+//   U_1 = u, U_i = u + Σ_j a_ij k_j (i = 2..5), U_6 = U_5 + k_5,
+// the new state is U_6 + k_6 (stiffly accurate) and k_6 the embedded error estimate.  With
+// W = M - h γ J as for Rosenbrock23 the right-hand sides are scaled by h γ instead:
+//   W k_i = h γ f(U_i) + M Σ_j (γ C_ij) k_j.
+// The coefficients are the published ones (the same in the oracle's restatement).
+constexpr double kR4Gamma = 0.25;
+__constant__ double c_r4a[5][4] = {
+    {0.0, 0.0, 0.0, 0.0},
+    {1.544, 0.0, 0.0, 0.0},
+    {0.9466785280815826, 0.2557011698983284, 0.0, 0.0},
+    {3.314825187068521, 2.896124015972201, 0.9986419139977817, 0.0},
+    {1.221224509226641, 6.019134481288629, 12.53708332932087, -0.6878860361058950}};
+__constant__ double c_r4c[6][5] = {
+    {0.0, 0.0, 0.0, 0.0, 0.0},
+    {-5.6688, 0.0, 0.0, 0.0, 0.0},
+    {-2.430093356833875, -0.2063599157091915, 0.0, 0.0, 0.0},
+    {-0.1073529058151375, -9.594562251023355, -20.47028614809616, 0.0, 0.0},
+    {7.496443313967647, -10.24680431464352, -33.99990352819905, 11.70890893206160, 0.0},
+    {8.083246795921522, -7.981132988064893, -31.52159432874371, 16.31930543123136, -6.058818238834054}};
+
+struct Stages {
+    const double* k[6];
+};
+
+// U = u + Σ_{j < i} a_ij k_j (stages i = 1..4, 0-based)
+__global__ void r4_state_kernel(int64_t n, int i, const double* __restrict__ u, Stages ks, double* __restrict__ U) {
+    for (int64_t x = (int64_t)blockIdx.x * kB + threadIdx.x; x < n; x += (int64_t)gridDim.x * kB) {
+        double acc = 0.0;
+        for (int j = 0; j < i; ++j) acc = __dadd_rn(acc, __dmul_rn(c_r4a[i][j], ks.k[j][x]));
+        U[x] = __dadd_rn(u[x], acc);
+    }
+}
+
+// rb = h γ f + M Σ_{j < i} (γ C_ij) k_j
+__global__ void r4_rhs_kernel(int64_t n, int i, double hg, const double* __restrict__ f, const double* __restrict__ mass,
+                              Stages ks, double* __restrict__ rb) {
+    for (int64_t x = (int64_t)blockIdx.x * kB + threadIdx.x; x < n; x += (int64_t)gridDim.x * kB) {
+        double acc = 0.0;
+        for (int j = 0; j < i; ++j) acc = __dadd_rn(acc, __dmul_rn(kR4Gamma * c_r4c[i][j], ks.k[j][x]));
+        const double m = mass ? mass[x] : 1.0;
+        rb[x] = __dadd_rn(__dmul_rn(hg, f[x]), __dmul_rn(m, acc));
+    }
+}
+
+// Σ (k6_i / (abstol + reltol max(|u_i|, |u1_i|)))² per block
+__global__ void r4_err_kernel(int64_t n, const double* __restrict__ e, const double* __restrict__ u,
+                              const double* __restrict__ u1, double abstol, double reltol, double* __restrict__ partial) {
+    __shared__ double red[kB / 32];
+    double acc = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * kB + threadIdx.x; i < n; i += (int64_t)gridDim.x * kB) {
+        const double sc = abstol + reltol * fmax(fabs(u[i]), fabs(u1[i]));
+        const double r = e[i] / sc;
+        acc = __dadd_rn(acc, __dmul_rn(r, r));
+    }
+    for (int off = 16; off > 0; off >>= 1) acc = __dadd_rn(acc, __shfl_xor_sync(0xffffffffu, acc, off));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < kB / 32; ++k) t = __dadd_rn(t, red[k]);
+        partial[blockIdx.x] = t;
+    }
+}
+
 }  // namespace
 
 }  // namespace nd
@@ -113,27 +209,8 @@ extern "C" int nd_solve_rosenbrock23(nd_handle* h, double* u, const double* p, c
     int rc = nd_jacobian_pattern(h, &nnz, nullptr, nullptr);
     if (rc != ND_OK) return rc;
     const int64_t n = h->dim;
-    const JacPlan& J = h->jac;
-    // W's pattern: J's columns plus the diagonal, sorted per row
-    std::vector<int32_t> wrow(n + 1, 0), wcol, jmap((size_t)std::max<int64_t>(nnz, 1)), wdiag(n);
-    wcol.reserve((size_t)nnz + n);
-    for (int64_t i = 0; i < n; ++i) {
-        const int32_t b = J.rowptr_h[i], e = J.rowptr_h[i + 1];
-        bool diag_done = false;
-        for (int32_t k = b; k <= e; ++k) {
-            const bool end = k == e;
-            const int32_t c = end ? INT32_MAX : J.colidx_h[k];
-            if (!diag_done && c >= (int32_t)i) {
-                if (c != (int32_t)i) wcol.push_back((int32_t)i);  // a diagonal the pattern lacks
-                wdiag[i] = (int32_t)wcol.size() - (c == (int32_t)i ? 0 : 1);
-                diag_done = true;
-            }
-            if (end) break;
-            jmap[k] = (int32_t)wcol.size();
-            wcol.push_back(c);
-        }
-        wrow[i + 1] = (int32_t)wcol.size();
-    }
+    std::vector<int32_t> wrow, wcol, jmap, wdiag;
+    w_pattern(h->jac, n, nnz, wrow, wcol, jmap, wdiag);
     const int64_t wnnz = (int64_t)wcol.size();
     const int m = 30;
     // device: W pattern (rowptr, col, jmap, wdiag), J values, W values, 8 vectors
@@ -242,6 +319,141 @@ extern "C" int nd_solve_rosenbrock23(nd_handle* h, double* u, const double* p, c
     if (status == ND_ERR_NOT_CONVERGED) {
         char msg[160];
         snprintf(msg, sizeof msg, "nd_solve_rosenbrock23: step size underflow at t = %.6g", t);
+        return fail(ND_ERR_NOT_CONVERGED, msg);
+    }
+    return ND_OK;
+}
+
+extern "C" int nd_solve_rodas4(nd_handle* h, double* u, const double* p, const double* mass, double t0, double t1,
+                               double reltol, double abstol, int64_t max_steps, nd_solve_stats* st, void* stream) {
+    clear_error();
+    ND_NVTX("nd_solve_rodas4");
+    if (!h || !u || !st) return fail(ND_ERR_ARG, "nd_solve_rodas4: NULL argument");
+    if (h->dtype != ND_F64) return fail(ND_ERR_DTYPE, "nd_solve_rodas4: FP64 handles only");
+    if (h->pdim > 0 && !p) return fail(ND_ERR_ARG, "nd_solve_rodas4: p is NULL");
+    if (!(t1 > t0)) return fail(ND_ERR_ARG, "nd_solve_rodas4: t1 must be greater than t0");
+    if (!(reltol > 0) || !(abstol > 0)) return fail(ND_ERR_ARG, "nd_solve_rodas4: tolerances must be > 0");
+    const int64_t budget = max_steps > 0 ? max_steps : (int64_t)ND_ENSEMBLE_DEFAULT_MAX_STEPS;
+    *st = nd_solve_stats{};
+    cudaStream_t s = (cudaStream_t)stream;
+    int64_t nnz = 0;
+    int rc = nd_jacobian_pattern(h, &nnz, nullptr, nullptr);
+    if (rc != ND_OK) return rc;
+    const int64_t n = h->dim;
+    std::vector<int32_t> wrow, wcol, jmap, wdiag;
+    w_pattern(h->jac, n, nnz, wrow, wcol, jmap, wdiag);
+    const int64_t wnnz = (int64_t)wcol.size();
+    const int m = 30;
+    // device: W pattern, J values, W values, 10 vectors (f0 f k1..k6 U u1 rb -> 11), error
+    // partials, GMRES workspace
+    const size_t ints = (size_t)(n + 1) + wnnz + jmap.size() + n;
+    const size_t dbl = (size_t)std::max<int64_t>(nnz, 1) + wnnz + 11 * (size_t)n + kErrBlocks + GmresSolver::doubles(n, m);
+    Buf buf;
+    cudaError_t err = cudaMalloc(&buf.p, ints * sizeof(int32_t) + 16 + dbl * sizeof(double));
+    if (err != cudaSuccess) return cuda_fail(err, "nd_solve_rodas4: workspace");
+    int32_t* d_wrow = static_cast<int32_t*>(buf.p);
+    int32_t* d_wcol = d_wrow + (n + 1);
+    int32_t* d_jmap = d_wcol + wnnz;
+    int32_t* d_wdiag = d_jmap + jmap.size();
+    double* jv = reinterpret_cast<double*>((reinterpret_cast<uintptr_t>(d_wdiag + n) + 15) & ~uintptr_t(15));
+    double* wv = jv + std::max<int64_t>(nnz, 1);
+    double* f0 = wv + wnnz;
+    double* f = f0 + n;
+    double* k[6];
+    k[0] = f + n;
+    for (int i = 1; i < 6; ++i) k[i] = k[i - 1] + n;
+    double* U = k[5] + n;
+    double* u1 = U + n;
+    double* rb = u1 + n;
+    double* partial = rb + n;
+    GmresSolver gm;
+    gm.attach(partial + kErrBlocks, n, m, s);
+    if ((err = cudaMemcpyAsync(d_wrow, wrow.data(), (n + 1) * sizeof(int32_t), cudaMemcpyHostToDevice, s)) !=
+            cudaSuccess ||
+        (err = cudaMemcpyAsync(d_wcol, wcol.data(), wnnz * sizeof(int32_t), cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (err = cudaMemcpyAsync(d_jmap, jmap.data(), jmap.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s)) !=
+            cudaSuccess ||
+        (err = cudaMemcpyAsync(d_wdiag, wdiag.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return cuda_fail(err, "nd_solve_rodas4: pattern upload");
+    const unsigned G = grid_of(n);
+    Stages ks{{k[0], k[1], k[2], k[3], k[4], k[5]}};
+    auto rhs = [&](double* out, const double* x) { return nd_rhs(h, ND_F64, out, n, x, n, p, h->pdim, NAN, s); };
+    // the linear systems are solved well below the step's own error scale
+    const double lin_tol = std::min(1e-3, 1e-2 * reltol);
+    auto wsolve = [&](const double* bvec, double* x) -> int {
+        cudaMemsetAsync(x, 0, n * sizeof(double), s);
+        return gm.solve(d_wrow, d_wcol, wv, bvec, x, lin_tol, 50, nullptr);
+    };
+    if ((rc = rhs(f0, u)) != ND_OK) return rc;
+    st->nf = 1;
+    double dt = std::min(1e-3 * (t1 - t0), 1e-2);
+    double t = t0;
+    int64_t steps = 0;
+    int status = ND_OK;
+    std::vector<double> hpart(kErrBlocks);
+    while (t < t1) {
+        if (steps >= budget) {
+            status = ND_ERR_MAXITERS;
+            break;
+        }
+        ++steps;
+        if (t + dt * (1 + 1e-12) > t1) dt = t1 - t;
+        const double hg = dt * kR4Gamma;
+        // W = M - h γ J at u
+        if ((rc = nd_jacobian(h, ND_F64, jv, u, p, t, s)) != ND_OK) return rc;
+        cudaMemsetAsync(wv, 0, wnnz * sizeof(double), s);
+        form_w_kernel<<<grid_of(std::max<int64_t>(nnz, 1)), kB, 0, s>>>(nnz, d_jmap, jv, hg, wv);
+        add_mass_kernel<<<G, kB, 0, s>>>(n, d_wdiag, mass, wv);
+        gm.jacobi(d_wrow, d_wcol, wv);
+        for (int i = 0; i < 6; ++i) {
+            const double* fi = f0;
+            if (i > 0) {
+                if (i < 5) {
+                    r4_state_kernel<<<G, kB, 0, s>>>(n, i, u, ks, U);  // U_i = u + Σ a_ij k_j
+                } else {
+                    vec_axpby(n, 1.0, k[4], 1.0, U, s);  // U_6 = U_5 + k_5
+                }
+                if ((rc = rhs(f, U)) != ND_OK) return rc;
+                fi = f;
+            }
+            r4_rhs_kernel<<<G, kB, 0, s>>>(n, i, hg, fi, mass, ks, rb);
+            if ((rc = wsolve(rb, k[i])) != ND_OK) return rc;
+        }
+        st->nf += 5;
+        // u1 = U_6 + k_6; the error estimate is k_6
+        cudaMemcpyAsync(u1, U, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+        vec_axpby(n, 1.0, k[5], 1.0, u1, s);
+        r4_err_kernel<<<kErrBlocks, kB, 0, s>>>(n, k[5], u, u1, abstol, reltol, partial);
+        cudaMemcpyAsync(hpart.data(), partial, kErrBlocks * sizeof(double), cudaMemcpyDeviceToHost, s);
+        if ((rc = gm.sync("nd_solve_rodas4")) != ND_OK) return rc;
+        double e2 = 0.0;
+        for (double x : hpart) e2 += x;
+        double EEst = std::sqrt(e2 / (double)(n ? n : 1));
+        if (!(EEst == EEst)) EEst = 1e10;
+        const double fac = std::min(6.0, std::max(0.2, 0.9 * std::pow(std::max(EEst, 1e-10), -0.25)));
+        if (EEst <= 1.0) {
+            t = (std::fabs(t1 - (t + dt)) <= 1e-14 * std::max(1.0, std::fabs(t1))) ? t1 : t + dt;
+            cudaMemcpyAsync(u, u1, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+            if ((rc = rhs(f0, u)) != ND_OK) return rc;
+            st->nf += 1;
+            st->naccept++;
+        } else {
+            st->nreject++;
+        }
+        st->dt_last = dt * fac;
+        dt *= fac;
+        if (t < t1 && dt < 1e-14 * std::max(1.0, std::fabs(t))) {
+            status = ND_ERR_NOT_CONVERGED;
+            break;
+        }
+    }
+    if ((rc = gm.sync("nd_solve_rodas4")) != ND_OK) return rc;
+    st->t_final = t;
+    st->status = status;
+    if (status == ND_ERR_MAXITERS) return fail(ND_ERR_MAXITERS, "nd_solve_rodas4: step budget exhausted before t1");
+    if (status == ND_ERR_NOT_CONVERGED) {
+        char msg[160];
+        snprintf(msg, sizeof msg, "nd_solve_rodas4: step size underflow at t = %.6g", t);
         return fail(ND_ERR_NOT_CONVERGED, msg);
     }
     return ND_OK;

@@ -200,6 +200,7 @@ SIGNATURES["nd_solve_tsit5"] = (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.
 SIGNATURES["nd_solve_rosenbrock23"] = (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
                                                  C.c_double, C.c_double, C.c_double, C.c_int64,
                                                  C.POINTER(nd_solve_stats), C.c_void_p])
+SIGNATURES["nd_solve_rodas4"] = SIGNATURES["nd_solve_rosenbrock23"]
 
 
 class nd_ensemble_desc(C.Structure):

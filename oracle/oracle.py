@@ -311,6 +311,73 @@ def rosenbrock23(rhs, jac, u0, t0, t1, reltol, abstol, mass=None, max_steps=100_
     return u, na, nr
 
 
+# Rodas4 (Hairer & Wanner, Solving ODEs II, section VI.4; the RODAS code's first method),
+# in the transformed variables that need no matrix-vector product with J: gamma, the stage
+# coefficients a_ij (applied to the k's) and C_ij (divided by h), and the stiffly accurate
+# solution u5 + k5 + k6 with the embedded error estimate k6.
+RODAS4_GAMMA = 0.25
+RODAS4_A = ((), (1.544,), (0.9466785280815826, 0.2557011698983284),
+            (3.314825187068521, 2.896124015972201, 0.9986419139977817),
+            (1.221224509226641, 6.019134481288629, 12.53708332932087, -0.6878860361058950))
+RODAS4_C = ((), (-5.6688,), (-2.430093356833875, -0.2063599157091915),
+            (-0.1073529058151375, -9.594562251023355, -20.47028614809616),
+            (7.496443313967647, -10.24680431464352, -33.99990352819905, 11.70890893206160),
+            (8.083246795921522, -7.981132988064893, -31.52159432874371, 16.31930543123136, -6.058818238834054))
+
+
+def rodas4_step(rhs, jac, u, f0, dt, M):
+    """One Rodas4 step of M u' = rhs(u) (autonomous, diagonal M): returns (u_new, err, f at
+    u_new is not evaluated).  W = M/(h γ) - J; k_i = W⁻¹ (f(U_i) + M Σ_j C_ij k_j / h) with
+    U_1 = u, U_i = u + Σ_j a_ij k_j (i <= 5), U_6 = U_5 + k_5; u_new = U_6 + k_6, err = k_6."""
+    W = np.diag(M / (dt * RODAS4_GAMMA)) - jac(u)
+    ks = []
+    U = u
+    for i in range(6):
+        if i == 0:
+            f = f0
+        else:
+            if i < 5:
+                U = u + sum(a * k for a, k in zip(RODAS4_A[i], ks))
+            else:
+                U = U + ks[4]
+            f = rhs(U)
+        b = f + M * sum(c * k for c, k in zip(RODAS4_C[i], ks)) / dt if i else f
+        ks.append(np.linalg.solve(W, b))
+    return U + ks[5], ks[5]
+
+
+def rodas4(rhs, jac, u0, t0, t1, reltol, abstol, mass=None, max_steps=100_000, fixed_dt=None):
+    """Rodas4 for M u' = rhs(u) with a diagonal mass matrix (None: identity), dense.  Error
+    in the scaled RMS norm of k6 against abstol + reltol max(|u|, |u_new|); step factor
+    min(6, max(0.2, 0.9 err^(-1/4))); first step min(1e-3 (t1 - t0), 1e-2).  fixed_dt
+    takes steps of that size, accepting every one (for convergence-order checks).  The
+    restatement the GPU solver is checked against.  Returns (u(t1), accepted, rejected)."""
+    u = np.array(u0, dtype=np.float64, copy=True)
+    n = u.size
+    M = np.ones(n) if mass is None else np.broadcast_to(np.asarray(mass, dtype=np.float64), (n,))
+    f0 = rhs(u)
+    t = t0
+    dt = fixed_dt if fixed_dt else min(1e-3 * (t1 - t0), 1e-2)
+    na = nr = 0
+    while t < t1 and na + nr < max_steps:
+        if t + dt * (1 + 1e-12) > t1:
+            dt = t1 - t
+        u1, err = rodas4_step(rhs, jac, u, f0, dt, M)
+        E = np.sqrt(np.mean((err / (abstol + reltol * np.maximum(np.abs(u), np.abs(u1)))) ** 2))
+        if not E == E:
+            E = 1e10
+        if fixed_dt or E <= 1.0:
+            t = t1 if abs(t1 - (t + dt)) <= 1e-14 * max(1.0, abs(t1)) else t + dt
+            u = u1
+            f0 = rhs(u)
+            na += 1
+        else:
+            nr += 1
+        if not fixed_dt:
+            dt *= min(6.0, max(0.2, 0.9 * max(E, 1e-10) ** (-0.25)))
+    return u, na, nr
+
+
 def rhs_numpy(nv, src, dst, vk, ek, u, p, dtype=np.float64):
     """Independent numpy restatement of the sequential RHS for one homogeneous batch."""
     src = np.asarray(src, dtype=np.int64)

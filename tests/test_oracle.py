@@ -166,3 +166,30 @@ def test_oracle_rosenbrock23_known_answer():
     x0[0] = -L[0, 1:] @ x0[1:] / L[0, 0]  # consistent: (L x)_0 = 0
     u, _, _ = O.rosenbrock23(rhs, jac, x0, 0.0, 1.0, 1e-6, 1e-9, mass=mass)
     assert abs(L[0] @ u) < 1e-10
+
+
+def test_oracle_rodas4_is_fourth_order():
+    """The Rodas4 restatement (the coefficients the GPU solver uses) converges with order 4
+    at fixed steps on a nonlinear ODE (y' = -y², y(1) = 1/2), a stiff linear system and an
+    index-1 DAE with a nonlinear algebraic row (mass matrix diag(1, 0)): halving the step
+    divides the error by ~16."""
+    def ratios(f, jac, y0, exact, mass=None):
+        errs = [np.abs(O.rodas4(f, jac, y0, 0.0, 1.0, 1.0, 1.0, mass=mass, fixed_dt=h)[0] - exact).max()
+                for h in (0.1, 0.05, 0.025)]
+        return [errs[i] / errs[i + 1] for i in range(2)]
+
+    for r in ratios(lambda y: -y ** 2, lambda y: np.diag(-2 * y), np.array([1.0]), 0.5):
+        assert 14.0 < r < 19.0
+    A = np.array([[-1.0, 1.0], [0.0, -100.0]])
+    y0 = np.array([1.0, 1.0])
+    for r in ratios(lambda y: A @ y, lambda y: A, y0, scipy.linalg.expm(A) @ y0):
+        assert 14.0 < r < 19.0
+    f = lambda y: np.array([-y[0] + y[1], y[0] - 2 * y[1] + 0.1 * y[1] ** 2])
+    jac = lambda y: np.array([[-1.0, 1.0], [1.0, -2.0 + 0.2 * y[1]]])
+    z0 = np.array([1.0, (2 - np.sqrt(3.6)) / 0.2])  # consistent: 0 = y1 - 2 y2 + 0.1 y2²
+    ref = O.rodas4(f, jac, z0, 0.0, 1.0, 1e-13, 1e-13, mass=[1.0, 0.0])[0]
+    for r in ratios(f, jac, z0, ref, mass=[1.0, 0.0]):
+        assert 14.0 < r < 19.0
+    # adaptive: the algebraic row stays satisfied and the steps follow tol^(-1/4)
+    y, na, _ = O.rodas4(f, jac, z0, 0.0, 1.0, 1e-6, 1e-8, mass=[1.0, 0.0])
+    assert abs(y[0] - 2 * y[1] + 0.1 * y[1] ** 2) < 1e-9 and np.abs(y - ref).max() < 1e-6
