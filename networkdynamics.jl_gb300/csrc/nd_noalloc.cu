@@ -140,7 +140,20 @@ __global__ void static_row_kernel(int64_t nv, int64_t ne, const int32_t* __restr
                 s1 = s0;
             }
         }
-        T acc = T(0);
+        // FP32 rows longer than kLightMaxDeg add with Kahan compensation, as the row phase of
+        // nd_rhs does: both give the same bits on every row of degree <= kMediumMaxDeg
+        const bool kahan = sizeof(T) == 4 && (d1 - d0) + (s1 - s0) > (uint32_t)kLightMaxDeg;
+        T acc = T(0), comp = T(0);
+        auto add = [&](T term) {
+            if (kahan) {
+                const T yk = A::sub(term, comp);
+                const T s2 = A::add(acc, yk);
+                comp = A::sub(A::sub(s2, acc), yk);
+                acc = s2;
+            } else {
+                acc = A::add(acc, term);
+            }
+        };
         [[maybe_unused]] int32_t prev = -1;
         for (uint32_t k = d0; k < d1; ++k) {
             const int32_t e = dst_eid[k];
@@ -153,14 +166,15 @@ __global__ void static_row_kernel(int64_t nv, int64_t ne, const int32_t* __restr
                 if (e <= prev) check_report(kChkDstEidOrder, k, e);
                 prev = e;
             }
-            acc = A::add(acc, y[e]);
+            add(y[e]);
         }
         for (uint32_t e = s0; e < s1; ++e) {
             if constexpr (CHECK) {
                 if (src[e] != v) check_report(kChkSrcBlock, e, src[e]);
             }
-            acc = A::add(acc, -y[e]);
+            add(-y[e]);
         }
+        if constexpr (sizeof(T) == 4) acc = A::sub(acc, comp);
         vertex_f<T, VK>(du, u, p, v, acc);
     }
 }
@@ -169,9 +183,15 @@ template <typename T, int VK, int EK, bool CHECK>
 cudaError_t launch_static(int64_t nv, int64_t ne, const int32_t* src, const int32_t* dst, const uint32_t* src_ptr,
                           const uint32_t* dst_ptr, const int32_t* dst_eid, void* du, const void* u, const void* p,
                           void* scratch, cudaStream_t s) {
+    // grid-stride kernels: at most 16 blocks per SM of the current device
     const int block = 256;
-    const unsigned ge = (unsigned)std::min<int64_t>((ne + block - 1) / block, 152 * 16);
-    const unsigned gv = (unsigned)std::min<int64_t>((nv + block - 1) / block, 152 * 16);
+    int dev = 0, sms = 0;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err == cudaSuccess) err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (err != cudaSuccess) return err;
+    const int64_t cap = 16 * (int64_t)std::max(sms, 1);
+    const unsigned ge = (unsigned)std::min<int64_t>((ne + block - 1) / block, cap);
+    const unsigned gv = (unsigned)std::min<int64_t>((nv + block - 1) / block, cap);
     T* y = static_cast<T*>(scratch);
     if (ne > 0)
         static_edge_kernel<T, VK, EK, CHECK><<<ge, block, 0, s>>>(nv, ne, src, dst, static_cast<const T*>(u),
