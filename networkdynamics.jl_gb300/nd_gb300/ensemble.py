@@ -154,6 +154,10 @@ class Ensemble:
         if resume:
             if snapshot.control.shape != (self.n, 3):
                 raise capi.ArgumentError(capi.ND_ERR_ARG, f"snapshot control must have shape ({self.n}, 3)")
+            if np.any(snapshot.control[:, 0] != snapshot.control[0, 0]):
+                # an instance that stopped early (step budget, step underflow) has no state at
+                # the snapshot time
+                raise capi.ArgumentError(capi.ND_ERR_ARG, "snapshot instances ended at different times")
             control = torch.from_numpy(np.ascontiguousarray(snapshot.control, dtype=np.float64)).to(dev)
         elif snapshot:
             control = torch.zeros((self.n, 3), dtype=torch.float64, device=dev)
