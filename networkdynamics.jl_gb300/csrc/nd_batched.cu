@@ -160,6 +160,58 @@ __device__ __forceinline__ T thread_row_sum(const T* __restrict__ y2, const int3
     return sizeof(T) == 4 ? A::sub(acc, comp) : acc;
 }
 
+// The same sum for the long thread rows of dense networks (FP64): batches of 32 terms, the
+// next batch's values and the term indices of the one after that in flight while the current
+// batch is added.  Dense graphs have few rows, each a long serial chain, so every exposed
+// round trip lengthens the whole row phase; the extra registers cost no occupancy there.
+template <typename T>
+__device__ __forceinline__ T thread_row_sum_deep(const T* __restrict__ y2, const int32_t* __restrict__ idx, int n) {
+    using A = Arith<T>;
+    constexpr int kB = 32;
+    const bool kahan = sizeof(T) == 4 && n > kLightMaxDeg;
+    T acc = T(0), comp = T(0);
+    int ia[kB], ib[kB];
+    T cur[kB], nxt[kB];
+    auto load_idx = [&](int j0, int (&ix)[kB]) {
+#pragma unroll
+        for (int k = 0; k < kB; ++k) ix[k] = j0 + k < n ? __ldg(idx + j0 + k) : 0;
+    };
+    auto load_val = [&](int j0, const int (&ix)[kB], T (&t)[kB]) {
+#pragma unroll
+        for (int k = 0; k < kB; ++k) t[k] = j0 + k < n ? __ldg(y2 + ix[k]) : T(0);
+    };
+    load_idx(0, ia);
+    load_val(0, ia, cur);
+    load_idx(kB, ib);
+    for (int j0 = 0; j0 < n; j0 += kB) {
+        load_val(j0 + kB, ib, nxt);
+        load_idx(j0 + 2 * kB, ia);
+        const int lim = __reduce_max_sync(__activemask(), (unsigned)min(kB, n - j0));
+#pragma unroll
+        for (int k = 0; k < kB; ++k) {
+            if (k >= lim) break;
+            if (j0 + k >= n) continue;
+            if (sizeof(T) == 8 && j0 + k == 0) {
+                const double t0 = (double)cur[0];
+                acc = (T)((__double_as_longlong(t0) << 1) == 0 ? 0.0 : t0);
+            } else if (kahan) {
+                const T yk = A::sub(cur[k], comp);
+                const T s2 = A::add(acc, yk);
+                comp = A::sub(A::sub(s2, acc), yk);
+                acc = s2;
+            } else {
+                acc = A::add(acc, cur[k]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kB; ++k) {
+            cur[k] = nxt[k];
+            ib[k] = ia[k];
+        }
+    }
+    return sizeof(T) == 4 ? A::sub(acc, comp) : acc;
+}
+
 // Sum of a row's n terms by one warp (the result is valid in every lane).
 //   FP64 exact   the sequential sum, bit for bit: the terms are gathered tile by tile into
 //                shared memory and added by the windowed exact scan (256 terms per warp
@@ -249,30 +301,30 @@ __device__ __forceinline__ void batched_vertex_f(const BatchedKArgs& a, int64_t 
 // thread.  Blocks are small (kRowBlock threads) so that networks with few rows -- dense
 // graphs, whose long per-thread chains are the whole cost -- still spread over every SM.
 constexpr int kRowBlock = 64;
-constexpr int kRowWarps = kRowBlock / 32;
-template <typename T>
-__global__ void __launch_bounds__(kRowBlock) batched_row_kernel(BatchedKArgs a, int64_t n_warp_blocks) {
+template <typename T, bool kDense, int NT>
+__global__ void __launch_bounds__(NT) batched_row_kernel(BatchedKArgs a, int64_t n_warp_blocks) {
+    constexpr int kWarps = NT / 32;
     const T* __restrict__ y2 = static_cast<const T*>(a.y2);
     if ((int64_t)blockIdx.x < n_warp_blocks) {
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        const int64_t slot = (int64_t)blockIdx.x * kRowWarps + warp;
+        const int64_t slot = (int64_t)blockIdx.x * kWarps + warp;
         if (slot >= a.n_warp_rows) return;  // warp-uniform
         const uint32_t t0 = __ldg(a.tptr + slot);
         const int n = (int)(__ldg(a.tptr + slot + 1) - t0);
         T acc;
         if constexpr (sizeof(T) == 8) {
-            __shared__ double tiles[kRowWarps][kWarpTile];
+            __shared__ double tiles[kWarps][kWarpTile];
             acc = warp_row_sum<T>(y2, a.tidx + t0, n, lane, a.mode, tiles[warp]);
         } else {
             acc = warp_row_sum<T>(y2, a.tidx + t0, n, lane, a.mode, nullptr);
         }
         if (lane == 0) batched_vertex_f<T>(a, __ldg(a.slot_vpos + slot), acc);
     } else {
-        const int64_t slot = a.n_warp_rows + ((int64_t)blockIdx.x - n_warp_blocks) * kRowBlock + threadIdx.x;
+        const int64_t slot = a.n_warp_rows + ((int64_t)blockIdx.x - n_warp_blocks) * NT + threadIdx.x;
         if (slot >= a.nv) return;
         const uint32_t t0 = __ldg(a.tptr + slot);
         const int n = (int)(__ldg(a.tptr + slot + 1) - t0);
-        const T acc = thread_row_sum<T>(y2, a.tidx + t0, n);
+        const T acc = kDense ? thread_row_sum_deep<T>(y2, a.tidx + t0, n) : thread_row_sum<T>(y2, a.tidx + t0, n);
         batched_vertex_f<T>(a, __ldg(a.slot_vpos + slot), acc);
     }
 }
@@ -377,9 +429,14 @@ cudaError_t launch_typed(const BatchedNet& b, void* du, const void* u, const voi
         batched_edge_kernel<T><<<(unsigned)blocks, kBlock, 0, s>>>(a);
     }
     if (phases & kPhaseRow) {
-        const int64_t wb = (b.n_warp_rows + kRowWarps - 1) / kRowWarps;
-        const int64_t tb = (b.nv - b.n_warp_rows + kRowBlock - 1) / kRowBlock;
-        if (wb + tb > 0) batched_row_kernel<T><<<(unsigned)(wb + tb), kRowBlock, 0, s>>>(a, wb);
+        // dense networks: one-warp blocks, so that their few row warps reach as many SMs
+        const int nt = b.dense_rows ? 32 : kRowBlock;
+        const int64_t wb = (b.n_warp_rows + nt / 32 - 1) / (nt / 32);
+        const int64_t tb = (b.nv - b.n_warp_rows + nt - 1) / nt;
+        if (wb + tb > 0) {
+            if (b.dense_rows) batched_row_kernel<T, true, 32><<<(unsigned)(wb + tb), 32, 0, s>>>(a, wb);
+            else batched_row_kernel<T, false, kRowBlock><<<(unsigned)(wb + tb), kRowBlock, 0, s>>>(a, wb);
+        }
     }
     return cudaGetLastError();
 }
@@ -646,6 +703,13 @@ int build_batched(const nd_batched_network_desc* d, int elem, BatchedNet* out) {
     bn.max_degree = (int32_t)maxdeg;
     bn.depth = depth;
     bn.n_warp_rows = (int64_t)longr.size();
+    {
+        // FP64 thread rows longer than kLightMaxDeg carrying most of the thread-row terms: a
+        // dense network, whose row kernel takes the deep batches of thread_row_sum_deep
+        int64_t inc_long = 0, inc_short = 0;
+        for (int32_t v : shortr) (deg[v] > (uint32_t)kLightMaxDeg ? inc_long : inc_short) += deg[v];
+        bn.dense_rows = elem == 8 && inc_long > inc_short;
+    }
     auto upload = [&](void** dptr, const void* hptr, size_t bytes) -> cudaError_t {
         cudaError_t err = cudaMalloc(dptr, std::max<size_t>(bytes, 16));
         if (err != cudaSuccess) return err;

@@ -279,6 +279,10 @@ int build_topology(int64_t nv, int64_t ne, const int64_t* src, const int64_t* ds
             free_topology(&t);
             return cuda_fail(err, "upload of the edge-centric layout");
         }
+        int64_t inc_medium = 0, inc_light = 0;
+        for (int32_t v : medium) inc_medium += deg[v];
+        for (int32_t v : light) inc_light += deg[v];
+        el.dense_rows = inc_medium > inc_light;
         el.enabled = true;
     }
     *topo = t;
@@ -590,6 +594,7 @@ int nd_rhs(nd_handle* h, int dtype, void* du, int64_t n_du, const void* u, int64
     a.ybkt = el.ybkt;
     a.heavy_only = 0;
     a.heavy_separate = 0;
+    a.dense_rows = el.dense_rows ? 1 : 0;
     const bool edge = el.enabled && h->edge_path;
     const bool split = h->topo.n_heavy > 0;  // heavy rows: their own kernel, on the side stream
     a.heavy_separate = split ? 1 : 0;

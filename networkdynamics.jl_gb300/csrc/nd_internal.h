@@ -116,6 +116,9 @@ struct EdgeLayout {
     // multiple of 4 entries (padding entries hold 0), so they load as 16-byte vectors
     int32_t* locp = nullptr;
     void* y = nullptr;         // [ne + 2] scratch, element type of the handle (+2: pair loads)
+    // rows of degree 33..kMediumMaxDeg carry most of the incidences (a dense graph): the
+    // row phase takes its dense-network kernel
+    bool dense_rows = false;
     void* ybkt = nullptr;      // [ne] scratch
 };
 
@@ -169,6 +172,7 @@ struct RhsArgs {
     const int32_t* locp;
     void* y;
     void* ybkt;
+    int32_t dense_rows;  // the row phase runs dense_row_kernel (see EdgeLayout::dense_rows)
 };
 
 // Launch the fused RHS for the given element type.
@@ -230,6 +234,7 @@ struct BatchedNet {
     int32_t max_degree = 0;
     int32_t depth = 1;           // output dimension of vertices and edge sides (2: complex)
     int64_t n_warp_rows = 0;     // slots [0, n_warp_rows): the long rows, a warp per row
+    bool dense_rows = false;     // FP64 thread rows in deep batches (a dense network)
     int2* eu = nullptr;          // [ne] by edge position: u indices of the src / dst vertex outputs
     uint32_t* tptr = nullptr;    // [nv+1] by slot: range of the slot's terms in tidx
     int32_t* tidx = nullptr;     // [2ne] y2 indices of every row's terms, ascending

@@ -217,6 +217,110 @@ __global__ void __launch_bounds__(kBlock, 5) row_phase_kernel(RhsArgs a) {
     vertex_f<T, VK>(static_cast<T*>(a.du), static_cast<const T*>(a.u), static_cast<const T*>(a.p), v, acc);
 }
 
+// ---- phase R on dense networks: rows of hundreds of terms ------------------------------------
+// When the medium rows carry most of the incidences (dense graphs such as the reference's
+// diffusion benchmark on WS(3000, 1500)), there are few rows and each is a long serial chain:
+// 3000 rows fill 94 warps, and a row waits one memory round trip per batch of terms.  Here a
+// thread still sums one row in the same order (the same bits), but its terms come in batches
+// of 32, with the values of the next batch and the destination-side positions of the one
+// after that in flight while the current batch is added, and one-warp blocks spread the few
+// warps over as many SMs as there are warps.
+constexpr int kDenseBlock = 32;
+
+// Sequential sum of n terms in batches of KB, the next batch's loads in flight while the
+// current one is added.  load(j0, t) fills t with terms j0 .. j0 + KB - 1 (0 past the end);
+// add(t) adds one term.  The adds of a batch stop at the longest remaining run in the warp.
+template <typename T, int KB, typename Load, typename Add>
+__device__ __forceinline__ void pipelined_sum(int n, Load&& load, Add&& add) {
+    T cur[KB], nxt[KB];
+    load(0, cur);
+    for (int j0 = 0; j0 < n; j0 += KB) {
+        load(j0 + KB, nxt);
+        const int lim = __reduce_max_sync(__activemask(), (unsigned)min(KB, n - j0));
+#pragma unroll
+        for (int k = 0; k < KB; ++k) {
+            if (k >= lim) break;
+            if (j0 + k < n) add(j0 + k, cur[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < KB; ++k) cur[k] = nxt[k];
+    }
+}
+
+template <typename T, int VK>
+__global__ void __launch_bounds__(kDenseBlock) dense_row_kernel(RhsArgs a) {
+    using A = Arith<T>;
+    constexpr int KB = 32;
+    const int64_t slot = (int64_t)a.n_heavy + (int64_t)blockIdx.x * kDenseBlock + threadIdx.x;
+    if (slot >= a.nv) return;
+    const T* __restrict__ y = static_cast<const T*>(a.y);
+    const T* __restrict__ ybkt = static_cast<const T*>(a.ybkt);
+    const uint64_t stream = policy_evict_first();
+    const int4 rm = ld_hint(a.rmeta + slot, stream);
+    const int64_t v = rm.x;
+    const int32_t lp = rm.y;  // multiple of 4
+    const uint32_t sp = (uint32_t)rm.z;
+    const int nd = rm.w & 0xffff;
+    const int ns = (int)((uint32_t)rm.w >> 16);
+    const bool kahan = sizeof(T) == 4 && nd + ns > kLightMaxDeg;
+    T acc = T(0), comp = T(0);
+    auto add = [&](T term) {
+        if (kahan) {
+            const T yk = A::sub(term, comp);
+            const T s2 = A::add(acc, yk);
+            comp = A::sub(A::sub(s2, acc), yk);
+            acc = s2;
+        } else {
+            acc = A::add(acc, term);
+        }
+    };
+    // destination side: positions in locp, values in ybkt
+    {
+        int pos[KB];
+        auto load_pos = [&](int j0) {
+#pragma unroll
+            for (int k4 = 0; k4 < KB / 4; ++k4) {
+                const int4 q = j0 + 4 * k4 < nd
+                                   ? ld_hint(reinterpret_cast<const int4*>(a.locp + lp + j0) + k4, stream)
+                                   : int4{0, 0, 0, 0};
+                pos[4 * k4] = q.x;
+                pos[4 * k4 + 1] = q.y;
+                pos[4 * k4 + 2] = q.z;
+                pos[4 * k4 + 3] = q.w;
+            }
+        };
+        load_pos(0);
+        pipelined_sum<T, KB>(
+            nd,
+            [&](int j0, T (&t)[KB]) {
+#pragma unroll
+                for (int k = 0; k < KB; ++k) t[k] = j0 + k < nd ? ld_hint(ybkt + pos[k], stream) : T(0);
+                load_pos(j0 + KB);  // the positions of the batch after
+            },
+            [&](int j, T t) {
+                if constexpr (sizeof(T) == 8) {
+                    if (j == 0) acc = (T)((__double_as_longlong((double)t) << 1) == 0 ? 0.0 : (double)t);
+                    else acc = __dadd_rn(acc, t);
+                } else {
+                    add(t);
+                }
+            });
+    }
+    // source side: the row's own block of y
+    pipelined_sum<T, KB>(
+        ns,
+        [&](int j0, T (&t)[KB]) {
+#pragma unroll
+            for (int k = 0; k < KB; ++k) t[k] = j0 + k < ns ? ld_hint(y + sp + (uint32_t)(j0 + k), stream) : T(0);
+        },
+        [&](int, T t) {
+            if constexpr (sizeof(T) == 8) acc = __dsub_rn(acc, t);
+            else add(-t);
+        });
+    if constexpr (sizeof(T) == 4) acc = A::sub(acc, comp);
+    vertex_f<T, VK>(static_cast<T*>(a.du), static_cast<const T*>(a.u), static_cast<const T*>(a.p), v, acc);
+}
+
 template <typename T, int VK, int EK>
 cudaError_t launch_typed(const RhsArgs& a, cudaStream_t s, int phases) {
     if ((phases & kPhaseEdge) && a.n_chunks > 0)
@@ -224,7 +328,10 @@ cudaError_t launch_typed(const RhsArgs& a, cudaStream_t s, int phases) {
     // rows below the heavy ones; every summation order adds them sequentially
     const int64_t rows = a.nv - a.n_heavy;
     if (!(phases & kPhaseRow) || rows <= 0) return cudaGetLastError();
-    row_phase_kernel<T, VK><<<(unsigned)((rows + kBlock - 1) / kBlock), kBlock, 0, s>>>(a);
+    if (a.dense_rows)
+        dense_row_kernel<T, VK><<<(unsigned)((rows + kDenseBlock - 1) / kDenseBlock), kDenseBlock, 0, s>>>(a);
+    else
+        row_phase_kernel<T, VK><<<(unsigned)((rows + kBlock - 1) / kBlock), kBlock, 0, s>>>(a);
     return cudaGetLastError();
 }
 
