@@ -321,6 +321,39 @@ __global__ void __launch_bounds__(kDenseBlock) dense_row_kernel(RhsArgs a) {
     vertex_f<T, VK>(static_cast<T*>(a.du), static_cast<const T*>(a.u), static_cast<const T*>(a.p), v, acc);
 }
 
+// FP32 rows of dense networks carry no order to keep: a warp takes each row, its lanes add
+// every 32nd term with Kahan compensation, and a butterfly joins the lane sums (as the FP32
+// heavy rows and the batched path's long FP32 rows do).  Positions and source blocks load
+// coalesced across the lanes.
+template <int VK>
+__global__ void __launch_bounds__(kBlock) dense_warp_row_kernel(RhsArgs a) {
+    using A = Arith<float>;
+    const int lane = threadIdx.x & 31;
+    const int64_t slot = (int64_t)a.n_heavy + (int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (slot >= a.nv) return;  // warp-uniform
+    const float* __restrict__ y = static_cast<const float*>(a.y);
+    const float* __restrict__ ybkt = static_cast<const float*>(a.ybkt);
+    const uint64_t stream = policy_evict_first();
+    const int4 rm = ld_hint(a.rmeta + slot, stream);
+    const int nd = rm.w & 0xffff;
+    const int n = nd + (int)((uint32_t)rm.w >> 16);
+    float acc = 0.f, comp = 0.f;
+    for (int j = lane; j < n; j += 32) {
+        const float term = j < nd ? ld_hint(ybkt + ld_hint(a.locp + rm.y + j, stream), stream)
+                                  : -ld_hint(y + (uint32_t)rm.z + (uint32_t)(j - nd), stream);
+        const float yk = A::sub(term, comp);
+        const float s2 = A::add(acc, yk);
+        comp = A::sub(A::sub(s2, acc), yk);
+        acc = s2;
+    }
+    acc = A::sub(acc, comp);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc = A::add(acc, __shfl_xor_sync(kFull, acc, off));
+    if (lane == 0)
+        vertex_f<float, VK>(static_cast<float*>(a.du), static_cast<const float*>(a.u), static_cast<const float*>(a.p),
+                            rm.x, acc);
+}
+
 template <typename T, int VK, int EK>
 cudaError_t launch_typed(const RhsArgs& a, cudaStream_t s, int phases) {
     if ((phases & kPhaseEdge) && a.n_chunks > 0)
@@ -328,7 +361,9 @@ cudaError_t launch_typed(const RhsArgs& a, cudaStream_t s, int phases) {
     // rows below the heavy ones; every summation order adds them sequentially
     const int64_t rows = a.nv - a.n_heavy;
     if (!(phases & kPhaseRow) || rows <= 0) return cudaGetLastError();
-    if (a.dense_rows)
+    if (a.dense_rows && sizeof(T) == 4)
+        dense_warp_row_kernel<VK><<<(unsigned)((rows + kWarpsPerBlock - 1) / kWarpsPerBlock), kBlock, 0, s>>>(a);
+    else if (a.dense_rows)
         dense_row_kernel<T, VK><<<(unsigned)((rows + kDenseBlock - 1) / kDenseBlock), kDenseBlock, 0, s>>>(a);
     else
         row_phase_kernel<T, VK><<<(unsigned)((rows + kBlock - 1) / kBlock), kBlock, 0, s>>>(a);
