@@ -57,6 +57,29 @@ def rhs(nv=10_000_000, m=4, dtype="f64", calls=8, seed=1):
             "checksum": float(du.double().sum().item())}
 
 
+def dense(nv=3000, dtype="f64", calls=8):
+    """A few calls of the reference's dense diffusion benchmark network, diffusion_static_edge
+    (benchmark/benchmark_cases.jl): WS(nv, nv/2, 0) with unit diffusion edges, N(0, 1) states
+    -- rows of nv/2 terms, summed by the dense-network row kernels.  The short program that
+    per-kernel profiler captures run; reports the mean wall time of the calls."""
+    import torch
+    import nd_gb300 as nd
+    td = {"f64": torch.float64, "f32": torch.float32}[dtype]
+    g = nd.watts_strogatz(nv, nv // 2, 0.0, seed=1)
+    nw = nd.adapt(nd.Network(g, nd.diffusion_vertex(), nd.diffusion_edge_unit()), td)
+    u = torch.from_numpy(np.random.default_rng(2).normal(size=nw.dim)).to("cuda", td)
+    du = torch.empty_like(u)
+    nw(du, u, None, 0.0)
+    _sync()
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        nw(du, u, None, 0.0)
+    _sync()
+    return {"workload": f"diffusion_static_edge, WS({nv}, {nv // 2}, 0), {dtype.upper()} RHS", "ne": g.ne,
+            "calls": calls, "ms_per_call_wall": 1e3 * (time.perf_counter() - t0) / calls,
+            "checksum": float(du.double().sum().item())}
+
+
 def warmstart(n_train=20000, n_test=2000, nv=2000, m=2, layers=4, epochs=80, batch=64, lr=2e-3, lr_final=5e-5,
               seed=0, tol=1e-10):
     """Swing steady states on BA(nv, m): solve n_train + n_test instances from the cold
@@ -352,7 +375,7 @@ def fixpoint(nv=1_000_000, m=2, seed=0):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("which", choices=["rhs", "warmstart", "ensemble", "swing", "jacobian", "fixpoint"])
+    ap.add_argument("which", choices=["rhs", "dense", "warmstart", "ensemble", "swing", "jacobian", "fixpoint"])
     ap.add_argument("--dtype", choices=["f64", "f32"], default="f64")
     ap.add_argument("--calls", type=int, default=8)
     ap.add_argument("--train", type=int, default=20000)
@@ -365,6 +388,8 @@ def main():
     a = ap.parse_args()
     if a.which == "rhs":
         r = rhs(a.nv or 10_000_000, dtype=a.dtype, calls=a.calls)
+    elif a.which == "dense":
+        r = dense(a.nv or 3000, dtype=a.dtype, calls=a.calls)
     elif a.which == "warmstart":
         r = warmstart(a.train, a.test, a.nv or 2000, epochs=a.epochs)
     elif a.which == "ensemble":
