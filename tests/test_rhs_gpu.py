@@ -344,3 +344,25 @@ def test_execution_options_reach_the_handle(cuda):
     got = gpu_rhs(tree, u, p, cuda, np.float64)
     # a hub of n terms summed in two orders differs by at most about n·eps·Σ|terms| (n < 4500)
     assert np.all(np.abs(got - ref) <= 1e-12 * on.abs_terms(u, p))
+
+
+@pytest.mark.parametrize("vk,ek", [(O.V_SWING, O.E_KURAMOTO), (O.V_KURAMOTO, O.E_DIFFUSION)])
+def test_dense_network_rows(cuda, vk, ek):
+    """A dense graph (rows of ~900 terms carry every incidence) takes the dense-network row
+    kernels: FP64 gives the fused layout's bits and the oracle within the sine bound, FP32
+    (a warp per row) stays within the FP32 bound."""
+    g = nd.watts_strogatz(1800, 900, 0.1, seed=21)
+    assert g.degree().min() > 32
+    on = O.OracleNetwork.from_graph(g, vk, ek)
+    u, p = random_inputs(on, vk, np.random.default_rng(21))
+    nw = make(g, vk, ek, np.float64)
+    got = gpu_rhs(nw, u, p, cuda, np.float64)
+    nw.set_layout("fused")
+    np.testing.assert_array_equal(gpu_rhs(nw, u, p, cuda, np.float64), got)
+    check_f64(got, on.rhs(u, p), on.abs_terms(u, p), exact=ek != O.E_KURAMOTO)
+    nw32 = make(g, vk, ek, np.float32)
+    u32, p32 = u.astype(np.float32), p.astype(np.float32)
+    got32 = gpu_rhs(nw32, u32, p32, cuda, np.float32).astype(np.float64)
+    ref = on.rhs(u32.astype(np.float64), p32.astype(np.float64))
+    terms = on.abs_terms(u32.astype(np.float64), p32.astype(np.float64))
+    assert np.all(np.abs(got32 - ref) <= 4e-6 * (terms + np.abs(ref)))
