@@ -283,6 +283,9 @@ int build_topology(int64_t nv, int64_t ne, const int64_t* src, const int64_t* ds
         for (int32_t v : medium) inc_medium += deg[v];
         for (int32_t v : light) inc_light += deg[v];
         el.dense_rows = inc_medium > inc_light;
+        int32_t nw32 = 0;  // medium rows are sorted by degree, longest first
+        while (nw32 < (int32_t)medium.size() && deg[medium[nw32]] >= (uint32_t)kWarpRowMinF32) ++nw32;
+        el.n_warp_f32 = nw32;
         el.enabled = true;
     }
     *topo = t;
@@ -595,6 +598,7 @@ int nd_rhs(nd_handle* h, int dtype, void* du, int64_t n_du, const void* u, int64
     a.heavy_only = 0;
     a.heavy_separate = 0;
     a.dense_rows = el.dense_rows ? 1 : 0;
+    a.n_warp_f32 = el.n_warp_f32;
     const bool edge = el.enabled && h->edge_path;
     const bool split = h->topo.n_heavy > 0;  // heavy rows: their own kernel, on the side stream
     a.heavy_separate = split ? 1 : 0;

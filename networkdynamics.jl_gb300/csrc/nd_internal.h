@@ -77,6 +77,7 @@ inline int edge_outdim(int ek) { return ek == ND_E_PILINE ? 2 : 1; }
 constexpr int kLightMaxDeg = 32;
 constexpr int kMediumMaxDeg = 2048;
 constexpr int kWindow = 256;
+constexpr int kWarpRowMinF32 = 128;  // FP32 rows at least this long take a warp in the row phase
 constexpr int kLightRun = 128;
 
 // Device-resident topology of one network.
@@ -119,6 +120,7 @@ struct EdgeLayout {
     // rows of degree 33..kMediumMaxDeg carry most of the incidences (a dense graph): the
     // row phase takes its dense-network kernel
     bool dense_rows = false;
+    int32_t n_warp_f32 = 0;  // medium rows of at least kWarpRowMinF32 terms (the first medium slots)
     void* ybkt = nullptr;      // [ne] scratch
 };
 
@@ -173,6 +175,7 @@ struct RhsArgs {
     void* y;
     void* ybkt;
     int32_t dense_rows;  // the row phase runs dense_row_kernel (see EdgeLayout::dense_rows)
+    int32_t n_warp_f32;  // FP32: the first medium slots with >= kWarpRowMinF32 terms, a warp each
 };
 
 // Launch the fused RHS for the given element type.
@@ -234,7 +237,8 @@ struct BatchedNet {
     int32_t max_degree = 0;
     int32_t depth = 1;           // output dimension of vertices and edge sides (2: complex)
     int64_t n_warp_rows = 0;     // slots [0, n_warp_rows): the long rows, a warp per row
-    bool dense_rows = false;     // FP64 thread rows in deep batches (a dense network)
+    bool dense_rows = false;
+    int32_t n_warp_f32 = 0;  // medium rows of at least kWarpRowMinF32 terms (the first medium slots)     // FP64 thread rows in deep batches (a dense network)
     int2* eu = nullptr;          // [ne] by edge position: u indices of the src / dst vertex outputs
     uint32_t* tptr = nullptr;    // [nv+1] by slot: range of the slot's terms in tidx
     int32_t* tidx = nullptr;     // [2ne] y2 indices of every row's terms, ascending

@@ -114,6 +114,44 @@ __global__ void __launch_bounds__(kBlock) edge_phase_kernel(RhsArgs a) {
     }
 }
 
+// ---- FP32 rows of many terms: a warp per row ----------------------------------------------
+// FP32 rows carry no order to keep: the lanes of a warp add every 32nd term of the row with
+// Kahan compensation and a butterfly joins the lane sums (as the FP32 heavy rows and the
+// batched path's long FP32 rows do).  Positions and source blocks load coalesced across the
+// lanes.  Used for every row of a dense network and for the medium rows of any other.
+template <int VK>
+__device__ __forceinline__ void warp_row_f32(const RhsArgs& a, int64_t slot) {
+    using A = Arith<float>;
+    const int lane = threadIdx.x & 31;
+    const float* __restrict__ y = static_cast<const float*>(a.y);
+    const float* __restrict__ ybkt = static_cast<const float*>(a.ybkt);
+    const uint64_t stream = policy_evict_first();
+    const int4 rm = ld_hint(a.rmeta + slot, stream);
+    const int nd = rm.w & 0xffff;
+    const int n = nd + (int)((uint32_t)rm.w >> 16);
+    float acc = 0.f, comp = 0.f;
+    for (int j = lane; j < n; j += 32) {
+        const float term = j < nd ? ld_hint(ybkt + ld_hint(a.locp + rm.y + j, stream), stream)
+                                  : -ld_hint(y + (uint32_t)rm.z + (uint32_t)(j - nd), stream);
+        const float yk = A::sub(term, comp);
+        const float s2 = A::add(acc, yk);
+        comp = A::sub(A::sub(s2, acc), yk);
+        acc = s2;
+    }
+    acc = A::sub(acc, comp);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc = A::add(acc, __shfl_xor_sync(kFull, acc, off));
+    if (lane == 0)
+        vertex_f<float, VK>(static_cast<float*>(a.du), static_cast<const float*>(a.u), static_cast<const float*>(a.p),
+                            rm.x, acc);
+}
+
+template <int VK>
+__global__ void __launch_bounds__(kBlock) dense_warp_row_kernel(RhsArgs a) {
+    const int64_t slot = (int64_t)a.n_heavy + (int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (slot < a.nv) warp_row_f32<VK>(a, slot);  // warp-uniform
+}
+
 // ---- phase R: a thread per row, reading the row's terms from global memory -------------------
 // Rows of degree up to kMediumMaxDeg, in slot order: medium rows sorted by degree over all
 // of them, light rows sorted by degree inside runs of consecutive vertices, so the 32 rows
@@ -128,11 +166,9 @@ template <typename T, int VK>
 // 327 µs against 349 µs at the 64 registers the kernel takes uncapped (4 blocks), 374-390 µs
 // with 8-term batches at 5-6 blocks, 351 µs with 16-term batches at 4; FP32: 252 µs against
 // 309-451 µs with 8-term batches at 6-8 blocks.
-__global__ void __launch_bounds__(kBlock, 5) row_phase_kernel(RhsArgs a) {
+__device__ __forceinline__ void row_thread(const RhsArgs& a, int64_t slot) {
     using A = Arith<T>;
     constexpr int kBatch = 12;
-    const int64_t slot = (int64_t)a.n_heavy + (int64_t)blockIdx.x * kBlock + threadIdx.x;
-    if (slot >= a.nv) return;
     const T* __restrict__ y = static_cast<const T*>(a.y);
     const T* __restrict__ ybkt = static_cast<const T*>(a.ybkt);
     const uint64_t stream = policy_evict_first();
@@ -215,6 +251,31 @@ __global__ void __launch_bounds__(kBlock, 5) row_phase_kernel(RhsArgs a) {
     }
     if constexpr (sizeof(T) == 4) acc = A::sub(acc, comp);
     vertex_f<T, VK>(static_cast<T*>(a.du), static_cast<const T*>(a.u), static_cast<const T*>(a.p), v, acc);
+}
+
+template <typename T, int VK>
+__global__ void __launch_bounds__(kBlock, 5) row_phase_kernel(RhsArgs a) {
+    const int64_t slot = (int64_t)a.n_heavy + (int64_t)blockIdx.x * kBlock + threadIdx.x;
+    if (slot < a.nv) row_thread<T, VK>(a, slot);
+}
+
+// FP32 row phase when some rows have at least kWarpRowMinF32 terms: those rows (the first
+// n_warp_f32 medium slots, sorted by degree) take a warp each in the first blocks, the rest a
+// thread each, in one launch.  Per thread, such a row is a chain of one memory round trip per
+// 12 terms that outlasts every other row: on BA(1e5, 2) swing (rows up to 935 terms) the row
+// phase took 57.8 µs with a thread per row and 9.9 µs with a warp per medium row.  Shorter
+// rows keep a thread: giving all 170K medium rows of BA(1e7, 4) a warp each (most have 33 to
+// 100 terms) made its row phase 302 µs against 250.
+template <int VK>
+__global__ void __launch_bounds__(kBlock, 5) row_phase_f32_kernel(RhsArgs a) {
+    const int64_t nb_w = ((int64_t)a.n_warp_f32 + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    if ((int64_t)blockIdx.x < nb_w) {
+        const int64_t r = (int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+        if (r < a.n_warp_f32) warp_row_f32<VK>(a, a.n_heavy + r);  // warp-uniform
+        return;
+    }
+    const int64_t slot = (int64_t)a.n_heavy + a.n_warp_f32 + ((int64_t)blockIdx.x - nb_w) * kBlock + threadIdx.x;
+    if (slot < a.nv) row_thread<float, VK>(a, slot);
 }
 
 // ---- phase R on dense networks: rows of hundreds of terms ------------------------------------
@@ -321,39 +382,6 @@ __global__ void __launch_bounds__(kDenseBlock) dense_row_kernel(RhsArgs a) {
     vertex_f<T, VK>(static_cast<T*>(a.du), static_cast<const T*>(a.u), static_cast<const T*>(a.p), v, acc);
 }
 
-// FP32 rows of dense networks carry no order to keep: a warp takes each row, its lanes add
-// every 32nd term with Kahan compensation, and a butterfly joins the lane sums (as the FP32
-// heavy rows and the batched path's long FP32 rows do).  Positions and source blocks load
-// coalesced across the lanes.
-template <int VK>
-__global__ void __launch_bounds__(kBlock) dense_warp_row_kernel(RhsArgs a) {
-    using A = Arith<float>;
-    const int lane = threadIdx.x & 31;
-    const int64_t slot = (int64_t)a.n_heavy + (int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
-    if (slot >= a.nv) return;  // warp-uniform
-    const float* __restrict__ y = static_cast<const float*>(a.y);
-    const float* __restrict__ ybkt = static_cast<const float*>(a.ybkt);
-    const uint64_t stream = policy_evict_first();
-    const int4 rm = ld_hint(a.rmeta + slot, stream);
-    const int nd = rm.w & 0xffff;
-    const int n = nd + (int)((uint32_t)rm.w >> 16);
-    float acc = 0.f, comp = 0.f;
-    for (int j = lane; j < n; j += 32) {
-        const float term = j < nd ? ld_hint(ybkt + ld_hint(a.locp + rm.y + j, stream), stream)
-                                  : -ld_hint(y + (uint32_t)rm.z + (uint32_t)(j - nd), stream);
-        const float yk = A::sub(term, comp);
-        const float s2 = A::add(acc, yk);
-        comp = A::sub(A::sub(s2, acc), yk);
-        acc = s2;
-    }
-    acc = A::sub(acc, comp);
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) acc = A::add(acc, __shfl_xor_sync(kFull, acc, off));
-    if (lane == 0)
-        vertex_f<float, VK>(static_cast<float*>(a.du), static_cast<const float*>(a.u), static_cast<const float*>(a.p),
-                            rm.x, acc);
-}
-
 template <typename T, int VK, int EK>
 cudaError_t launch_typed(const RhsArgs& a, cudaStream_t s, int phases) {
     if ((phases & kPhaseEdge) && a.n_chunks > 0)
@@ -365,6 +393,10 @@ cudaError_t launch_typed(const RhsArgs& a, cudaStream_t s, int phases) {
         dense_warp_row_kernel<VK><<<(unsigned)((rows + kWarpsPerBlock - 1) / kWarpsPerBlock), kBlock, 0, s>>>(a);
     else if (a.dense_rows)
         dense_row_kernel<T, VK><<<(unsigned)((rows + kDenseBlock - 1) / kDenseBlock), kDenseBlock, 0, s>>>(a);
+    else if (sizeof(T) == 4 && a.n_warp_f32 > 0)
+        row_phase_f32_kernel<VK><<<(unsigned)((a.n_warp_f32 + kWarpsPerBlock - 1) / kWarpsPerBlock +
+                                              (rows - a.n_warp_f32 + kBlock - 1) / kBlock),
+                                   kBlock, 0, s>>>(a);
     else
         row_phase_kernel<T, VK><<<(unsigned)((rows + kBlock - 1) / kBlock), kBlock, 0, s>>>(a);
     return cudaGetLastError();
