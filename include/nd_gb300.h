@@ -340,8 +340,8 @@ int nd_solve_rodas4(nd_handle* h, double* u, const double* p, const double* mass
  * device arrays and are not checked.  Another order still gives the network's RHS, but its
  * sums run in that order, not the reference's.
  * Result: the same du as nd_rhs on the same network: in FP64 bit for bit; in FP32 bit for
- * bit on every row of degree <= 2048 (rows longer than 32 with Kahan compensation, as in
- * nd_rhs), within the FP32 rounding on longer rows, which nd_rhs sums with a warp tree.
+ * bit on every row of fewer than 128 terms (rows longer than 32 with Kahan compensation,
+ * as in nd_rhs), within the FP32 rounding on longer rows, which nd_rhs sums a warp per row.
  * ne above the scratch size returns
  * ND_ERR_ARG.  The first call on a device looks up the scratch array's device address
  * (cudaGetSymbolAddress, with that device current) and should come before any stream

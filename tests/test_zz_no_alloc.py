@@ -80,9 +80,9 @@ def test_static_scratch_rhs_matches_nd_rhs(cuda, vk, ek, make_vm, make_em):
             else:
                 dd = np.abs(got.cpu().numpy() - want)
                 assert np.all((dd <= 1e-13 * np.abs(want)) | (dd <= 1e-13 * on.abs_terms(u_h, p_h)))
-    # FP32: the bits of nd_rhs on every row of degree <= 2048 (both compensate rows longer
-    # than 32); within the FP32 tolerance of the parity tests on the longer rows, which
-    # nd_rhs sums with a warp tree
+    # FP32: the bits of nd_rhs on every row of fewer than 128 terms (both add them in order,
+    # compensating rows longer than 32); within the FP32 tolerance of the parity tests on the
+    # longer rows, which nd_rhs sums a warp per row
     nw32 = nd.adapt(nd.Network(g, make_vm(), make_em()), torch.float32)
     u32 = u.float()
     p32 = p.float()
@@ -91,7 +91,7 @@ def test_static_scratch_rhs_matches_nd_rhs(cuda, vk, ek, make_vm, make_em):
     got32 = torch.empty_like(u32)
     capi.check(static_rhs(lib, vk, ek, g, dev_arrays, got32, u32, p32, capi.ND_F32))
     r32, g32 = ref32.cpu().numpy(), got32.cpu().numpy()
-    short = np.repeat(g.degree() <= 2048, nw.dim // g.nv)
+    short = np.repeat(g.degree() < 128, nw.dim // g.nv)
     assert short.sum() > 0.99 * len(short) and (~short).any()
     np.testing.assert_array_equal(g32[short], r32[short])
     terms = on.abs_terms(u32.double().cpu().numpy(), p32.double().cpu().numpy())
