@@ -219,3 +219,21 @@ def test_execution_options_are_checked_and_kept():
         nd.GB300Execution(layout="blocked")
     nw = nd.Network(nd.cycle_graph(5), nd.diffusion_vertex(), nd.diffusion_edge(), execution=ex)
     assert nw.execution is ex
+
+
+def test_ensemble_snapshot_files_round_trip(tmp_path):
+    """EnsembleSolveResult.save_snapshot / load_snapshot: state and step control as .npy
+    files, the snapshot time, and the refusal to save a solve without step control."""
+    import torch
+    from nd_gb300.ensemble import EnsembleSolveResult, load_snapshot
+    u = torch.arange(6, dtype=torch.float64)
+    control = torch.tensor([[2.0, 0.1, 1e-3], [2.0, 0.2, 2e-3]], dtype=torch.float64)
+    res = EnsembleSolveResult(u, torch.zeros(2, dtype=torch.int32), torch.tensor([5, 7]), control)
+    res.save_snapshot(tmp_path / "s")
+    snap = load_snapshot(tmp_path / "s")
+    np.testing.assert_array_equal(snap.u, u.numpy())
+    np.testing.assert_array_equal(snap.control, control.numpy())
+    assert snap.t == 2.0
+    np.testing.assert_array_equal(np.load(tmp_path / "s" / "nsteps.npy"), [5, 7])
+    with pytest.raises(nd.ArgumentError):
+        EnsembleSolveResult(u, None, None).save_snapshot(tmp_path / "t")
