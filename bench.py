@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--no-ensemble", action="store_true",
                     help="skip the basin-stability ensemble (FP32 vs FP64 solves/s) leg")
     ap.add_argument("--no-warmstart", action="store_true", help="skip the learned warm-start leg")
+    ap.add_argument("--no-dense", action="store_true", help="skip the reference's dense diffusion case")
     ap.add_argument("--cases", action="store_true",
                     help="instead of the headline workload: the reference's benchmark cases at their largest size, "
                          "one JSON line each")
@@ -277,6 +278,33 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def dense_case_leg(dev, steps=200):
+    """The reference's dense diffusion benchmark case (diffusion_static_edge at its largest N,
+    WS(3000, 1500): rows of 1500 terms), FP64 and FP32: device time per RHS over back-to-back
+    calls on resident buffers, as `bench.py --cases` times it."""
+    import torch
+
+    import nd_gb300 as nd
+    name, N = CASES[0]
+    g, vm, em = _case_networks(N, name)
+    net = nd.Network(g, vm, em)
+    u, p = case_inputs(name, net, g)
+    out = {"case": name, "N": N, "ne": g.ne, "steps": steps}
+    stream = torch.cuda.current_stream(dev)
+    for tag, dt in (("f64", torch.float64), ("f32", torch.float32)):
+        nw = nd.adapt(net, dt)
+        ut = torch.from_numpy(u).to(dev, dt)
+        pt = torch.from_numpy(p).to(dev, dt) if net.pdim else None
+        du = torch.empty_like(ut)
+        for _ in range(5):
+            nw(du, ut, pt, 0.0, stream=stream)
+        torch.cuda.synchronize(dev)
+        el = time_device(nw, du, ut, pt, steps, stream)
+        out[tag] = {"rhs_us": 1e6 * el / steps, "edges_per_s": g.ne * steps / el}
+        del nw, ut, pt, du
+    return out
+
+
 def time_device(nw, du, u, p, steps, stream):
     import torch
     start = torch.cuda.Event(enable_timing=True)
@@ -475,6 +503,11 @@ def run_gb300(args, rank, world, local):
         ok = np.array_equal(duh[(ke - 1) & 1].numpy(), dub[(ke - 1) & 1].cpu().numpy())
         line["e2e"]["result_matches_device"] = bool(ok)
     line["clocks"] = clk.summary()
+    if world == 1 and not args.no_dense:
+        try:
+            line["reference_dense_case"] = dense_case_leg(dev)
+        except Exception as exc:  # a secondary leg never costs the headline line
+            line["reference_dense_case"] = {"error": f"{type(exc).__name__}: {exc}"}
     # the second half of the headline metric: ensemble solves/s, FP32 vs FP64, and the
     # learned warm start (single-GPU runs; the instances are independent replicas)
     if world == 1 and not (args.no_ensemble and args.no_warmstart):
